@@ -1,0 +1,125 @@
+"""Build recipe for oracle/_ref: the UNMODIFIED reference library
+(kisupov/grns, src/*.cuh) compiled for the CPU as a checker.
+
+The reference is header-only CUDA C++.  Its host path compiles with g++ as
+is; its device path (`namespace cuda`) compiles with g++ through the host
+emulation in oracle/ref/shim/cuda_host_shim.h.  GMP/MPFR come from the
+system's libgmp.so.10 / libmpfr.so.6 through the prototype shims in
+oracle/ref/shim/ (the system has no GMP/MPFR headers).
+
+One shared library per moduli set.  A params header generated into
+oracle/_ref/ is pre-included ahead of the reference's src/params.h, whose
+include guard (GRNS_PARAMS_H) then skips the shipped default set; the tag
+"ref8" keeps the shipped default set instead.
+
+Reads the reference sources where they lie (default /root/reference, or
+$GRNS_REFERENCE); writes only into oracle/_ref/.  When the sources or the
+GMP/MPFR runtime libraries are absent (e.g. on a machine without the
+reference checkout) it builds nothing and says so.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from math import gcd
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+OUT = os.path.join(ORACLE, "_ref")
+REF = os.environ.get("GRNS_REFERENCE", "/root/reference")
+
+
+def greedy_moduli(n, start=2 ** 30 - 1):
+    """Pairwise-coprime odd integers taken greedily downward from `start`."""
+    out, c = [], start
+    while len(out) < n:
+        if c % 2 == 1 and all(gcd(c, m) == 1 for m in out):
+            out.append(c)
+        c -= 1
+    return out
+
+
+def floor_log2_product(moduli):
+    M = 1
+    for m in moduli:
+        M *= m
+    return M.bit_length() - 1
+
+
+# tag -> moduli (None = the reference's shipped src/params.h)
+SETS = {
+    "ref8": None,
+    "g8": greedy_moduli(8),
+    "g12": greedy_moduli(12),
+    "g32": greedy_moduli(32),
+    "g64": greedy_moduli(64),
+}
+
+
+def params_header(moduli):
+    n = len(moduli)
+    vals = ",".join(str(m) for m in moduli)
+    return f"""/* generated by oracle/ref/build_ref.py */
+#ifndef GRNS_PARAMS_H
+#define GRNS_PARAMS_H
+#define RNS_MODULI_SIZE ({n})
+#define RNS_MODULI_PRODUCT_LOG2 ({floor_log2_product(moduli)})
+#define RNS_P2_SCALING_THRESHOLD (30)
+#define RNS_EVAL_RELATIVE_ERROR (0.0000001)
+#define RNS_MODULI_VALUES {{{vals}}}
+constexpr int RNS_MODULI[RNS_MODULI_SIZE] = RNS_MODULI_VALUES;
+#define EMPLOY_STD_FMA false
+#endif
+"""
+
+
+def find_lib(name):
+    for d in ("/usr/lib/x86_64-linux-gnu", "/usr/lib/aarch64-linux-gnu", "/usr/lib64", "/usr/lib"):
+        p = os.path.join(d, name)
+        if os.path.exists(p):
+            return p
+    return None
+
+
+def build_one(tag, gmp, mpfr):
+    src = os.path.join(REF, "src")
+    out = os.path.join(OUT, f"libgrnsref_{tag}.so")
+    drv = os.path.join(HERE, "ref_driver.cpp")
+    cmd = ["g++", "-std=c++14", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-frounding-math",
+           "-w", "-include", os.path.join(HERE, "shim", "cuda_host_shim.h")]
+    if SETS[tag] is not None:
+        hdr = os.path.join(OUT, f"params_{tag}.h")
+        with open(hdr, "w") as f:
+            f.write(params_header(SETS[tag]))
+        cmd += ["-include", hdr]
+    cmd += ["-I", os.path.join(HERE, "shim"), "-I", src, drv, "-o", out, mpfr, gmp]
+    newest_input = max(os.path.getmtime(p) for p in [drv, os.path.abspath(__file__)] +
+                       [os.path.join(HERE, "shim", f) for f in os.listdir(os.path.join(HERE, "shim"))])
+    if os.path.exists(out) and os.path.getmtime(out) >= newest_input:
+        return out
+    subprocess.run(cmd, check=True)
+    return out
+
+
+def build(tags=None, quiet=False):
+    """Compile the checker libraries; returns {tag: path} (empty if unavailable)."""
+    if not os.path.isdir(os.path.join(REF, "src")):
+        if not quiet:
+            print(f"oracle/_ref: reference sources not found at {REF}; nothing built")
+        return {}
+    gmp, mpfr = find_lib("libgmp.so.10"), find_lib("libmpfr.so.6")
+    if not gmp or not mpfr:
+        if not quiet:
+            print("oracle/_ref: libgmp.so.10 / libmpfr.so.6 not found; nothing built")
+        return {}
+    os.makedirs(OUT, exist_ok=True)
+    tags = list(tags or SETS)
+    with ThreadPoolExecutor(len(tags)) as ex:
+        paths = list(ex.map(lambda t: build_one(t, gmp, mpfr), tags))
+    return dict(zip(tags, paths))
+
+
+if __name__ == "__main__":
+    res = build(sys.argv[1:] or None)
+    for k, v in res.items():
+        print(k, v)
