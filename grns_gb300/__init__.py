@@ -1,0 +1,206 @@
+"""grns_gb300 -- GB300-native RNS interval-evaluation path (host side).
+
+Python mirror of the reference library's interface for this path
+(kisupov/grns): the same operation names and argument meanings, applied to
+whole device arrays through the C ABI of libgrns_gb300.so.
+
+    ctx = RNSContext(moduli)                  # rns_const_init() + mpint_const_init()
+    ev  = ctx.rns_eval_compute(x)             # cuda::rns_eval_compute  (src/rnseval.cuh:182)
+    s   = ctx.rns_cmp(x, y)                   # cuda::rns_cmp           (src/rnscmp.cuh:55)
+    q,r = ctx.rns_div(x, d)                   # cuda::rns_div           (src/rnsdiv.cuh:128)
+    z   = ctx.rns_scale2pow(x, D)             # cuda::rns_scale2pow     (src/rnsscal.cuh:207)
+    z   = ctx.mpint_add(a, b) / mpint_sub / mpint_mul   (src/mpint.cuh:336/:407/:478)
+    v,i = ctx.rns_max(x)                      # cuda::rns_max           (src/dpp/rnsmax.cuh:129)
+
+RNS arrays are int32 CUDA tensors: layout "soa" is shape (n, count) (residue
+i of every number contiguous, the native layout), "aos" is shape (count, n)
+(the reference layout).  Interval evaluations come back as uint8 tensors of
+32 bytes per number (interval_t); `intervals_to_numpy` views them on the
+host.  mp_int arrays are uint8 tensors of count * GRNS_MPINT_BYTES(n).
+torch is used only as device-memory and stream plumbing.
+"""
+import ctypes
+
+import numpy as np
+
+from . import native
+from .native import GrnsError, check
+
+ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
+IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
+LAYOUTS = {"soa": 0, "aos": 1}
+SUPPORTED_N = (4, 8, 12, 16, 32, 64)
+
+FLAG_INVALID_INPUT = 1
+FLAG_DIV_BY_ZERO = 2
+FLAG_ITER_CAP = 4
+FLAG_OVERFLOW = 8
+FLAG_MAY_OVERFLOW = 16
+
+
+def mpint_bytes(n):
+    return ((4 * n + 4 + 7) // 8) * 8 + 32
+
+
+def mpint_dtype(n):
+    """numpy dtype with the byte layout of mp_int_t (reference src/types.cuh:45)"""
+    off = ((4 * n + 4 + 7) // 8) * 8
+    return np.dtype({"names": ["digits", "sign", "eval"], "formats": [("<i4", (n,)), "<i4", (ER_DTYPE, (2,))],
+                     "offsets": [0, 4 * n, off], "itemsize": off + 32})
+
+
+def intervals_to_numpy(t):
+    """device uint8 tensor of interval_t -> numpy structured array"""
+    return t.cpu().numpy().view(IV_DTYPE)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class RNSContext:
+    """One moduli set resident on the current CUDA device (replaces the
+    reference's process-global tables from rns_const_init)."""
+
+    def __init__(self, moduli):
+        import torch
+        torch.cuda.init()
+        self.moduli = [int(m) for m in moduli]
+        self.n = len(self.moduli)
+        arr = (ctypes.c_int32 * self.n)(*self.moduli)
+        h = ctypes.c_void_p()
+        check(native.lib().grns_ctx_create(arr, self.n, ctypes.byref(h)), "grns_ctx_create")
+        self._h = h
+        self.log2M = native.lib().grns_ctx_log2(h)
+        self.M = 1
+        for m in self.moduli:
+            self.M *= m
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            native.lib().grns_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- constants ----
+    def table(self, which):
+        n, L = self.n, self.log2M
+        spec = {0: (np.int32, n), 1: (np.float64, n), 2: (np.float64, n), 3: (np.float64, 1), 4: (np.int32, 1),
+                5: (IV_DTYPE, 1), 6: (IV_DTYPE, 1), 7: (np.int32, n * n), 8: (np.int32, (L + 1) * n),
+                9: (np.int32, 30), 10: (np.int32, 30 * n), 11: (np.int32, 30 * n)}[which]
+        out = np.zeros(spec[1], dtype=spec[0])
+        check(native.lib().grns_ctx_get_table(self._h, which, ctypes.c_void_p(out.ctypes.data), out.nbytes),
+              "grns_ctx_get_table")
+        return out
+
+    # ---- helpers ----
+    def _count(self, x, layout):
+        if x.dtype.itemsize != 4 or not x.is_cuda or not x.is_contiguous():
+            raise ValueError("RNS arrays must be contiguous int32 CUDA tensors")
+        if layout == "soa":
+            if x.dim() != 2 or x.shape[0] != self.n:
+                raise ValueError(f"SoA array must have shape ({self.n}, count)")
+            return x.shape[1]
+        if x.dim() != 2 or x.shape[1] != self.n:
+            raise ValueError(f"AoS array must have shape (count, {self.n})")
+        return x.shape[0]
+
+    # ---- operations ----
+    def rns_eval_compute(self, x, layout="soa", flags=None, stream=None):
+        import torch
+        count = self._count(x, layout)
+        out = torch.empty(count * 32, dtype=torch.uint8, device=x.device)
+        check(native.lib().grns_eval(self._h, _ptr(x), count, LAYOUTS[layout], _ptr(out), _ptr(flags),
+                                     _stream(stream)), "grns_eval")
+        return out
+
+    def rns_cmp(self, x, y, layout="soa", flags=None, stream=None):
+        import torch
+        count = self._count(x, layout)
+        if self._count(y, layout) != count:
+            raise ValueError("x and y differ in length")
+        out = torch.empty(count, dtype=torch.int32, device=x.device)
+        check(native.lib().grns_cmp(self._h, _ptr(x), _ptr(y), count, LAYOUTS[layout], _ptr(out), _ptr(flags),
+                                    _stream(stream)), "grns_cmp")
+        return out
+
+    def rns_div(self, x, d, layout="soa", flags=None, stream=None):
+        import torch
+        count = self._count(x, layout)
+        if self._count(d, layout) != count:
+            raise ValueError("x and d differ in length")
+        q = torch.empty_like(x)
+        r = torch.empty_like(x)
+        check(native.lib().grns_div(self._h, _ptr(x), _ptr(d), count, LAYOUTS[layout], _ptr(q), _ptr(r),
+                                    _ptr(flags), _stream(stream)), "grns_div")
+        return q, r
+
+    def rns_scale2pow(self, x, D, layout="soa", flags=None, stream=None):
+        """D: int (same exponent for all) or a uint32/int32 CUDA tensor of per-element exponents"""
+        import torch
+        count = self._count(x, layout)
+        out = torch.empty_like(x)
+        if isinstance(D, int):
+            dptr, du = ctypes.c_void_p(0), D
+        else:
+            if D.numel() != count or D.dtype.itemsize != 4 or not D.is_cuda:
+                raise ValueError("D must hold one 32-bit exponent per element")
+            dptr, du = _ptr(D), 0
+        check(native.lib().grns_scale2pow(self._h, _ptr(x), dptr, du, count, LAYOUTS[layout], _ptr(out),
+                                          _ptr(flags), _stream(stream)), "grns_scale2pow")
+        return out
+
+    def _mpint(self, fn, x, y, flags, stream):
+        import torch
+        nb = mpint_bytes(self.n)
+        if x.numel() % nb or x.numel() != y.numel():
+            raise ValueError("mp_int arrays must be count * mpint_bytes(n) bytes and of equal length")
+        count = x.numel() // nb
+        out = torch.empty_like(x)
+        check(fn(self._h, _ptr(x), _ptr(y), count, _ptr(out), _ptr(flags), _stream(stream)), fn.__name__)
+        return out
+
+    def mpint_add(self, x, y, flags=None, stream=None):
+        return self._mpint(native.lib().grns_mpint_add, x, y, flags, stream)
+
+    def mpint_sub(self, x, y, flags=None, stream=None):
+        return self._mpint(native.lib().grns_mpint_sub, x, y, flags, stream)
+
+    def mpint_mul(self, x, y, flags=None, stream=None):
+        return self._mpint(native.lib().grns_mpint_mul, x, y, flags, stream)
+
+    def rns_max(self, x, layout="soa", scratch=None, stream=None):
+        """returns (value residues int32[n], index int64[1]) on the device"""
+        import torch
+        count = self._count(x, layout)
+        val = torch.zeros(self.n, dtype=torch.int32, device=x.device)
+        idx = torch.empty(1, dtype=torch.int64, device=x.device)
+        nbytes = scratch.numel() if scratch is not None else 0
+        check(native.lib().grns_max(self._h, _ptr(x), count, LAYOUTS[layout], _ptr(val), _ptr(idx), _ptr(scratch),
+                                    nbytes, _stream(stream)), "grns_max")
+        return val, idx
+
+    def max_scratch_size(self, count):
+        v = ctypes.c_size_t()
+        check(native.lib().grns_max_scratch_size(self._h, count, ctypes.byref(v)), "grns_max_scratch_size")
+        return v.value
+
+
+def rns_const_init(moduli):
+    """reference-named constructor: a context for one moduli set"""
+    return RNSContext(moduli)

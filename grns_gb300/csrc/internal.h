@@ -1,0 +1,89 @@
+/*
+ * grns_gb300 -- internal host-side declarations shared by the translation
+ * units of libgrns_gb300.so.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "../../include/grns/grns.h"
+#include "rns_common.cuh"
+
+struct grns_ctx {
+    int n = 0;
+    int log2M = 0;
+    int device = 0;
+    int sm_count = 0;
+    std::vector<uint32_t> moduli;
+    /* host copies of the tables (returned by grns_ctx_get_table) */
+    std::vector<uint32_t> w, w_sh, mu, bits;
+    std::vector<double> rrd, rru;
+    double acc = 0;
+    int ref_factor = 0;
+    grns::Er unit_low{}, unit_upp{}, inv_unit_low{}, inv_unit_upp{};
+    std::vector<uint32_t> pow2;              // (log2M+1) x n
+    std::vector<uint32_t> mrc_inv, mrc_inv_sh;  // n x n, [j*n+i] = m_j^-1 mod m_i
+    std::vector<uint32_t> mi_pow2, m_pow2, pow2_inv, pow2_inv_sh;  // 30 x n, 30, 30 x n, 30 x n
+    /* one device allocation holding all tables */
+    void *d_tables = nullptr;
+    /* kernel constant block for this n (a grns::Consts<n>), bytes */
+    alignas(16) unsigned char consts[sizeof(grns::Consts<grns::kMaxModuli>)];
+    /* library-managed scratch (rns_max partials), grown on demand */
+    std::mutex scratch_mu;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+namespace grns {
+
+template <int N>
+inline const Consts<N> &consts_of(const grns_ctx *c) {
+    return *reinterpret_cast<const Consts<N> *>(c->consts);
+}
+
+inline grns_status cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return GRNS_OK;
+    if (e == cudaErrorMemoryAllocation) return GRNS_ERR_OUT_OF_MEMORY;
+    return GRNS_ERR_CUDA;
+}
+
+/* grid size for grid-stride kernels: enough blocks to cover `work`, capped
+ * at `waves` resident blocks per SM */
+inline unsigned grid_for(const grns_ctx *c, int64_t work, int block, int per_sm = 8) {
+    int64_t need = (work + block - 1) / block;
+    int64_t cap = (int64_t)c->sm_count * per_sm;
+    if (need < 1) need = 1;
+    return (unsigned)(need < cap ? need : cap);
+}
+
+/* launchers (one translation unit per op family) */
+grns_status launch_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
+                        uint8_t *flags, cudaStream_t s);
+grns_status launch_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, int64_t ld, int64_t count,
+                       int32_t *out, uint8_t *flags, cudaStream_t s);
+grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
+                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s);
+grns_status launch_scale2pow(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t D_uniform,
+                             int64_t ld, int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s);
+grns_status launch_mpint(const grns_ctx *c, int op, const void *x, const void *y, int64_t count, void *out,
+                         uint8_t *flags, cudaStream_t s);
+grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out_value,
+                       int64_t *out_index, void *scratch, size_t scratch_bytes, cudaStream_t s);
+size_t max_scratch_bytes(const grns_ctx *c, int64_t count);
+
+}  // namespace grns
+
+#define GRNS_DISPATCH_N(n, CALL) \
+    switch (n) {                 \
+        case 4: CALL(4);         \
+        case 8: CALL(8);         \
+        case 12: CALL(12);       \
+        case 16: CALL(16);       \
+        case 32: CALL(32);       \
+        case 64: CALL(64);       \
+        default: return GRNS_ERR_UNSUPPORTED; \
+    }

@@ -1,0 +1,160 @@
+/*
+ * grns_gb300 -- maximum of an RNS array in ONE launch.
+ *
+ * Replaces cuda::rns_max (reference src/dpp/rnsmax.cuh:129-138), which runs
+ * an evaluation kernel writing N xinterval_t to a buffer, two tree kernels
+ * and a copy kernel, then synchronises the device.  Here each thread
+ * evaluates its numbers in registers and keeps its best candidate
+ * (interval, index); candidates are reduced by warp shuffles, then across
+ * warps in shared memory, then across blocks by the last block to finish
+ * (one atomic ticket per block).  Comparisons follow rns_max_cmp
+ * (:24-48): interval test first, exact mixed-radix comparison only when
+ * the intervals overlap.  Equal values resolve to the smallest index.
+ */
+#include "internal.h"
+#include "rns_device.cuh"
+
+namespace grns {
+
+struct Cand {
+    Er lo, up;
+    int64_t idx;  // < 0: empty
+};
+
+template <int N>
+__device__ __forceinline__ bool better(const Consts<N> &C, const Operand<N> &x, const Cand &a, const Cand &b) {
+    if (b.idx < 0) return a.idx >= 0;
+    if (a.idx < 0) return false;
+    int r = cmp_intervals<N>(a.lo, a.up, b.lo, b.up);
+    if (r == 2) {
+        const int64_t ia = a.idx, ib = b.idx;
+        r = cmp_tie<N>(C, [&](int i) { return x.load(ia, i); }, [&](int i) { return x.load(ib, i); });
+    }
+    if (r != 0) return r > 0;
+    return a.idx < b.idx;
+}
+
+__device__ __forceinline__ Cand shfl_cand(const Cand &c, int src_lane_xor) {
+    Cand o;
+    o.lo.frac = __shfl_xor_sync(0xffffffffu, c.lo.frac, src_lane_xor);
+    o.lo.exp = __shfl_xor_sync(0xffffffffu, c.lo.exp, src_lane_xor);
+    o.up.frac = __shfl_xor_sync(0xffffffffu, c.up.frac, src_lane_xor);
+    o.up.exp = __shfl_xor_sync(0xffffffffu, c.up.exp, src_lane_xor);
+    o.idx = __shfl_xor_sync(0xffffffffu, c.idx, src_lane_xor);
+    return o;
+}
+
+template <int N>
+__device__ __forceinline__ Cand block_reduce(const Consts<N> &C, const Operand<N> &x, Cand best, Cand *sm) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Cand o = shfl_cand(best, off);
+        if (better<N>(C, x, o, best)) best = o;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) sm[wid] = best;
+    __syncthreads();
+    if (wid == 0) {
+        best = lane < nw ? sm[lane] : Cand{{0.0, 0}, {0.0, 0}, -1};
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            Cand o = shfl_cand(best, off);
+            if (better<N>(C, x, o, best)) best = o;
+        }
+    }
+    return best;  // valid in thread 0
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_max(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+                                             uint32_t *__restrict__ out_value, int64_t *__restrict__ out_index,
+                                             unsigned *__restrict__ ticket, Cand *__restrict__ partial) {
+    __shared__ Cand sm[32];
+    __shared__ bool last;
+    Cand best{{0.0, 0}, {0.0, 0}, -1};
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t f = 0;
+        Cand c;
+        c.idx = k;
+        eval<N>(C, [&](int i) { return x.load(k, i); }, c.lo, c.up, f);
+        if (better<N>(C, x, c, best)) best = c;
+    }
+    best = block_reduce<N>(C, x, best, sm);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = best;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    best = Cand{{0.0, 0}, {0.0, 0}, -1};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        const Cand *p = partial + b;  /* written by other blocks: read through L2 */
+        Cand c;
+        c.lo.frac = __ldcg(&p->lo.frac);
+        c.lo.exp = __ldcg((const long long *)&p->lo.exp);
+        c.up.frac = __ldcg(&p->up.frac);
+        c.up.exp = __ldcg((const long long *)&p->up.exp);
+        c.idx = __ldcg((const long long *)&p->idx);
+        if (better<N>(C, x, c, best)) best = c;
+    }
+    __syncthreads();
+    best = block_reduce<N>(C, x, best, sm);
+    if (threadIdx.x == 0) sm[0] = best;
+    __syncthreads();
+    const int64_t bi = sm[0].idx;
+    if (threadIdx.x == 0 && out_index) *out_index = bi;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) out_value[i] = bi >= 0 ? x.load(bi, i) : 0u;
+}
+
+constexpr int kMaxBlock = 256;
+constexpr int kMaxPerSm = 4;
+
+static unsigned max_grid(const grns_ctx *c, int64_t count) { return grid_for(c, count, kMaxBlock, kMaxPerSm); }
+
+size_t max_scratch_bytes(const grns_ctx *c, int64_t count) { return 64 + (size_t)max_grid(c, count) * sizeof(Cand); }
+
+template <int N>
+static grns_status run_max(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out_value,
+                           int64_t *out_index, void *scratch, cudaStream_t s) {
+    unsigned G = max_grid(c, count);
+    cudaError_t e = cudaMemsetAsync(scratch, 0, 64, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    k_max<N><<<G, kMaxBlock, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, out_value, out_index,
+                                     (unsigned *)scratch, (Cand *)((char *)scratch + 64));
+    return cuda_status(cudaGetLastError());
+}
+
+grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out_value,
+                       int64_t *out_index, void *scratch, size_t scratch_bytes, cudaStream_t s) {
+    if (count == 0) {
+        if (out_index) return cuda_status(cudaMemsetAsync(out_index, 0xff, sizeof(int64_t), s));
+        return GRNS_OK;
+    }
+    bool owned = false;
+    if (!scratch) {  /* stream-ordered allocation: safe for concurrent calls on different streams */
+        cudaError_t e = cudaMallocAsync(&scratch, max_scratch_bytes(c, count), s);
+        if (e != cudaSuccess) return cuda_status(e);
+        owned = true;
+    }
+    grns_status st;
+#define C_(n) st = run_max<n>(c, x, ld, count, out_value, out_index, scratch, s); break
+    switch (c->n) {
+        case 4: C_(4);
+        case 8: C_(8);
+        case 12: C_(12);
+        case 16: C_(16);
+        case 32: C_(32);
+        case 64: C_(64);
+        default: st = GRNS_ERR_UNSUPPORTED;
+    }
+#undef C_
+    if (owned) {
+        cudaError_t e = cudaFreeAsync(scratch, s);
+        if (st == GRNS_OK && e != cudaSuccess) st = cuda_status(e);
+    }
+    return st;
+}
+
+}  // namespace grns

@@ -1,0 +1,157 @@
+/*
+ * grns_gb300 -- shared host/device building blocks.
+ *
+ *   * per-moduli-set constant block passed to every kernel by value (so the
+ *     per-modulus constants sit in the kernel-parameter constant bank and are
+ *     read with compile-time offsets from fully unrolled loops);
+ *   * modular arithmetic on the integer pipe: Shoup multiplication by a
+ *     constant, Barrett multiplication of two residues, branch-free add/sub;
+ *   * extended-range float (er_float_t) helpers with the reference's exact
+ *     semantics (src/extrange.cuh:366-603).
+ *
+ * Residues are canonical uint32 in [0, m) with m odd and 3 <= m <= 1431655765
+ * (3m fits in 32 bits, which the Barrett step below relies on).
+ */
+#pragma once
+
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define GRNS_HD __host__ __device__ __forceinline__
+#else
+#define GRNS_HD inline
+#endif
+
+namespace grns {
+
+constexpr int kMaxModuli = 64;
+constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/params.h:22)
+
+struct Er {  // er_float_t
+    double frac;
+    int64_t exp;
+};
+
+/* Constant block of one moduli set, specialised on the moduli count N. */
+template <int N>
+struct Consts {
+    uint32_t m[N];        // moduli
+    uint32_t w[N];        // (M/m_i)^-1 mod m_i          RNS_PART_MODULI_PRODUCT_INVERSE
+    uint32_t w_sh[N];     // floor(w_i * 2^32 / m_i)     Shoup companion of w_i
+    uint32_t mu[N];       // floor(2^(2 b_i) / m_i)      Barrett constant, b_i = bit length of m_i
+    uint32_t b[N];        // b_i
+    double rrd[N];        // RNS_MODULI_RECIP_RD
+    double rru[N];        // RNS_MODULI_RECIP_RU
+    double acc;           // RNS_EVAL_ACCURACY
+    int ref_factor;       // RNS_EVAL_REF_FACTOR
+    int log2M;            // floor(log2 M), the RNS_MODULI_PRODUCT_LOG2 convention
+    Er unit_low, unit_upp, inv_unit_low, inv_unit_upp;  // RNS_EVAL_UNIT, RNS_EVAL_INV_UNIT
+    uint32_t m_pow2_res30;                // M mod 2^30
+    const uint32_t *pow2;       // [(log2M + 1) * N]  2^j mod m_i        (RNS_POW2)
+    const uint32_t *mrc_inv;    // [N * N]  [j * N + i] = m_j^-1 mod m_i (MRC_MULT_INV)
+    const uint32_t *mrc_inv_sh; // [N * N]  Shoup companions
+    const uint32_t *mi_pow2;    // [30 * N] M_i mod 2^(j+1)             (RNS_PART_MODULI_PRODUCT_POW2_RESIDUES)
+    const uint32_t *m_pow2;     // [30]     M mod 2^(j+1)               (RNS_MODULI_PRODUCT_POW2_RESIDUES)
+    const uint32_t *pow2_inv;   // [30 * N] (2^(j+1))^-1 mod m_i        (RNS_POW2_INVERSE)
+    const uint32_t *pow2_inv_sh;// [30 * N]
+};
+
+/* ---------------- modular arithmetic ---------------- */
+
+/* x * w mod m for a constant w with Shoup companion ws = floor(w 2^32 / m); x < 2^32. */
+GRNS_HD uint32_t mulmod_shoup(uint32_t x, uint32_t w, uint32_t ws, uint32_t m) {
+#ifdef __CUDA_ARCH__
+    uint32_t q = __umulhi(x, ws);
+#else
+    uint32_t q = (uint32_t)(((uint64_t)x * ws) >> 32);
+#endif
+    uint32_t r = x * w - q * m;  // true value in [0, 2m)
+    return r >= m ? r - m : r;
+}
+
+GRNS_HD uint32_t umin32(uint32_t a, uint32_t b) { return a < b ? a : b; }
+
+/* x * y mod m for canonical x, y (Barrett, HAC 14.42 in radix 2: quotient
+ * estimate within 2 of the true quotient, so r < 3m < 2^32). */
+GRNS_HD uint32_t mulmod_barrett(uint32_t x, uint32_t y, uint32_t m, uint32_t mu, uint32_t b) {
+    uint64_t p = (uint64_t)x * y;
+    uint32_t t = (uint32_t)(p >> (b - 1));
+    uint32_t q = (uint32_t)(((uint64_t)t * mu) >> (b + 1));
+    uint32_t r = (uint32_t)p - q * m;
+    r = umin32(r, r - m);
+    return umin32(r, r - m);
+}
+
+GRNS_HD uint32_t addmod(uint32_t x, uint32_t y, uint32_t m) {
+    uint32_t r = x + y;
+    return umin32(r, r - m);
+}
+GRNS_HD uint32_t submod(uint32_t x, uint32_t y, uint32_t m) {
+    uint32_t r = x - y;
+    return umin32(r, r + m);
+}
+
+/* ---------------- er_float_t (reference src/extrange.cuh) ---------------- */
+
+GRNS_HD uint64_t dbits(double x) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    __builtin_memcpy(&u, &x, 8);
+    return u;
+#endif
+}
+GRNS_HD double bitsd(uint64_t u) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    __builtin_memcpy(&x, &u, 8);
+    return x;
+#endif
+}
+
+/* er_set_d (src/extrange.cuh:75) */
+GRNS_HD Er er_from_double(double x) {
+    Er r;
+    uint64_t u = dbits(x);
+    if (x != 0) {
+        r.exp = (int64_t)((u & 0x7fffffffffffffffull) >> 52) - 1023;
+        r.frac = bitsd((u & 0x800fffffffffffffull) | 0x3ff0000000000000ull);
+    } else {
+        r.exp = 0;
+        r.frac = 0;
+    }
+    return r;
+}
+
+/* er_adjust (src/extrange.cuh:366) */
+GRNS_HD void er_adjust(Er &x) {
+    uint64_t u = dbits(x.frac);
+    int64_t nz = x.frac != 0;
+    x.exp = (x.exp + (int64_t)((u & 0x7fffffffffffffffull) >> 52) - 1023) * nz;
+    x.frac = bitsd((u & 0x800fffffffffffffull) | 0x3ff0000000000000ull) * (double)nz;
+}
+
+/* er_ucmp (src/extrange.cuh:597) */
+GRNS_HD int er_ucmp(const Er &x, const Er &y) {
+    int diff = (int)(x.exp - y.exp);
+    if (diff == 0) return x.frac == y.frac ? 0 : (x.frac > y.frac ? 1 : -1);
+    return (x.frac != 0 && (diff > 0 || (diff < 0 && y.frac == 0))) ? 1 : -1;
+}
+
+/* exact double of a uint32 built on the integer pipe (avoids the slow
+ * I2F.F64 conversion); equals (double)s */
+GRNS_HD double u32_to_double(uint32_t s) {
+#ifdef __CUDA_ARCH__
+    if (s == 0) return 0.0;
+    int lz = __clz(s);
+    uint64_t bits = ((uint64_t)(1053 - lz) << 52) + ((uint64_t)s << (lz + 21));
+    return bitsd(bits);
+#else
+    return (double)s;
+#endif
+}
+
+}  // namespace grns

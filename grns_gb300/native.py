@@ -1,0 +1,73 @@
+"""ctypes binding of libgrns_gb300.so (the C ABI declared in include/grns/grns.h).
+
+The library is built in-tree by grns_gb300/build.py.  There is no CPU or
+pure-PyTorch fallback: if the library is missing or fails to load, every
+entry point raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_lib = None
+
+c_int, c_int64, c_size_t, c_void_p, c_uint32 = ctypes.c_int, ctypes.c_int64, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_uint32
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "grns_status_string": (ctypes.c_char_p, [c_int]),
+    "grns_version": (ctypes.c_char_p, []),
+    "grns_ctx_create": (c_int, [c_void_p, c_int, ctypes.POINTER(c_void_p)]),
+    "grns_ctx_destroy": (c_int, [c_void_p]),
+    "grns_ctx_n": (c_int, [c_void_p]),
+    "grns_ctx_log2": (c_int, [c_void_p]),
+    "grns_ctx_get_table": (c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    "grns_eval": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "grns_cmp": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "grns_div": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "grns_scale2pow": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "grns_mpint_add": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "grns_mpint_sub": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "grns_mpint_mul": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "grns_max_scratch_size": (c_int, [c_void_p, c_int64, ctypes.POINTER(c_size_t)]),
+    "grns_max": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "grns_gen_uniform": (c_int, [c_void_p, ctypes.c_uint64, c_uint32, c_int64, c_int, c_void_p, c_void_p]),
+    "grns_gen_divisors": (c_int, [c_void_p, ctypes.c_uint64, c_int64, c_int, c_void_p, c_void_p]),
+    "grns_gen_shifts": (c_int, [ctypes.c_uint64, c_int64, c_uint32, c_void_p, c_void_p]),
+}
+
+
+class GrnsError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = lib().grns_status_string(status).decode()
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=False):
+    """Load the native library (building it first only when asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise RuntimeError(f"grns_gb300 native library not built ({path}); run grns_gb300/build.py")
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status, what=""):
+    if status != 0:
+        raise GrnsError(status, what)

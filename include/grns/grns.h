@@ -1,0 +1,155 @@
+/*
+ * grns_gb300 -- C ABI of the GB300-native RNS interval-evaluation path.
+ *
+ * Drop-in boundary for the data-parallel hot path of the reference library
+ * kisupov/grns (header-only CUDA C++).  The reference exposes device
+ * functions that user kernels call per number plus one host launcher
+ * (cuda::rns_max).  This ABI replaces the per-number device calls by batched,
+ * stream-ordered entry points over whole arrays, keeps the reference's data
+ * layouts (types.h) and its moduli-set convention (params.h: a list of
+ * pairwise-coprime moduli), and returns status codes instead of exiting.
+ *
+ * Conventions
+ *  - All array pointers are DEVICE pointers unless stated otherwise.
+ *  - RNS arrays: `layout` GRNS_LAYOUT_AOS is the reference layout
+ *    [x1..xn][x1..xn]... (reference src/dpp/rnsmax.cuh:125); GRNS_LAYOUT_SOA
+ *    stores residue i of all `count` numbers contiguously (x[i * count + k]),
+ *    the native layout: every modulus slice is a coalesced load.
+ *  - Residues are int32 in [0, m_i).  An out-of-range residue sets
+ *    GRNS_FLAG_INVALID_INPUT in the element's flag and yields zeros.
+ *  - `flags` (optional, may be NULL): one uint8 per element, bits GRNS_FLAG_*.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls only
+ *    enqueue work; nothing synchronises the device implicitly.
+ *  - A context is immutable after creation; it may be used from several host
+ *    threads and streams at once.
+ */
+#ifndef GRNS_GB300_GRNS_H
+#define GRNS_GB300_GRNS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GRNS_OK = 0,
+    GRNS_ERR_INVALID_ARGUMENT = 1,
+    GRNS_ERR_UNSUPPORTED = 2,   /* moduli count or values outside the supported range */
+    GRNS_ERR_CUDA = 3,          /* a CUDA runtime call or launch failed */
+    GRNS_ERR_OUT_OF_MEMORY = 4,
+    GRNS_ERR_TIMEOUT = 5,       /* a bounded wait ran out */
+    GRNS_ERR_REJECTED = 6,      /* admission refused (serving) */
+    GRNS_ERR_BUSY = 7
+} grns_status;
+
+typedef enum { GRNS_LAYOUT_SOA = 0, GRNS_LAYOUT_AOS = 1 } grns_layout;
+
+enum {
+    GRNS_FLAG_INVALID_INPUT = 1u << 0,
+    GRNS_FLAG_DIV_BY_ZERO = 1u << 1,
+    GRNS_FLAG_ITER_CAP = 1u << 2,
+    GRNS_FLAG_OVERFLOW = 1u << 3,      /* mp_int: "Overflow has occurred" (reference src/mpint.cuh:324) */
+    GRNS_FLAG_MAY_OVERFLOW = 1u << 4   /* mp_int: "Overflow may occurred" (reference src/mpint.cuh:327) */
+};
+
+typedef struct grns_ctx grns_ctx;
+
+const char *grns_status_string(grns_status s);
+const char *grns_version(void);
+
+/* ---- context: one moduli set resident on the current device ----
+ * Replaces rns_const_init() (reference src/rnsbase.cuh:324) and
+ * mpint_const_init() (src/mpint.cuh:20), which fill process-global tables;
+ * here every moduli set is its own context, so several (e.g. n = 32 and
+ * n = 64) can be resident together.  Supported n: 4, 8, 12, 16, 32, 64;
+ * moduli odd, pairwise coprime, 3 <= m_i <= 1431655765. */
+grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out);
+grns_status grns_ctx_destroy(grns_ctx *ctx);
+int grns_ctx_n(const grns_ctx *ctx);
+/* floor(log2 M): the reference's RNS_MODULI_PRODUCT_LOG2 (src/params.h:16) */
+int grns_ctx_log2(const grns_ctx *ctx);
+
+/* Host copies of the constant tables rns_const_init computes, for checking.
+ * which: 0 w_i (RNS_PART_MODULI_PRODUCT_INVERSE, int32[n]); 1 RNS_MODULI_RECIP_RD
+ * (double[n]); 2 RNS_MODULI_RECIP_RU (double[n]); 3 RNS_EVAL_ACCURACY (double);
+ * 4 RNS_EVAL_REF_FACTOR (int32); 5 RNS_EVAL_UNIT (interval_t); 6
+ * RNS_EVAL_INV_UNIT (interval_t); 7 MRC_MULT_INV (int32[n][n], [i][j] = m_i^-1
+ * mod m_j for j > i, else 0); 8 RNS_POW2 (int32[log2+1][n]); 9
+ * RNS_MODULI_PRODUCT_POW2_RESIDUES (int32[30]); 10
+ * RNS_PART_MODULI_PRODUCT_POW2_RESIDUES (int32[30][n]); 11 RNS_POW2_INVERSE
+ * (int32[30][n]).  `bytes` must equal the table size. */
+grns_status grns_ctx_get_table(const grns_ctx *ctx, int which, void *host_dst, size_t bytes);
+
+/* ---- interval evaluation ----
+ * out[k] = [low, upp] enclosing X_k / M, bit-identical to
+ * cuda::rns_eval_compute (reference src/rnseval.cuh:182). */
+grns_status grns_eval(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, interval_t *out,
+                      uint8_t *flags, void *stream);
+
+/* ---- magnitude comparison ----
+ * out[k] = sign(X_k - Y_k) in {-1, 0, 1}, as cuda::rns_cmp
+ * (reference src/rnscmp.cuh:55); the evaluations stay in registers. */
+grns_status grns_cmp(grns_ctx *ctx, const int32_t *x, const int32_t *y, int64_t count, int layout,
+                     int32_t *out, uint8_t *flags, void *stream);
+
+/* ---- general integer division ----
+ * q = floor(X / D), r = X - qD, as cuda::rns_div (reference
+ * src/rnsdiv.cuh:128).  D = 0 sets GRNS_FLAG_DIV_BY_ZERO and yields q = 0, r = X. */
+grns_status grns_div(grns_ctx *ctx, const int32_t *x, const int32_t *d, int64_t count, int layout,
+                     int32_t *q, int32_t *r, uint8_t *flags, void *stream);
+
+/* ---- power-of-two scaling ----
+ * out = floor(X / 2^D), as rns_scale2pow (reference src/rnsscal.cuh:93/:207).
+ * D is per element (device array `D`, uint32[count]); when D is NULL every
+ * element uses `D_uniform`. */
+grns_status grns_scale2pow(grns_ctx *ctx, const int32_t *x, const uint32_t *D, uint32_t D_uniform,
+                           int64_t count, int layout, int32_t *out, uint8_t *flags, void *stream);
+
+/* ---- multiple-precision integers (mp_int_t arrays, reference layout) ----
+ * result = x + y / x - y / x * y elementwise with the interval evaluation
+ * derived as cuda::mpint_add / mpint_sub / mpint_mul (reference
+ * src/mpint.cuh:336/:407/:478).  Overflow is reported through `flags`
+ * (GRNS_FLAG_OVERFLOW / GRNS_FLAG_MAY_OVERFLOW) instead of printf. */
+grns_status grns_mpint_add(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
+                           uint8_t *flags, void *stream);
+grns_status grns_mpint_sub(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
+                           uint8_t *flags, void *stream);
+grns_status grns_mpint_mul(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
+                           uint8_t *flags, void *stream);
+
+/* ---- maximum of an RNS array ----
+ * Replaces template cuda::rns_max<g1,b1,g2,b2>(out, in, N, buffer)
+ * (reference src/dpp/rnsmax.cuh:129): one fused launch, evaluations kept in
+ * registers.  out_value (device int32[n]) receives the maximum's residues,
+ * out_index (device int64, may be NULL) its index; equal maxima resolve to
+ * the smallest index.  count == 0 writes index -1 and leaves out_value as is.
+ * scratch: device buffer of at least grns_max_scratch_size() bytes, or NULL
+ * to let the call take a stream-ordered allocation (cudaMallocAsync /
+ * cudaFreeAsync on `stream`).  The call clears the scratch's first 64 bytes
+ * itself; calls that share one scratch buffer must be stream-ordered. */
+grns_status grns_max_scratch_size(const grns_ctx *ctx, int64_t count, size_t *bytes);
+grns_status grns_max(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, int32_t *out_value,
+                     int64_t *out_index, void *scratch, size_t scratch_bytes, void *stream);
+
+
+/* ---- seeded synthetic inputs in device memory ----
+ * No counterpart in the reference (its tests draw from GMP's Mersenne
+ * Twister seeded with time(NULL), tests/tsthelper.cuh:33).  Counter-based
+ * splitmix64 streams, identical to grns_gb300/workload.py:
+ *   grns_gen_uniform : numbers uniform in [0, M) (independent uniform residues)
+ *   grns_gen_divisors: divisors of bit length L, L uniform in [1, log2 M]
+ *   grns_gen_shifts  : exponents uniform in [1, dmax] */
+grns_status grns_gen_uniform(grns_ctx *ctx, uint64_t seed, uint32_t stream, int64_t count, int layout, int32_t *out,
+                             void *cuda_stream);
+grns_status grns_gen_divisors(grns_ctx *ctx, uint64_t seed, int64_t count, int layout, int32_t *out, void *cuda_stream);
+grns_status grns_gen_shifts(uint64_t seed, int64_t count, uint32_t dmax, uint32_t *out, void *cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

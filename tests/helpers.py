@@ -1,0 +1,28 @@
+"""Shared test helpers: golden fixtures and moduli sets."""
+import os
+
+import numpy as np
+
+from oracle.oracle import REFERENCE_DEFAULT_MODULI, greedy_moduli
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TAGS = ["ref8", "g8", "g12", "g32", "g64"]
+
+ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
+IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
+
+
+def moduli_for(tag):
+    if tag == "ref8":
+        return list(REFERENCE_DEFAULT_MODULI)
+    return greedy_moduli(int(tag[1:]))
+
+
+def golden(tag):
+    return dict(np.load(os.path.join(GOLDEN, f"golden_{tag}.npz")))
+
+
+def mpint_dtype(n):
+    off = ((4 * n + 4 + 7) // 8) * 8
+    return np.dtype({"names": ["digits", "sign", "eval"], "formats": [("<i4", (n,)), "<i4", (ER_DTYPE, (2,))],
+                     "offsets": [0, 4 * n, off], "itemsize": off + 32})

@@ -1,0 +1,61 @@
+"""CPU: the C-ABI library builds for sm_103a, loads, and exports every
+entry point declared in include/grns/*.h; the product never reaches into the
+oracle."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from grns_gb300 import build, native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include", "grns")
+    for f in os.listdir(inc):
+        src = open(os.path.join(inc, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        names.update(re.findall(r"\b(grns_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return native.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_bindings_cover_declarations():
+    assert set(declared_symbols()) <= set(native.SIGNATURES), set(declared_symbols()) - set(native.SIGNATURES)
+
+
+def test_status_strings(lib):
+    assert lib.grns_status_string(0) == b"ok"
+    assert b"sm_103a" in lib.grns_version()
+
+
+def test_invalid_arguments_rejected_without_gpu(lib):
+    out = ctypes.c_void_p()
+    assert lib.grns_ctx_create(None, 8, ctypes.byref(out)) == 1
+    mods = (ctypes.c_int32 * 8)(*([3] * 8))
+    assert lib.grns_ctx_create(mods, 7, ctypes.byref(out)) == 2  # unsupported n
+    assert lib.grns_eval(None, None, 1, 0, None, None, None) == 1
+
+
+def test_product_does_not_use_oracle():
+    for d, _, files in os.walk(os.path.join(ROOT, "grns_gb300")):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                src = open(os.path.join(d, f)).read()
+                assert "oracle" not in src.replace("oracle is", ""), os.path.join(d, f)

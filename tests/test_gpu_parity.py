@@ -1,0 +1,231 @@
+"""GPU parity: every op of the path through the C ABI on the device, against
+the reference's golden vectors (bit for bit), the oracle's restatement of the
+reference's device path (bit for bit, fresh seeded inputs), and exact
+big-integer arithmetic (integer results, enclosure of X/M)."""
+import random
+
+import numpy as np
+import pytest
+
+from grns_gb300 import workload as W
+from oracle import oracle as O
+from tests.helpers import IV_DTYPE, TAGS, golden, moduli_for, mpint_dtype
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from grns_gb300 import native
+    native.lib(build_if_missing=True)
+    return torch.device("cuda:0")
+
+
+@pytest.fixture(scope="module", params=TAGS)
+def case(request, dev):
+    import grns_gb300 as G
+    tag = request.param
+    mods = moduli_for(tag)
+    return tag, G.RNSContext(mods), O.Oracle(mods), golden(tag)
+
+
+def to_dev(a, layout):
+    a = np.ascontiguousarray(a if layout == "aos" else a.T, dtype=np.int32)
+    return torch.from_numpy(a).cuda()
+
+
+def from_dev(t, layout):
+    a = t.cpu().numpy()
+    return a if layout == "aos" else np.ascontiguousarray(a.T)
+
+
+def flags_buf(count):
+    return torch.zeros(count, dtype=torch.uint8, device="cuda")
+
+
+def test_constants_match_oracle(case):
+    tag, ctx, orc, g = case
+    c = orc.consts()
+    keys = ["w", "recip_rd", "recip_ru", "acc", "ref_factor", "unit", "inv_unit", "mrc_inv", "pow2", "m_pow2_res",
+            "mi_pow2_res", "pow2_inv"]
+    for which, k in enumerate(keys):
+        assert ctx.table(which).tobytes() == c[k].tobytes(), k
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_eval_golden(case, layout):
+    tag, ctx, orc, g = case
+    out = ctx.rns_eval_compute(to_dev(g["x"], layout), layout=layout)
+    assert out.cpu().numpy().tobytes() == g["eval_dev"].tobytes()
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_eval_random_bit_exact_and_enclosing(case, layout):
+    tag, ctx, orc, g = case
+    N = 6000 if orc.n <= 16 else 2000
+    x = W.uniform_residues(orc.moduli, N, seed=101, stream=W.S_X, layout="aos")
+    # sprinkle small values (refinement loop) and values near M (ambiguity branch)
+    rng = random.Random(5)
+    small = [rng.randrange(1, 1 << rng.randrange(1, orc.log2M)) for _ in range(200)]
+    big = [orc.M - rng.randrange(1, 1 << 40) for _ in range(100)]
+    x = np.concatenate([x, orc.exact.to_rns(small + big)])
+    flags = flags_buf(len(x))
+    got = ctx.rns_eval_compute(to_dev(x, layout), layout=layout, flags=flags).cpu().numpy().view(IV_DTYPE)
+    want = orc.eval(x, path=O.PATH_DEVICE)
+    assert got.tobytes() == want.tobytes()
+    assert int(flags.sum()) == 0
+    idx = list(range(0, len(x), max(1, len(x) // 300))) + list(range(len(x) - 300, len(x)))
+    X = orc.exact.from_rns(x[idx])
+    assert orc.exact.encloses(got[idx], X).all()
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_cmp(case, layout):
+    tag, ctx, orc, g = case
+    got = ctx.rns_cmp(to_dev(g["x"], layout), to_dev(g["y"], layout), layout=layout).cpu().numpy()
+    assert np.array_equal(got, g["cmp_dev"])
+    N = 8000 if orc.n <= 16 else 2000
+    x = W.uniform_residues(orc.moduli, N, seed=7, stream=W.S_X, layout="aos")
+    y = W.uniform_residues(orc.moduli, N, seed=7, stream=W.S_Y, layout="aos")
+    y[::7] = x[::7]                      # equal pairs
+    X = orc.exact.from_rns(x[1::7])
+    y[1::7] = orc.exact.to_rns([(v + 1) % orc.M for v in X])  # adjacent pairs: intervals overlap
+    got = ctx.rns_cmp(to_dev(x, layout), to_dev(y, layout), layout=layout).cpu().numpy()
+    assert np.array_equal(got, orc.cmp(x, y, path=O.PATH_DEVICE))
+    Xs, Ys = orc.exact.from_rns(x[:500]), orc.exact.from_rns(y[:500])
+    assert list(got[:500]) == [(a > b) - (a < b) for a, b in zip(Xs, Ys)]
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_div(case, layout):
+    tag, ctx, orc, g = case
+    q, r = ctx.rns_div(to_dev(g["xd"], layout), to_dev(g["d"], layout), layout=layout)
+    assert np.array_equal(from_dev(q, layout), g["div_q_dev"])
+    assert np.array_equal(from_dev(r, layout), g["div_r_dev"])
+    N = 400 if orc.n <= 16 else 120
+    x = W.uniform_residues(orc.moduli, N, seed=3, stream=W.S_X, layout="aos")
+    d, dv = W.divisors(orc.moduli, orc.log2M, N, seed=3, layout="aos")
+    flags = flags_buf(N)
+    q, r = ctx.rns_div(to_dev(x, layout), to_dev(d, layout), layout=layout, flags=flags)
+    X = orc.exact.from_rns(x)
+    assert orc.exact.from_rns(from_dev(q, layout)) == [a // b for a, b in zip(X, dv)]
+    assert orc.exact.from_rns(from_dev(r, layout)) == [a % b for a, b in zip(X, dv)]
+    assert int(flags.sum()) == 0
+
+
+def test_div_by_zero_flag(case):
+    tag, ctx, orc, g = case
+    x = orc.exact.to_rns([12345, 7])
+    d = orc.exact.to_rns([0, 7])
+    flags = flags_buf(2)
+    q, r = ctx.rns_div(to_dev(x, "aos"), to_dev(d, "aos"), layout="aos", flags=flags)
+    f = flags.cpu().numpy()
+    assert f[0] & 2 and f[1] == 0
+    assert orc.exact.from_rns(q.cpu().numpy()) == [0, 1]
+    assert orc.exact.from_rns(r.cpu().numpy()) == [12345, 0]
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_scale2pow(case, layout):
+    tag, ctx, orc, g = case
+    D = torch.from_numpy(g["shift"].astype(np.int32)).cuda()
+    out = from_dev(ctx.rns_scale2pow(to_dev(g["x"], layout), D, layout=layout), layout)
+    X = orc.exact.from_rns(g["x"])
+    assert orc.exact.from_rns(out) == [a >> int(k) for a, k in zip(X, g["shift"])]
+    # equals the reference device path except where its last-step rank choice errs
+    ref_dev = g["scale_dev"]
+    same = (out == ref_dev).all(axis=1)
+    wrong_ref = [orc.exact.from_rns(ref_dev[i:i + 1])[0] != X[i] >> int(g["shift"][i]) for i in range(len(X))]
+    assert all(s or w for s, w in zip(same, wrong_ref))
+    N = 1500 if orc.n <= 16 else 400
+    x = W.uniform_residues(orc.moduli, N, seed=9, stream=W.S_X, layout="aos")
+    Dh = W.shifts(N, min(900, orc.log2M + 40), seed=9)
+    out = from_dev(ctx.rns_scale2pow(to_dev(x, layout), torch.from_numpy(Dh.astype(np.int32)).cuda(), layout=layout),
+                   layout)
+    assert np.array_equal(out, orc.scale2pow(x, Dh, path=O.PATH_DEVICE, gpu_quirk=0))
+    X = orc.exact.from_rns(x[:300])
+    assert orc.exact.from_rns(out[:300]) == [a >> int(k) for a, k in zip(X, Dh[:300])]
+    out_u = from_dev(ctx.rns_scale2pow(to_dev(x, layout), 61, layout=layout), layout)
+    assert np.array_equal(out_u, orc.scale2pow(x, np.full(N, 61, np.uint32), path=O.PATH_DEVICE))
+
+
+@pytest.mark.parametrize("op", ["add", "sub", "mul"])
+def test_mpint(case, op):
+    tag, ctx, orc, g = case
+    fn = getattr(ctx, f"mpint_{op}")
+    a = torch.from_numpy(g["mpint_a"]).cuda()
+    b = torch.from_numpy(g["mpint_b"]).cuda()
+    flags = flags_buf(len(g["mpint_a"]) // mpint_dtype(orc.n).itemsize)
+    out = fn(a, b, flags=flags).cpu().numpy()
+    assert out.tobytes() == g[f"mpint_{op}_dev"].tobytes()
+    # fresh operands: magnitudes below 2^(log2M/2 - 10), eval from the device path
+    vals_a = W.mpint_values(600, orc.log2M // 2 - 10, seed=13)
+    vals_b = W.mpint_values(600, orc.log2M // 2 - 10, seed=14)
+    ma, mb = orc.mpint_from_ints(vals_a), orc.mpint_from_ints(vals_b)
+    out = fn(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda())
+    got = out.cpu().numpy().view(mpint_dtype(orc.n))
+    want, wflags = orc.mpint(op, ma, mb, path=O.PATH_DEVICE)
+    assert got.tobytes() == want.tobytes()
+    exact = {"add": lambda p, q: p + q, "sub": lambda p, q: p - q, "mul": lambda p, q: p * q}[op]
+    mags = orc.exact.from_rns(got["digits"])
+    assert [(-v if s else v) for v, s in zip(mags, got["sign"])] == [exact(p, q) for p, q in zip(vals_a, vals_b)]
+
+
+def test_mpint_overflow_flag(case):
+    tag, ctx, orc, g = case
+    big = orc.M // 2 + 12345
+    ma, mb = orc.mpint_from_ints([big, 3]), orc.mpint_from_ints([big, 4])
+    flags = flags_buf(2)
+    ctx.mpint_add(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda(), flags=flags)
+    _, want = orc.mpint("add", ma, mb)
+    f = flags.cpu().numpy()
+    assert (f[0] & 24) != 0 and f[1] == 0
+    assert bool(f[0] & 8) == (want[0] == 2)
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_max(case, layout):
+    tag, ctx, orc, g = case
+    N = 20000 if orc.n <= 16 else 5000
+    x = W.uniform_residues(orc.moduli, N, seed=21, stream=W.S_MAX, layout="aos")
+    X = orc.exact.from_rns(x)
+    top = max(X)
+    i0 = X.index(top)
+    # duplicates of the maximum after it: the smallest index must win
+    x[N - 1] = x[i0]
+    x[(i0 + N // 2) % N] = x[i0]
+    val, idx = ctx.rns_max(to_dev(x, layout), layout=layout)
+    assert int(idx.item()) == i0
+    assert orc.exact.from_rns(val.cpu().numpy()[None, :])[0] == top
+    # caller-provided scratch
+    scratch = torch.empty(ctx.max_scratch_size(N), dtype=torch.uint8, device="cuda")
+    val2, idx2 = ctx.rns_max(to_dev(x, layout), layout=layout, scratch=scratch)
+    assert int(idx2.item()) == i0 and torch.equal(val, val2)
+    assert orc.max(x) == i0
+
+
+def test_max_edge_cases(case):
+    tag, ctx, orc, g = case
+    val, idx = ctx.rns_max(torch.empty((0, orc.n), dtype=torch.int32, device="cuda"), layout="aos")
+    assert int(idx.item()) == -1
+    one = orc.exact.to_rns([42])
+    val, idx = ctx.rns_max(to_dev(one, "aos"), layout="aos")
+    assert int(idx.item()) == 0 and orc.exact.from_rns(val.cpu().numpy()[None, :])[0] == 42
+    # all equal, and near-equal values whose intervals overlap
+    x = orc.exact.to_rns([orc.M - 5] * 100 + [orc.M - 4] + [orc.M - 6] * 50)
+    val, idx = ctx.rns_max(to_dev(x, "aos"), layout="aos")
+    assert int(idx.item()) == 100
+
+
+def test_invalid_input_flag(case):
+    tag, ctx, orc, g = case
+    x = orc.exact.to_rns([5, 6])
+    x[1, 0] = orc.moduli[0]  # out of range residue
+    flags = flags_buf(2)
+    out = ctx.rns_eval_compute(to_dev(x, "aos"), layout="aos", flags=flags)
+    f = flags.cpu().numpy()
+    assert f[0] == 0 and f[1] & 1
