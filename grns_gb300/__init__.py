@@ -108,6 +108,21 @@ class RNSContext:
               "grns_ctx_get_table")
         return out
 
+    def set_path(self, path):
+        """"fast" (integer fixed-point enclosures, default) or "reference" (the
+        reference's own FP64 algorithms) for cmp / div / scale2pow / max"""
+        check(native.lib().grns_ctx_set_path(self._h, {"fast": 0, "reference": 1}[path]), "grns_ctx_set_path")
+
+    @staticmethod
+    def device_ceil_log2(xs):
+        """ceil(log2 x) as the device evaluates it in the refinement loop (diagnostics)"""
+        import torch
+        x = torch.as_tensor(np.ascontiguousarray(xs, dtype=np.float64)).cuda()
+        out = torch.empty(x.numel(), dtype=torch.int32, device=x.device)
+        check(native.lib().grns_device_ceil_log2(_ptr(x), _ptr(out), x.numel(), _stream(None)),
+              "grns_device_ceil_log2")
+        return out.cpu().numpy()
+
     # ---- helpers ----
     def _count(self, x, layout):
         if x.dtype.itemsize != 4 or not x.is_cuda or not x.is_contiguous():

@@ -1,0 +1,265 @@
+/*
+ * grns_gb300 -- host computation of a moduli set's constant tables (plain
+ * C++, no CUDA), shared by the device context (ctx.cu) and the CPU checks of
+ * the integer algorithms.
+ *
+ * Reference tables (rns_const_init, kisupov/grns src/rnsbase.cuh:324-451)
+ * reproduced bit for bit without GMP/MPFR: M is only needed as its bit
+ * length and its top 53 bits (MPFR rounds M down to 53 bits before 1/M is
+ * taken), everything else is a product, power or inverse modulo a 31-bit
+ * modulus or a power of two.  Plus the tables of the integer fast path:
+ * fixed-point reciprocals ceil(2^64/m_i), ceil(2^96/m_i), 2^32 mod m_i,
+ * Shoup companions, and the bit lengths of the mixed-radix weights.
+ */
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "rns_common.cuh"
+
+namespace grns {
+
+struct HostTables {
+    int n = 0, log2M = 0;
+    std::vector<uint32_t> m, w, w_sh, mu, bits;
+    std::vector<double> rrd, rru;
+    double acc = 0;
+    int ref_factor = 0;
+    Er unit_low{}, unit_upp{}, inv_unit_low{}, inv_unit_upp{};
+    std::vector<uint32_t> pow2, pow2_sh;          // (log2M+1) x n
+    std::vector<uint32_t> mrc_inv, mrc_inv_sh;    // n x n, [j*n+i] = m_j^-1 mod m_i (j < i)
+    std::vector<uint32_t> mi_pow2, m_pow2, pow2_inv, pow2_inv_sh;  // 30 x n, 30, 30 x n, 30 x n
+    std::vector<uint32_t> c64l, c64h, c96_0, c96_1, c96_2, t32, t32_sh, mrbits;
+    uint64_t E = 0;  // sum_i (m_i - 1)
+};
+
+namespace hostdetail {
+
+inline int64_t inverse_mod(int64_t x, int64_t m) {
+    int64_t a = ((x % m) + m) % m, b = m, x0 = 1, x1 = 0;
+    while (b) {
+        int64_t q = a / b, t = a - q * b;
+        a = b;
+        b = t;
+        t = x0 - q * x1;
+        x0 = x1;
+        x1 = t;
+    }
+    return ((x0 % m) + m) % m;
+}
+
+/* ddiv_rd/ddiv_ru(1, m) with the reference's host rounding (src/dinterval.cuh:124-136):
+ * the round-to-nearest quotient moved by PHI1*|c| + ETA; volatile keeps the
+ * multiply and add unfused. */
+inline double recip_host(double m, bool up) {
+    volatile double c = 1.0 / m;
+    volatile double phi1 = 0x1p-53 * (1.0 + 2.0 * 0x1p-53);
+    volatile double t = phi1 * std::fabs(c);
+    volatile double e = t + 0x1p-1074;
+    return up ? c + e : c - e;
+}
+
+/* directed rounding of 0 < p/q <= 1 to 53 bits, as mpfr_get_d_2exp reports
+ * it: frac in [0.5, 1), value = frac * 2^exp */
+inline void round_ratio(uint64_t p, uint64_t q, bool up, double &frac, int64_t &exp) {
+    const unsigned __int128 lo = (unsigned __int128)1 << 52;
+    int s = 0;
+    while (((unsigned __int128)p << s) / q < lo) s++;
+    unsigned __int128 num = (unsigned __int128)p << s;
+    unsigned __int128 mant = num / q, rem = num % q;
+    if (up && rem) mant += 1;
+    if (mant == ((unsigned __int128)1 << 53)) {
+        mant >>= 1;
+        s -= 1;
+    }
+    frac = std::ldexp((double)(uint64_t)mant, -53);
+    exp = 53 - s;
+}
+
+inline uint32_t shoup(uint32_t v, uint32_t m) { return (uint32_t)(((uint64_t)v << 32) / m); }
+
+}  // namespace hostdetail
+
+/* Fills every table for the moduli m[0..n-1] (odd, pairwise coprime, validated by the caller). */
+inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
+    using namespace hostdetail;
+    T.n = n;
+    T.m.assign(mod, mod + n);
+    const std::vector<uint32_t> &m = T.m;
+    std::vector<uint32_t> M(1, 1u);
+    for (int i = 0; i < n; i++) {
+        uint64_t carry = 0;
+        for (auto &limb : M) {
+            uint64_t t = (uint64_t)limb * m[i] + carry;
+            limb = (uint32_t)t;
+            carry = t >> 32;
+        }
+        if (carry) M.push_back((uint32_t)carry);
+    }
+    int bitlen = 32 * (int)(M.size() - 1);
+    for (uint32_t top = M.back(); top; top >>= 1) bitlen++;
+    T.log2M = bitlen - 1;
+    const int Eb = bitlen > 53 ? bitlen - 53 : 0;
+    uint64_t Top = 0;
+    for (int bit = bitlen - 1; bit >= Eb; bit--) Top = (Top << 1) | ((M[bit / 32] >> (bit % 32)) & 1u);
+
+    T.w.resize(n); T.w_sh.resize(n); T.mu.resize(n); T.bits.resize(n); T.rrd.resize(n); T.rru.resize(n);
+    T.c64l.resize(n); T.c64h.resize(n); T.c96_0.resize(n); T.c96_1.resize(n); T.c96_2.resize(n);
+    T.t32.resize(n); T.t32_sh.resize(n); T.mrbits.resize(n);
+    T.E = 0;
+    for (int i = 0; i < n; i++) {
+        int64_t mi = 1;
+        for (int j = 0; j < n; j++)
+            if (j != i) mi = (mi * (m[j] % m[i])) % m[i];
+        T.w[i] = (uint32_t)inverse_mod(mi, m[i]);
+        T.w_sh[i] = shoup(T.w[i], m[i]);
+        uint32_t b = 0;
+        for (uint32_t v = m[i]; v; v >>= 1) b++;
+        T.bits[i] = b;
+        T.mu[i] = (uint32_t)(((unsigned __int128)1 << (2 * b)) / m[i]);
+        T.rrd[i] = recip_host((double)m[i], false);
+        T.rru[i] = recip_host((double)m[i], true);
+        unsigned __int128 c64 = ((((unsigned __int128)1) << 64) + m[i] - 1) / m[i];
+        T.c64l[i] = (uint32_t)c64;
+        T.c64h[i] = (uint32_t)(c64 >> 32);
+        unsigned __int128 two96 = ((unsigned __int128)1) << 96;
+        unsigned __int128 c96 = (two96 + m[i] - 1) / m[i];
+        T.c96_0[i] = (uint32_t)c96;
+        T.c96_1[i] = (uint32_t)(c96 >> 32);
+        T.c96_2[i] = (uint32_t)(c96 >> 64);
+        T.t32[i] = (uint32_t)((((uint64_t)1) << 32) % m[i]);
+        T.t32_sh[i] = shoup(T.t32[i], m[i]);
+        T.E += m[i] - 1;
+    }
+    /* bit length of P_t = m_0 * ... * m_{t-1} */
+    {
+        std::vector<uint32_t> P(1, 1u);
+        for (int t = 0; t < n; t++) {
+            int bl = 32 * (int)(P.size() - 1);
+            for (uint32_t top = P.back(); top; top >>= 1) bl++;
+            T.mrbits[t] = (uint32_t)bl;
+            uint64_t carry = 0;
+            for (auto &limb : P) {
+                uint64_t v = (uint64_t)limb * m[t] + carry;
+                limb = (uint32_t)v;
+                carry = v >> 32;
+            }
+            if (carry) P.push_back((uint32_t)carry);
+        }
+    }
+    /* RNS_EVAL_ACCURACY, RNS_EVAL_REF_FACTOR (src/rnsbase.cuh:389-391), same operation order */
+    volatile double acc = 4 * std::pow(2.0, 1 - 53);
+    acc = acc * n;
+    acc = acc * std::log2((double)n);
+    acc = acc * (1 + 0.0000001 / 2);
+    acc = acc / 0.0000001;
+    T.acc = acc;
+    T.ref_factor = (int)std::floor(std::log2(1 / (2 * T.acc)));
+    /* RNS_EVAL_UNIT ~ 1/M53 and RNS_EVAL_INV_UNIT ~ 1 - 1/M53 (src/rnsbase.cuh:393-411) */
+    round_ratio(1, Top, false, T.unit_low.frac, T.unit_low.exp);
+    round_ratio(1, Top, true, T.unit_upp.frac, T.unit_upp.exp);
+    T.unit_low.exp -= Eb;
+    T.unit_upp.exp -= Eb;
+    if (Eb == 0) {
+        round_ratio(Top - 1, Top, false, T.inv_unit_low.frac, T.inv_unit_low.exp);
+        round_ratio(Top - 1, Top, true, T.inv_unit_upp.frac, T.inv_unit_upp.exp);
+    } else if (Eb == 1 && Top == ((uint64_t)1 << 52)) {
+        T.inv_unit_low = T.inv_unit_upp = Er{1.0 - 0x1p-53, 0};
+    } else {
+        T.inv_unit_low = Er{1.0 - 0x1p-53, 0};
+        T.inv_unit_upp = Er{0.5, 1};
+    }
+    /* RNS_POW2[j][i] = 2^j mod m_i, with Shoup companions */
+    T.pow2.resize((size_t)(T.log2M + 1) * n);
+    T.pow2_sh.resize(T.pow2.size());
+    for (int i = 0; i < n; i++) {
+        uint64_t v = 1;
+        for (int j = 0; j <= T.log2M; j++) {
+            T.pow2[(size_t)j * n + i] = (uint32_t)v;
+            T.pow2_sh[(size_t)j * n + i] = shoup((uint32_t)v, m[i]);
+            v = (v * 2) % m[i];
+        }
+    }
+    /* MRC_MULT_INV as [j*n + i] = m_j^-1 mod m_i for j < i */
+    T.mrc_inv.assign((size_t)n * n, 0);
+    T.mrc_inv_sh.assign((size_t)n * n, 0);
+    for (int j = 0; j < n; j++)
+        for (int i = j + 1; i < n; i++) {
+            uint32_t v = (uint32_t)inverse_mod(m[j], m[i]);
+            T.mrc_inv[(size_t)j * n + i] = v;
+            T.mrc_inv_sh[(size_t)j * n + i] = shoup(v, m[i]);
+        }
+    /* scaling tables (src/rnsbase.cuh:364-387) */
+    T.mi_pow2.resize((size_t)30 * n);
+    T.m_pow2.resize(30);
+    T.pow2_inv.resize((size_t)30 * n);
+    T.pow2_inv_sh.resize((size_t)30 * n);
+    for (int t = 0; t < 30; t++) {
+        uint64_t mask = ((uint64_t)1 << (t + 1)) - 1, mm = 1;
+        for (int i = 0; i < n; i++) mm = (mm * m[i]) & mask;
+        T.m_pow2[t] = (uint32_t)mm;
+        for (int i = 0; i < n; i++) {
+            uint64_t v = 1;
+            for (int j = 0; j < n; j++)
+                if (j != i) v = (v * m[j]) & mask;
+            T.mi_pow2[(size_t)t * n + i] = (uint32_t)v;
+            uint64_t p2 = ((uint64_t)1 << (t + 1)) % m[i];
+            uint32_t inv = (uint32_t)inverse_mod((int64_t)p2, m[i]);
+            T.pow2_inv[(size_t)t * n + i] = inv;
+            T.pow2_inv_sh[(size_t)t * n + i] = shoup(inv, m[i]);
+        }
+    }
+}
+
+/* The device-table blob (one allocation) and the pointer layout inside it. */
+inline std::vector<uint32_t> table_blob(const HostTables &T) {
+    std::vector<uint32_t> blob;
+    for (const auto *v : {&T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
+                          &T.pow2_inv_sh})
+        blob.insert(blob.end(), v->begin(), v->end());
+    return blob;
+}
+
+/* Fills a Consts<N> whose table pointers address `blob` (device or host copy). */
+template <int N>
+inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob) {
+    for (int i = 0; i < N; i++) {
+        C.m[i] = T.m[i];
+        C.w[i] = T.w[i];
+        C.w_sh[i] = T.w_sh[i];
+        C.mu[i] = T.mu[i];
+        C.b[i] = T.bits[i];
+        C.rrd[i] = T.rrd[i];
+        C.rru[i] = T.rru[i];
+        C.c64l[i] = T.c64l[i];
+        C.c64h[i] = T.c64h[i];
+        C.c96_0[i] = T.c96_0[i];
+        C.c96_1[i] = T.c96_1[i];
+        C.c96_2[i] = T.c96_2[i];
+        C.t32[i] = T.t32[i];
+        C.t32_sh[i] = T.t32_sh[i];
+        C.mrbits[i] = T.mrbits[i];
+    }
+    C.acc = T.acc;
+    C.ref_factor = T.ref_factor;
+    C.log2M = T.log2M;
+    C.unit_low = T.unit_low;
+    C.unit_upp = T.unit_upp;
+    C.inv_unit_low = T.inv_unit_low;
+    C.inv_unit_upp = T.inv_unit_upp;
+    C.m_pow2_res30 = T.m_pow2[29];
+    C.E = T.E;
+    size_t off = 0;
+    C.pow2 = blob + off;        off += T.pow2.size();
+    C.pow2_sh = blob + off;     off += T.pow2_sh.size();
+    C.mrc_inv = blob + off;     off += T.mrc_inv.size();
+    C.mrc_inv_sh = blob + off;  off += T.mrc_inv_sh.size();
+    C.mi_pow2 = blob + off;     off += T.mi_pow2.size();
+    C.m_pow2 = blob + off;      off += T.m_pow2.size();
+    C.pow2_inv = blob + off;    off += T.pow2_inv.size();
+    C.pow2_inv_sh = blob + off;
+}
+
+}  // namespace grns

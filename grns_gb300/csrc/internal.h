@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/grns/grns.h"
+#include "consts_host.h"
 #include "rns_common.cuh"
 
 struct grns_ctx {
@@ -18,24 +19,11 @@ struct grns_ctx {
     int log2M = 0;
     int device = 0;
     int sm_count = 0;
-    std::vector<uint32_t> moduli;
-    /* host copies of the tables (returned by grns_ctx_get_table) */
-    std::vector<uint32_t> w, w_sh, mu, bits;
-    std::vector<double> rrd, rru;
-    double acc = 0;
-    int ref_factor = 0;
-    grns::Er unit_low{}, unit_upp{}, inv_unit_low{}, inv_unit_upp{};
-    std::vector<uint32_t> pow2;              // (log2M+1) x n
-    std::vector<uint32_t> mrc_inv, mrc_inv_sh;  // n x n, [j*n+i] = m_j^-1 mod m_i
-    std::vector<uint32_t> mi_pow2, m_pow2, pow2_inv, pow2_inv_sh;  // 30 x n, 30, 30 x n, 30 x n
-    /* one device allocation holding all tables */
-    void *d_tables = nullptr;
-    /* kernel constant block for this n (a grns::Consts<n>), bytes */
+    int path = 0;  // 0: integer fast path, 1: reference-faithful FP64 kernels (GRNS_PATH_*)
+    grns::HostTables T;  // host copies of all tables
+    void *d_tables = nullptr;  // one device allocation holding the table blob
+    /* kernel constant block for this n (a grns::Consts<n>) */
     alignas(16) unsigned char consts[sizeof(grns::Consts<grns::kMaxModuli>)];
-    /* library-managed scratch (rns_max partials), grown on demand */
-    std::mutex scratch_mu;
-    void *d_scratch = nullptr;
-    size_t scratch_bytes = 0;
 };
 
 namespace grns {

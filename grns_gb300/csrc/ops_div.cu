@@ -7,10 +7,11 @@
  */
 #include "internal.h"
 #include "rns_device.cuh"
+#include "rns_fast.cuh"
 
 namespace grns {
 
-template <int N>
+template <int N, bool FAST>
 __global__ void __launch_bounds__(128) k_div(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d,
                                              int64_t count, Output<N> q, Output<N> r, uint8_t *__restrict__ flags) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
@@ -24,6 +25,8 @@ __global__ void __launch_bounds__(128) k_div(const __grid_constant__ Consts<N> C
         if (f) {
 #pragma unroll
             for (int i = 0; i < N; i++) { qa[i] = 0; ra[i] = 0; }
+        } else if (FAST) {
+            div_fast<N>(C, qa, ra, xa, da, f);
         } else {
             div_ref<N>(C, qa, ra, xa, da, f);
         }
@@ -36,7 +39,7 @@ __global__ void __launch_bounds__(128) k_div(const __grid_constant__ Consts<N> C
     }
 }
 
-template <int N>
+template <int N, bool FAST>
 __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N> C, Operand<N> x,
                                                const uint32_t *__restrict__ D, uint32_t D_uniform, int64_t count,
                                                Output<N> out, uint8_t *__restrict__ flags) {
@@ -51,6 +54,8 @@ __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N>
         if (f) {
 #pragma unroll
             for (int i = 0; i < N; i++) ya[i] = 0;
+        } else if (FAST) {
+            scale_fast<N>(C, ya, xa, dk);
         } else {
             scale2pow_ref<N>(C, ya, xa, dk);
         }
@@ -64,8 +69,12 @@ template <int N>
 static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
                            uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s) {
     const int B = 128;
-    k_div<N><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld}, count,
-                                                    Output<N>{q, ld}, Output<N>{r, ld}, flags);
+    if (c->path == GRNS_PATH_REFERENCE)
+        k_div<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
+                                                               count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
+    else
+        k_div<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
+                                                              count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
     return cuda_status(cudaGetLastError());
 }
 
@@ -73,8 +82,12 @@ template <int N>
 static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
                              int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s) {
     const int B = 128;
-    k_scale<N><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
-                                                      Output<N>{out, ld}, flags);
+    if (c->path == GRNS_PATH_REFERENCE)
+        k_scale<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
+                                                                 Output<N>{out, ld}, flags);
+    else
+        k_scale<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
+                                                                Output<N>{out, ld}, flags);
     return cuda_status(cudaGetLastError());
 }
 

@@ -13,6 +13,7 @@
  */
 #include "internal.h"
 #include "rns_device.cuh"
+#include "rns_fast.cuh"
 
 namespace grns {
 
@@ -21,15 +22,18 @@ struct Cand {
     int64_t idx;  // < 0: empty
 };
 
+/* exact comparison of elements ia, ib (rare: overlapping intervals) */
+template <int N>
+__device__ __noinline__ int ref_tie(const Consts<N> &C, const Operand<N> x, int64_t ia, int64_t ib) {
+    return cmp_tie<N>(C, [&](int i) { return x.load(ia, i); }, [&](int i) { return x.load(ib, i); });
+}
+
 template <int N>
 __device__ __forceinline__ bool better(const Consts<N> &C, const Operand<N> &x, const Cand &a, const Cand &b) {
     if (b.idx < 0) return a.idx >= 0;
     if (a.idx < 0) return false;
     int r = cmp_intervals<N>(a.lo, a.up, b.lo, b.up);
-    if (r == 2) {
-        const int64_t ia = a.idx, ib = b.idx;
-        r = cmp_tie<N>(C, [&](int i) { return x.load(ia, i); }, [&](int i) { return x.load(ib, i); });
-    }
+    if (r == 2) r = ref_tie<N>(C, x, a.idx, b.idx);
     if (r != 0) return r > 0;
     return a.idx < b.idx;
 }
@@ -108,6 +112,84 @@ __global__ void __launch_bounds__(256) k_max(const __grid_constant__ Consts<N> C
     for (int i = threadIdx.x; i < N; i += blockDim.x) out_value[i] = bi >= 0 ? x.load(bi, i) : 0u;
 }
 
+/* ---- fast path: candidates are (64-bit fixed-point fraction, index) ---- */
+struct FCand {
+    uint64_t a;    // sum_i s_i ceil(2^64/m_i) mod 2^64 (>= X/M * 2^64, within E)
+    int64_t idx;   // < 0: empty
+};
+
+/* 96-bit then exact comparison of elements ip, iq (rare: fractions within E) */
+template <int N>
+__device__ __noinline__ int fast_tie(const Consts<N> &C, const Operand<N> x, int64_t ip, int64_t iq) {
+    return cmp_fx96_then_exact<N>(C, [&](int i) { return x.load(ip, i); }, [&](int i) { return x.load(iq, i); });
+}
+
+template <int N>
+__device__ __forceinline__ bool fbetter(const Consts<N> &C, const Operand<N> &x, const FCand &p, const FCand &q) {
+    if (q.idx < 0) return p.idx >= 0;
+    if (p.idx < 0) return false;
+    int r = fx64_order(p.a, q.a, C.E);
+    if (r == 2) r = fast_tie<N>(C, x, p.idx, q.idx);
+    if (r != 0) return r > 0;
+    return p.idx < q.idx;
+}
+
+template <int N>
+__device__ __forceinline__ FCand fblock_reduce(const Consts<N> &C, const Operand<N> &x, FCand best, FCand *sm) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        FCand o{__shfl_xor_sync(0xffffffffu, best.a, off), __shfl_xor_sync(0xffffffffu, best.idx, off)};
+        if (fbetter<N>(C, x, o, best)) best = o;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) sm[wid] = best;
+    __syncthreads();
+    if (wid == 0) {
+        best = lane < nw ? sm[lane] : FCand{0, -1};
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            FCand o{__shfl_xor_sync(0xffffffffu, best.a, off), __shfl_xor_sync(0xffffffffu, best.idx, off)};
+            if (fbetter<N>(C, x, o, best)) best = o;
+        }
+    }
+    return best;
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_max_fast(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+                                                  uint32_t *__restrict__ out_value, int64_t *__restrict__ out_index,
+                                                  unsigned *__restrict__ ticket, FCand *__restrict__ partial) {
+    __shared__ FCand sm[32];
+    __shared__ bool last;
+    FCand best{0, -1};
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        FCand c{fx64<N>(C, [&](int i) { return x.load(k, i); }), k};
+        if (fbetter<N>(C, x, c, best)) best = c;
+    }
+    best = fblock_reduce<N>(C, x, best, sm);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = best;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    best = FCand{0, -1};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        const FCand *p = partial + b;  /* written by other blocks: read through L2 */
+        FCand c{(uint64_t)__ldcg((const unsigned long long *)&p->a), __ldcg((const long long *)&p->idx)};
+        if (fbetter<N>(C, x, c, best)) best = c;
+    }
+    __syncthreads();
+    best = fblock_reduce<N>(C, x, best, sm);
+    if (threadIdx.x == 0) sm[0] = best;
+    __syncthreads();
+    const int64_t bi = sm[0].idx;
+    if (threadIdx.x == 0 && out_index) *out_index = bi;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) out_value[i] = bi >= 0 ? x.load(bi, i) : 0u;
+}
+
 constexpr int kMaxBlock = 256;
 constexpr int kMaxPerSm = 4;
 
@@ -121,8 +203,12 @@ static grns_status run_max(const grns_ctx *c, const uint32_t *x, int64_t ld, int
     unsigned G = max_grid(c, count);
     cudaError_t e = cudaMemsetAsync(scratch, 0, 64, s);
     if (e != cudaSuccess) return cuda_status(e);
-    k_max<N><<<G, kMaxBlock, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, out_value, out_index,
-                                     (unsigned *)scratch, (Cand *)((char *)scratch + 64));
+    if (c->path == GRNS_PATH_REFERENCE)
+        k_max<N><<<G, kMaxBlock, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, out_value, out_index,
+                                         (unsigned *)scratch, (Cand *)((char *)scratch + 64));
+    else
+        k_max_fast<N><<<G, kMaxBlock, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, out_value, out_index,
+                                              (unsigned *)scratch, (FCand *)((char *)scratch + 64));
     return cuda_status(cudaGetLastError());
 }
 

@@ -11,9 +11,10 @@
 namespace grns {
 
 template <int N>
-struct MpInt {  // byte layout of the reference mp_int_t for n = N
+struct MpInt {  // byte layout of the reference mp_int_t for n = N (N even: 4 bytes of padding)
     uint32_t digits[N];
     int32_t sign;
+    int32_t pad;  // written as 0
     Er eval[2];
 };
 static_assert(sizeof(MpInt<8>) == 72 && sizeof(MpInt<32>) == 168 && sizeof(MpInt<64>) == 296, "mp_int_t layout");
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(256) k_mpint(const __grid_constant__ Consts<N>
                                                int64_t count, MpInt<N> *__restrict__ out, uint8_t *__restrict__ flags) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         MpInt<N> a = x[k], b = y[k], r;
+        r.pad = 0;
         uint32_t f = 0;
         if (op == 2) mpint_mul<N>(C, r, a, b, f);
         else mpint_addsub<N>(C, r, a, b, op == 1, f);

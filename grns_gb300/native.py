@@ -22,6 +22,8 @@ SIGNATURES = {
     "grns_ctx_n": (c_int, [c_void_p]),
     "grns_ctx_log2": (c_int, [c_void_p]),
     "grns_ctx_get_table": (c_int, [c_void_p, c_int, c_void_p, c_size_t]),
+    "grns_ctx_set_path": (c_int, [c_void_p, c_int]),
+    "grns_device_ceil_log2": (c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
     "grns_eval": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_cmp": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_div": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),

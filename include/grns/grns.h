@@ -84,6 +84,21 @@ int grns_ctx_log2(const grns_ctx *ctx);
  * (int32[30][n]).  `bytes` must equal the table size. */
 grns_status grns_ctx_get_table(const grns_ctx *ctx, int which, void *host_dst, size_t bytes);
 
+/* Kernel family used by the comparison, division, scaling and maximum calls:
+ * GRNS_PATH_FAST (default) -- integer-pipe fixed-point enclosures with exact
+ * mixed-radix fallback; GRNS_PATH_REFERENCE -- the reference's own GPU
+ * algorithms (FP64 interval evaluation inside cmp, one quotient bit per
+ * division step as src/rnsdiv.cuh:128), one thread per number.  Both give
+ * identical results; eval and mp_int ops are the same in both.  Not to be
+ * changed while calls on the context are being enqueued from other threads. */
+enum { GRNS_PATH_FAST = 0, GRNS_PATH_REFERENCE = 1 };
+grns_status grns_ctx_set_path(grns_ctx *ctx, int path);
+
+/* ceil(log2(x)) as the device computes it inside the evaluation's refinement
+ * loop (src/rnseval.cuh:236 calls CUDA's log2, which is not exact at every
+ * power of two).  Diagnostics for checking; x, out are device arrays. */
+grns_status grns_device_ceil_log2(const double *x, int32_t *out, int64_t count, void *stream);
+
 /* ---- interval evaluation ----
  * out[k] = [low, upp] enclosing X_k / M, bit-identical to
  * cuda::rns_eval_compute (reference src/rnseval.cuh:182). */

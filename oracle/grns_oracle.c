@@ -255,3 +255,8 @@ double oracle_d_op(int op, double a, double b) {
         default: return d_sub_ru(a, b);
     }
 }
+
+/* ceil(log2 x) override support for the device path (see or_ceil_log2_dev) */
+void oracle_log2_record(double *buf, long cap) { or_l2_rec = buf; or_l2_rec_cap = cap; or_l2_rec_n = 0; }
+long oracle_log2_recorded(void) { long n = or_l2_rec_n; or_l2_rec = 0; or_l2_rec_cap = 0; or_l2_rec_n = 0; return n; }
+void oracle_log2_table(const double *xs, const int *cs, long n) { or_l2_tab_x = xs; or_l2_tab_c = cs; or_l2_tab_n = n; }

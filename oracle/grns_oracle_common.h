@@ -139,6 +139,32 @@ static inline int or_er_cmp(const or_er *x, const or_er *y) {
     return ((diff > 0 && x->frac > 0) || (diff < 0 && y->frac < 0)) ? 1 : -1;
 }
 
+/* ---------------- ceil(log2 x) of the device refinement loop ----------------
+ * The reference's GPU refinement (src/rnseval.cuh:236) evaluates
+ * ceil(log2(sumu)) with CUDA's device log2, which is not exact at every power
+ * of two.  The oracle uses the C library's log2 unless the caller supplies the
+ * device's values for the exact inputs met (record mode collects them; the
+ * override table, sorted by x, replays them).  Record/override use is
+ * single-threaded. */
+static double *or_l2_rec = 0;
+static long or_l2_rec_n = 0, or_l2_rec_cap = 0;
+static const double *or_l2_tab_x = 0;
+static const int *or_l2_tab_c = 0;
+static long or_l2_tab_n = 0;
+
+static inline double or_ceil_log2_dev(double x) {
+    if (or_l2_rec_cap && or_l2_rec_n < or_l2_rec_cap) or_l2_rec[or_l2_rec_n++] = x;
+    if (or_l2_tab_n) {
+        long lo = 0, hi = or_l2_tab_n - 1;
+        while (lo <= hi) {
+            long mid = (lo + hi) / 2;
+            if (or_l2_tab_x[mid] == x) return (double)or_l2_tab_c[mid];
+            if (or_l2_tab_x[mid] < x) lo = mid + 1; else hi = mid - 1;
+        }
+    }
+    return ceil(log2(x));
+}
+
 /* ---------------- modular helpers ---------------- */
 /* host mod_mul(x,y,m,d): FP reciprocal trick, may be non-canonical (src/modular.cuh:74) */
 static inline int h_modmul_d(int x, int y, int m) {

@@ -175,7 +175,7 @@ static void OFN(eval_d)(const or_ctx *c, or_iv *out, const int *x) {
     if (sumu >= c->acc) return;
     int K = 0;
     while (sumu < c->acc) {
-        double a = -(ceil(log2(sumu)) + 1);
+        double a = -(or_ceil_log2_dev(sumu) + 1);
         int k = (int)(a > c->ref_factor ? a : (double)c->ref_factor);
         const int *p2 = c->pow2 + (long)k * ON;
         for (int i = 0; i < ON; i++) s[i] = or_modmul(s[i], p2[i], c->m[i]);

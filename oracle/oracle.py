@@ -45,6 +45,9 @@ def lib():
         L.oracle_max.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long]
         L.oracle_d_op.restype = ctypes.c_double
         L.oracle_d_op.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.oracle_log2_recorded.restype = ctypes.c_long
+        L.oracle_log2_record.argtypes = [ctypes.c_void_p, ctypes.c_long]
+        L.oracle_log2_table.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long]
         for name in ("oracle_eval", "oracle_cmp", "oracle_div", "oracle_scale2pow", "oracle_mrc",
                      "oracle_mpint", "oracle_consts"):
             getattr(L, name).restype = None
@@ -101,6 +104,27 @@ class Oracle:
         out = np.zeros(x.shape[0], IV_DTYPE)
         lib().oracle_eval(ctypes.c_void_p(self._h), _p(x), ctypes.c_long(x.shape[0]), _p(out), path, threads)
         return out
+
+    def log2_inputs(self, x, cap=1 << 20):
+        """the distinct values whose ceil(log2) the device-path refinement loop
+        evaluates for these numbers (sorted)"""
+        buf = np.zeros(cap)
+        lib().oracle_log2_record(_p(buf), cap)
+        self.eval(x, path=PATH_DEVICE)
+        n = lib().oracle_log2_recorded()
+        return np.unique(buf[:n])
+
+    def eval_with_device_log2(self, x, xs, cs):
+        """device-path evaluation using the device's ceil(log2 x) values `cs` for inputs `xs`"""
+        xs = np.ascontiguousarray(xs, dtype=np.float64)
+        cs = np.ascontiguousarray(cs, dtype=np.int32)
+        order = np.argsort(xs)
+        xs, cs = xs[order], cs[order]
+        lib().oracle_log2_table(_p(xs), _p(cs), len(xs))
+        try:
+            return self.eval(x, path=PATH_DEVICE)
+        finally:
+            lib().oracle_log2_table(ctypes.c_void_p(0), ctypes.c_void_p(0), 0)
 
     def cmp(self, x, y, path=PATH_DEVICE, threads=1):
         x = np.ascontiguousarray(x, dtype=np.int32)

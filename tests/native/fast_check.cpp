@@ -1,0 +1,79 @@
+// CPU build of the product's integer fast-path algorithms (grns_gb300/csrc/rns_fast.cuh)
+// for exhaustive and randomised checks against exact integer arithmetic.
+// Driven by tests/test_fast_paths.py; arrays are AoS [count][n].
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../../grns_gb300/csrc/consts_host.h"
+#include "../../grns_gb300/csrc/rns_fast.cuh"
+
+using namespace grns;
+
+struct Box {
+    int n;
+    HostTables T;
+    std::vector<uint32_t> blob;
+    alignas(16) unsigned char consts[sizeof(Consts<64>)];
+};
+
+template <int N>
+static const Consts<N> &K(const Box *b) { return *reinterpret_cast<const Consts<N> *>(b->consts); }
+
+#define DISPATCH(n, CALL) switch (n) { case 4: CALL(4); break; case 8: CALL(8); break; case 12: CALL(12); break; \
+    case 16: CALL(16); break; case 32: CALL(32); break; case 64: CALL(64); break; default: return -1; }
+
+extern "C" {
+
+void *fc_create(const uint32_t *m, int n) {
+    Box *b = new Box();
+    b->n = n;
+    build_tables(b->T, m, n);
+    b->blob = table_blob(b->T);
+#define F_(N) fill_consts<N>(*reinterpret_cast<Consts<N> *>(b->consts), b->T, b->blob.data())
+    switch (n) { case 4: F_(4); break; case 8: F_(8); break; case 12: F_(12); break; case 16: F_(16); break;
+                 case 32: F_(32); break; case 64: F_(64); break; default: delete b; return nullptr; }
+#undef F_
+    return b;
+}
+void fc_destroy(void *p) { delete (Box *)p; }
+
+int fc_cmp(void *p, const uint32_t *x, const uint32_t *y, long cnt, int32_t *out) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) out[k] = cmp_fast<N>(K<N>(b), [&](int i) { return x[k * N + i]; }, \
+                                                                [&](int i) { return y[k * N + i]; })
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
+int fc_div(void *p, const uint32_t *x, const uint32_t *d, long cnt, uint32_t *q, uint32_t *r, uint32_t *flags) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) { uint32_t f = 0; div_fast<N>(K<N>(b), q + k * N, r + k * N, x + k * N, \
+                                                                           d + k * N, f); flags[k] = f; }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
+int fc_scale(void *p, const uint32_t *x, const uint32_t *D, long cnt, uint32_t *out) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) scale_fast<N>(K<N>(b), out + k * N, x + k * N, D[k])
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
+/* fixed-point sums for direct checks: frac64 = fx64, and the 128-bit fx96 total */
+int fc_fx(void *p, const uint32_t *x, long cnt, uint64_t *f64, uint64_t *f96lo, uint64_t *f96hi) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) { auto g = [&](int i) { return x[k * N + i]; }; \
+        f64[k] = fx64<N>(K<N>(b), g); u128 t = fx96<N>(K<N>(b), g); f96lo[k] = (uint64_t)t; f96hi[k] = (uint64_t)(t >> 64); }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
+uint64_t fc_E(void *p) { return ((Box *)p)->T.E; }
+
+}

@@ -1,0 +1,143 @@
+"""CPU: the integer fast-path algorithms of the product (grns_gb300/csrc/rns_fast.cuh),
+compiled for the host, against exact big-integer arithmetic.  Tiny moduli sets are
+checked exhaustively (every pair of numbers); the configuration moduli sets on
+seeded random and special inputs.  The GPU runs the identical source."""
+import ctypes
+import os
+import random
+import subprocess
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from grns_gb300 import workload as W
+from tests.helpers import moduli_for
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SMALL_SETS = [[3, 5, 7, 11], [3, 5, 7, 11, 13, 17, 19, 23], [3, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43]]
+
+
+@pytest.fixture(scope="module")
+def fc(tmp_path_factory):
+    out = tmp_path_factory.mktemp("fast") / "libfast.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+                    os.path.join(HERE, "native", "fast_check.cpp"), "-o", str(out)], check=True)
+    L = ctypes.CDLL(str(out))
+    L.fc_create.restype = ctypes.c_void_p
+    L.fc_create.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.fc_destroy.argtypes = [ctypes.c_void_p]
+    L.fc_E.restype = ctypes.c_uint64
+    L.fc_E.argtypes = [ctypes.c_void_p]
+    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx"):
+        getattr(L, f).argtypes = None
+    return L
+
+
+class FC:
+    def __init__(self, L, moduli):
+        self.L, self.moduli, self.n = L, list(moduli), len(moduli)
+        arr = np.array(moduli, np.uint32)
+        self.h = ctypes.c_void_p(L.fc_create(ctypes.c_void_p(arr.ctypes.data), self.n))
+        self.M = 1
+        for m in moduli:
+            self.M *= m
+
+    def res(self, vals):
+        return W.to_residues(vals, self.moduli, layout="aos").astype(np.uint32)
+
+    def ints(self, arr):
+        return W.from_residues(arr, self.moduli, layout="aos")
+
+    @staticmethod
+    def P(a):
+        return ctypes.c_void_p(a.ctypes.data)
+
+    def cmp(self, X, Y):
+        x, y = self.res(X), self.res(Y)
+        out = np.zeros(len(X), np.int32)
+        self.L.fc_cmp(self.h, self.P(x), self.P(y), ctypes.c_long(len(X)), self.P(out))
+        return out
+
+    def div(self, X, D):
+        x, d = self.res(X), self.res(D)
+        q, r = np.zeros_like(x), np.zeros_like(x)
+        fl = np.zeros(len(X), np.uint32)
+        self.L.fc_div(self.h, self.P(x), self.P(d), ctypes.c_long(len(X)), self.P(q), self.P(r), self.P(fl))
+        return self.ints(q), self.ints(r), fl
+
+    def scale(self, X, S):
+        x = self.res(X)
+        s = np.asarray(S, np.uint32)
+        out = np.zeros_like(x)
+        self.L.fc_scale(self.h, self.P(x), self.P(s), ctypes.c_long(len(X)), self.P(out))
+        return self.ints(out)
+
+    def fx(self, X):
+        x = self.res(X)
+        a, lo, hi = (np.zeros(len(X), np.uint64) for _ in range(3))
+        self.L.fc_fx(self.h, self.P(x), ctypes.c_long(len(X)), self.P(a), self.P(lo), self.P(hi))
+        return a, [int(l) + (int(h) << 64) for l, h in zip(lo, hi)]
+
+
+def sgn(a, b):
+    return (a > b) - (a < b)
+
+
+@pytest.mark.parametrize("moduli", SMALL_SETS[:2])
+def test_exhaustive_small_sets(fc, moduli):
+    f = FC(fc, moduli)
+    M = f.M
+    step = max(1, M // 1200)
+    vals = list(range(0, M, step)) + [M - 1, M - 2, 1, 2]
+    X = [a for a in vals for _ in vals]
+    Y = [b for _ in vals for b in vals]
+    assert list(f.cmp(X, Y)) == [sgn(a, b) for a, b in zip(X, Y)]
+    Dv = [b if b else 1 for b in Y]
+    q, r, fl = f.div(X, Dv)
+    assert q == [a // b for a, b in zip(X, Dv)] and r == [a % b for a, b in zip(X, Dv)]
+    assert not fl.any()
+    S = [1 + (k % 40) for k in range(len(X))]
+    assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
+
+
+def test_fixed_point_enclosure(fc):
+    for tag in ("g8", "g32", "g64"):
+        f = FC(fc, moduli_for(tag))
+        E = int(fc.fc_E(f.h))
+        rng = random.Random(3)
+        X = [rng.randrange(f.M) for _ in range(300)] + [0, 1, f.M - 1, f.M // 2]
+        a64, t96 = f.fx(X)
+        for v, a, t in zip(X, a64, t96):
+            frac64 = Fraction(v, f.M) * 2 ** 64
+            U = t % 2 ** 96
+            if int(a) >= E:
+                assert int(a) - E <= frac64 <= int(a)
+            if U >= E:
+                assert U - E <= Fraction(v, f.M) * 2 ** 96 <= U
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+def test_random_and_special(fc, tag):
+    f = FC(fc, moduli_for(tag))
+    M = f.M
+    L = M.bit_length() - 1
+    rng = random.Random(17)
+    N = 400 if f.n <= 16 else 120
+    X = [rng.randrange(M) for _ in range(N)]
+    Y = [rng.randrange(M) for _ in range(N)]
+    # ties, neighbours, tiny and near-M values, powers of two
+    X += [5, M - 1, M - 1, 0, 1, 1 << (L // 2), M // 2, M // 2 + 1] + [1 << j for j in range(0, L, 37)]
+    Y += [5, M - 2, M - 1, 1, 0, (1 << (L // 2)) + 1, M // 2 + 1, M // 2] + [(1 << j) - 1 for j in range(0, L, 37)]
+    Y[3] = X[3] + 1 if X[3] + 1 < M else 0
+    assert list(f.cmp(X, Y)) == [sgn(a, b) for a, b in zip(X, Y)]
+    # division: divisor bit length uniform in [1, L], plus edge cases
+    Dv = [rng.randrange(1 << (b - 1), 1 << b) for b in (rng.randrange(1, L + 1) for _ in range(len(X)))]
+    Dv[:6] = [1, 2, M - 1, X[3], X[4] + 1 if X[4] + 1 < M else 1, (M - 1) // 2]
+    q, r, fl = f.div(X, Dv)
+    assert q == [a // b for a, b in zip(X, Dv)]
+    assert r == [a % b for a, b in zip(X, Dv)]
+    assert not fl.any()
+    S = [rng.randrange(1, min(901, L + 40)) for _ in range(len(X))]
+    S[:5] = [1, 29, 30, 31, L]
+    assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
