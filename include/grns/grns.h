@@ -43,7 +43,8 @@ typedef enum {
     GRNS_ERR_OUT_OF_MEMORY = 4,
     GRNS_ERR_TIMEOUT = 5,       /* a bounded wait ran out */
     GRNS_ERR_REJECTED = 6,      /* admission refused (serving) */
-    GRNS_ERR_BUSY = 7
+    GRNS_ERR_BUSY = 7,
+    GRNS_ERR_TOO_LARGE = 8      /* the request needs more than a fixed capacity */
 } grns_status;
 
 typedef enum { GRNS_LAYOUT_SOA = 0, GRNS_LAYOUT_AOS = 1 } grns_layout;
@@ -149,6 +150,24 @@ grns_status grns_mpint_mul(grns_ctx *ctx, const void *x, const void *y, int64_t 
 grns_status grns_max_scratch_size(const grns_ctx *ctx, int64_t count, size_t *bytes);
 grns_status grns_max(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, int32_t *out_value,
                      int64_t *out_index, void *scratch, size_t scratch_bytes, void *stream);
+
+/* ---- maximum without allocating ----
+ * No counterpart in the reference.  Same results as grns_max, for callers
+ * that cannot allocate device memory at call time: processes whose device
+ * memory belongs to another allocator with a fixed budget, and
+ * latency-critical callers that cannot accept cudaMalloc/cudaFree (which may
+ * synchronise the device).  The scratch is a fixed area inside the library,
+ * GRNS_NOALLOC_SCRATCH_BYTES per GPU that loads it, held until the process
+ * exits; counts whose launch would need more scratch than that return
+ * GRNS_ERR_TOO_LARGE (on a 152-SM GB300 every count fits: the largest launch
+ * needs 24,384 bytes).
+ * The first call on a GPU looks the area up with that GPU current and should
+ * come before any stream capture.  All calls on a GPU share the area: calls
+ * that overlap on the GPU race, so order them on one stream.  The context's
+ * device must be the current device. */
+#define GRNS_NOALLOC_SCRATCH_BYTES 32768
+grns_status grns_max_noalloc(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, int32_t *out_value,
+                             int64_t *out_index, void *stream);
 
 
 /* ---- seeded synthetic inputs in device memory ----
