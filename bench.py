@@ -156,6 +156,65 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def greedy(n):
+    from math import gcd
+    out, c = [], 2 ** 30 - 1
+    while len(out) < n:
+        if c % 2 and all(gcd(c, m) == 1 for m in out):
+            out.append(c)
+        c -= 1
+    return out
+
+
+def run_only(args):
+    """one op on a (small) seeded case, for ncu captures"""
+    import ctypes
+    import torch
+    import grns_gb300 as G
+    from grns_gb300 import native
+    from grns_gb300.workload import S_X, S_Y
+    L = native.lib(build_if_missing=True)
+    n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "mpint64": 64}[args.only]
+    ctx = G.RNSContext(greedy(n))
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    cnt = args.pairs
+    x = torch.empty((n, cnt), dtype=torch.int32, device="cuda")
+    y = torch.empty_like(x)
+    native.check(L.grns_gen_uniform(ctx.handle, SEED, S_X, cnt, 0, P(x), sp))
+    if args.only == "div":
+        native.check(L.grns_gen_divisors(ctx.handle, SEED, cnt, 0, P(y), sp))
+    else:
+        native.check(L.grns_gen_uniform(ctx.handle, SEED, S_Y, cnt, 0, P(y), sp))
+    D = torch.empty(cnt, dtype=torch.int32, device="cuda")
+    native.check(L.grns_gen_shifts(SEED, cnt, DMAX, P(D), sp))
+    a, b = torch.empty_like(x), torch.empty_like(x)
+    out = torch.empty(cnt * 32, dtype=torch.uint8, device="cuda")
+    val = torch.empty(n, dtype=torch.int32, device="cuda")
+    idx = torch.empty(1, dtype=torch.int64, device="cuda")
+    mb = G.mpint_bytes(n)
+    if args.only == "mpint64":
+        from grns_gb300.workload import mpint_values  # operands: residues of random ints below 2^950
+        ma = torch.zeros(cnt * mb, dtype=torch.uint8, device="cuda")
+        mc = torch.zeros_like(ma)
+        mo = torch.zeros_like(ma)
+    for _ in range(args.warmup + args.steps):
+        if args.only == "div":
+            native.check(L.grns_div(ctx.handle, P(x), P(y), cnt, 0, P(a), P(b), None, sp))
+        elif args.only == "scale":
+            native.check(L.grns_scale2pow(ctx.handle, P(x), P(D), 0, cnt, 0, P(a), None, sp))
+        elif args.only in ("cmp32", "cmp8"):
+            native.check(L.grns_cmp(ctx.handle, P(x), P(y), cnt, 0, P(D), None, sp))
+        elif args.only == "max64":
+            native.check(L.grns_max(ctx.handle, P(x), cnt, 0, P(val), P(idx), None, 0, sp))
+        elif args.only == "eval32":
+            native.check(L.grns_eval(ctx.handle, P(x), cnt, 0, P(out), None, sp))
+        elif args.only == "mpint64":
+            native.check(L.grns_mpint_mul(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
+    torch.cuda.synchronize()
+    print(f"ok: {args.only} on {cnt} numbers x {args.warmup + args.steps}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -163,10 +222,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="grns_gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
+    ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "mpint64"], default=None,
+                    help="profiling: run just this op --warmup + --steps times on --pairs numbers, no JSON line")
     args = ap.parse_args()
-    args.warmup = max(3, args.warmup)
+    args.warmup = max(3, args.warmup) if args.only is None else args.warmup
     if args.impl == "reference":
         return run_reference(args)
+    if args.only:
+        return run_only(args)
 
     import torch
     import grns_gb300 as G
@@ -175,15 +239,6 @@ def main():
     L = native.lib(build_if_missing=True)
     from grns_gb300.workload import S_X, S_Y
     import ctypes
-
-    def greedy(n):
-        from math import gcd
-        out, c = [], 2 ** 30 - 1
-        while len(out) < n:
-            if c % 2 and all(gcd(c, m) == 1 for m in out):
-                out.append(c)
-            c -= 1
-        return out
 
     ctx = G.RNSContext(greedy(N32))
     dev = torch.device("cuda", local)
