@@ -32,6 +32,7 @@ struct HostTables {
     std::vector<uint32_t> mrc_inv, mrc_inv_sh;    // n x n, [j*n+i] = m_j^-1 mod m_i (j < i)
     std::vector<uint32_t> mi_pow2, m_pow2, pow2_inv, pow2_inv_sh;  // 30 x n, 30, 30 x n, 30 x n
     std::vector<uint32_t> c64l, c64h, c96_0, c96_1, c96_2, t32, t32_sh, mrbits;
+    std::vector<uint32_t> c96k;  // (log2M+1) x n x 4 words: ceil(2^96 (2^k w_i mod m_i)/m_i) mod 2^96, 0
     uint64_t E = 0;  // sum_i (m_i - 1)
 };
 
@@ -121,7 +122,7 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
         T.mu[i] = (uint32_t)(((unsigned __int128)1 << (2 * b)) / m[i]);
         T.rrd[i] = recip_host((double)m[i], false);
         T.rru[i] = recip_host((double)m[i], true);
-        unsigned __int128 c64 = ((((unsigned __int128)1) << 64) + m[i] - 1) / m[i];
+        unsigned __int128 c64 = ((((unsigned __int128)T.w[i]) << 64) + m[i] - 1) / m[i];  /* w-folded */
         T.c64l[i] = (uint32_t)c64;
         T.c64h[i] = (uint32_t)(c64 >> 32);
         unsigned __int128 two96 = ((unsigned __int128)1) << 96;
@@ -182,6 +183,18 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
             v = (v * 2) % m[i];
         }
     }
+    /* magnification rows: ceil(2^96 u / m_i) mod 2^96 with u = 2^k w_i mod m_i */
+    T.c96k.assign((size_t)(T.log2M + 1) * n * 4, 0);
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k <= T.log2M; k++) {
+            uint64_t u = ((uint64_t)T.pow2[(size_t)k * n + i] * T.w[i]) % m[i];
+            unsigned __int128 c = ((((unsigned __int128)u) << 96) + m[i] - 1) / m[i];
+            uint32_t *row = &T.c96k[((size_t)k * n + i) * 4];
+            row[0] = (uint32_t)c;
+            row[1] = (uint32_t)(c >> 32);
+            row[2] = (uint32_t)(c >> 64);
+        }
+    }
     /* MRC_MULT_INV as [j*n + i] = m_j^-1 mod m_i for j < i */
     T.mrc_inv.assign((size_t)n * n, 0);
     T.mrc_inv_sh.assign((size_t)n * n, 0);
@@ -215,7 +228,7 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
 
 /* The device-table blob (one allocation) and the pointer layout inside it. */
 inline std::vector<uint32_t> table_blob(const HostTables &T) {
-    std::vector<uint32_t> blob;
+    std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows */
     for (const auto *v : {&T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
                           &T.pow2_inv_sh})
         blob.insert(blob.end(), v->begin(), v->end());
@@ -251,7 +264,8 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     C.inv_unit_upp = T.inv_unit_upp;
     C.m_pow2_res30 = T.m_pow2[29];
     C.E = T.E;
-    size_t off = 0;
+    C.c96k = reinterpret_cast<const uint4 *>(blob);
+    size_t off = T.c96k.size();
     C.pow2 = blob + off;        off += T.pow2.size();
     C.pow2_sh = blob + off;     off += T.pow2_sh.size();
     C.mrc_inv = blob + off;     off += T.mrc_inv.size();

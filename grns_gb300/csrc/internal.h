@@ -14,6 +14,13 @@
 #include "consts_host.h"
 #include "rns_common.cuh"
 
+namespace grns {
+struct Sched {
+    int coop;   // 0 serial (one thread per number), 1 n-threaded lane groups
+    int chunk;  // numbers per warp claim in the batched kernel
+};
+}  // namespace grns
+
 struct grns_ctx {
     int n = 0;
     int log2M = 0;
@@ -22,6 +29,8 @@ struct grns_ctx {
     int path = 0;  // 0: integer fast path, 1: reference-faithful FP64 kernels (GRNS_PATH_*)
     grns::HostTables T;  // host copies of all tables
     void *d_tables = nullptr;  // one device allocation holding the table blob
+    /* batched-kernel schedule per grns_op (eval, cmp, div, scale2pow, max, mp_int add/sub/mul) */
+    grns::Sched sched[8] = {{0, 256}, {0, 1024}, {0, 32}, {0, 64}, {0, 1024}, {0, 256}, {0, 256}, {0, 256}};
     /* kernel constant block for this n (a grns::Consts<n>) */
     alignas(16) unsigned char consts[sizeof(grns::Consts<grns::kMaxModuli>)];
 };

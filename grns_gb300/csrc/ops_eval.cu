@@ -46,30 +46,103 @@ __device__ __noinline__ int fast_tie_cmp(const Consts<N> &C, const Operand<N> x,
     return cmp_fx96_then_exact<N>(C, [&](int i) { return x.load(k, i); }, [&](int i) { return y.load(k, i); });
 }
 
-/* fast path: 64-bit fixed-point enclosures on the integer pipe, exact fallback */
+/* fast path: 64-bit fixed-point enclosures on the integer pipe, exact fallback.
+ * SoA: each thread takes 4 consecutive numbers and reads every modulus slice
+ * with one 128-bit load per operand; AoS: each thread reads its own number
+ * with n/4 128-bit loads.  Register-capped so several blocks stay resident. */
+__device__ __forceinline__ void fx64_acc(uint64_t &a, uint32_t x, uint32_t cl, uint32_t ch) {
+    a += (uint64_t)x * cl;
+    a += (uint64_t)(uint32_t)(x * ch) << 32;
+}
+
 template <int N>
-__global__ void __launch_bounds__(256) k_cmp_fast(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> y,
-                                                  int64_t count, int32_t *__restrict__ out, uint8_t *__restrict__ flags) {
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
-        auto gx = [&](int i) { return x.load(k, i); };
-        auto gy = [&](int i) { return y.load(k, i); };
-        uint64_t a = 0, b = 0;
+__device__ __forceinline__ void cmp_finish(const Consts<N> &C, const Operand<N> &x, const Operand<N> &y, int64_t k,
+                                           uint64_t a, uint64_t b, bool bad, int32_t *out, uint8_t *flags) {
+    int r = fx64_order(a, b, C.E);
+    if (r == 2 && !bad) r = fast_tie_cmp<N>(C, x, y, k);
+    out[k] = bad ? 0 : r;
+    if (flags) flags[k] = bad ? (uint8_t)kFlagInvalidInput : (uint8_t)0;
+}
+
+template <int N>
+__global__ void __launch_bounds__(256, 3) k_cmp_fast_soa4(const __grid_constant__ Consts<N> C, Operand<N> x,
+                                                          Operand<N> y, int64_t count, int32_t *__restrict__ out,
+                                                          uint8_t *__restrict__ flags) {
+    const int64_t quads = count / 4;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < quads; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = 4 * t;
+        uint64_t a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
         uint32_t bad = 0;
 #pragma unroll
         for (int i = 0; i < N; i++) {
-            const uint32_t xi = gx(i), yi = gy(i);
-            bad |= (uint32_t)(xi >= C.m[i]) | (uint32_t)(yi >= C.m[i]);
-            const uint32_t sx = mulmod_shoup(xi, C.w[i], C.w_sh[i], C.m[i]);
-            const uint32_t sy = mulmod_shoup(yi, C.w[i], C.w_sh[i], C.m[i]);
-            a += (uint64_t)sx * C.c64l[i];
-            a += (uint64_t)(uint32_t)(sx * C.c64h[i]) << 32;
-            b += (uint64_t)sy * C.c64l[i];
-            b += (uint64_t)(uint32_t)(sy * C.c64h[i]) << 32;
+            const uint4 xv = __ldcs(reinterpret_cast<const uint4 *>(x.base + (int64_t)i * x.ld + k));
+            const uint4 yv = __ldcs(reinterpret_cast<const uint4 *>(y.base + (int64_t)i * y.ld + k));
+            const uint32_t m = C.m[i], cl = C.c64l[i], ch = C.c64h[i];
+            bad |= (uint32_t)(xv.x >= m) | (uint32_t)(xv.y >= m) | (uint32_t)(xv.z >= m) | (uint32_t)(xv.w >= m);
+            bad |= ((uint32_t)(yv.x >= m) | (uint32_t)(yv.y >= m) | (uint32_t)(yv.z >= m) | (uint32_t)(yv.w >= m));
+            fx64_acc(a[0], xv.x, cl, ch); fx64_acc(a[1], xv.y, cl, ch);
+            fx64_acc(a[2], xv.z, cl, ch); fx64_acc(a[3], xv.w, cl, ch);
+            fx64_acc(b[0], yv.x, cl, ch); fx64_acc(b[1], yv.y, cl, ch);
+            fx64_acc(b[2], yv.z, cl, ch); fx64_acc(b[3], yv.w, cl, ch);
         }
-        int r = fx64_order(a, b, C.E);
-        if (r == 2 && !bad) r = fast_tie_cmp<N>(C, x, y, k);
-        out[k] = bad ? 0 : r;
-        if (flags) flags[k] = bad ? (uint8_t)kFlagInvalidInput : (uint8_t)0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            bool badj = false;
+            if (bad) {  /* rare: find which of the four numbers is invalid */
+#pragma unroll 1
+                for (int i = 0; i < N; i++) badj |= x.load(k + j, i) >= C.m[i] || y.load(k + j, i) >= C.m[i];
+            }
+            cmp_finish<N>(C, x, y, k + j, a[j], b[j], badj, out, flags);
+        }
+    }
+    /* tail: count % 4 numbers */
+    const int64_t tail = 4 * quads + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tail < count) {
+        uint64_t a = 0, b = 0;
+        bool bad = false;
+#pragma unroll 1
+        for (int i = 0; i < N; i++) {
+            const uint32_t xi = x.load(tail, i), yi = y.load(tail, i);
+            bad |= xi >= C.m[i] || yi >= C.m[i];
+            fx64_acc(a, xi, C.c64l[i], C.c64h[i]);
+            fx64_acc(b, yi, C.c64l[i], C.c64h[i]);
+        }
+        cmp_finish<N>(C, x, y, tail, a, b, bad, out, flags);
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> y,
+                                                     int64_t count, int32_t *__restrict__ out,
+                                                     uint8_t *__restrict__ flags) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t a = 0, b = 0;
+        uint32_t bad = 0;
+        if (x.ld == 0 && (N % 4) == 0) {  /* AoS: the number's residues are contiguous */
+            const uint4 *px = reinterpret_cast<const uint4 *>(x.base + k * N);
+            const uint4 *py = reinterpret_cast<const uint4 *>(y.base + k * N);
+#pragma unroll
+            for (int q = 0; q < N / 4; q++) {
+                const uint4 xv = __ldcs(px + q), yv = __ldcs(py + q);
+                const uint32_t xs[4] = {xv.x, xv.y, xv.z, xv.w}, ys[4] = {yv.x, yv.y, yv.z, yv.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int i = 4 * q + j;
+                    bad |= (uint32_t)(xs[j] >= C.m[i]) | (uint32_t)(ys[j] >= C.m[i]);
+                    fx64_acc(a, xs[j], C.c64l[i], C.c64h[i]);
+                    fx64_acc(b, ys[j], C.c64l[i], C.c64h[i]);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                const uint32_t xi = x.load_cs(k, i), yi = y.load_cs(k, i);
+                bad |= (uint32_t)(xi >= C.m[i]) | (uint32_t)(yi >= C.m[i]);
+                fx64_acc(a, xi, C.c64l[i], C.c64h[i]);
+                fx64_acc(b, yi, C.c64l[i], C.c64h[i]);
+            }
+        }
+        cmp_finish<N>(C, x, y, k, a, b, bad != 0, out, flags);
     }
 }
 
@@ -88,9 +161,12 @@ static grns_status run_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t 
     if (c->path == GRNS_PATH_REFERENCE)
         k_cmp<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{y, ld}, count, out,
                                                     flags);
+    else if (ld != 0 && ld % 4 == 0 && ((uintptr_t)x % 16) == 0 && ((uintptr_t)y % 16) == 0)
+        k_cmp_fast_soa4<N><<<grid_for(c, (count + 3) / 4, B, 3), B, 0, s>>>(
+            consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{y, ld}, count, out, flags);
     else
-        k_cmp_fast<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{y, ld}, count,
-                                                         out, flags);
+        k_cmp_fast<N><<<grid_for(c, count, B, 3), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{y, ld},
+                                                            count, out, flags);
     return cuda_status(cudaGetLastError());
 }
 

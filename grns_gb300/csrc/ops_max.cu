@@ -156,15 +156,45 @@ __device__ __forceinline__ FCand fblock_reduce(const Consts<N> &C, const Operand
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_max_fast(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+__global__ void __launch_bounds__(256, 3) k_max_fast(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
                                                   uint32_t *__restrict__ out_value, int64_t *__restrict__ out_index,
                                                   unsigned *__restrict__ ticket, FCand *__restrict__ partial) {
     __shared__ FCand sm[32];
     __shared__ bool last;
     FCand best{0, -1};
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
-        FCand c{fx64<N>(C, [&](int i) { return x.load(k, i); }), k};
-        if (fbetter<N>(C, x, c, best)) best = c;
+    if (x.ld != 0 && x.ld % 4 == 0 && ((uintptr_t)x.base % 16) == 0) {
+        /* SoA: 4 consecutive numbers per thread, one 128-bit load per modulus slice */
+        const int64_t quads = count / 4;
+        for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < quads;
+             t += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t k = 4 * t;
+            uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+                const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(x.base + (int64_t)i * x.ld + k));
+                const uint32_t cl = C.c64l[i], ch = C.c64h[i];
+                a0 += (uint64_t)v.x * cl; a0 += (uint64_t)(uint32_t)(v.x * ch) << 32;
+                a1 += (uint64_t)v.y * cl; a1 += (uint64_t)(uint32_t)(v.y * ch) << 32;
+                a2 += (uint64_t)v.z * cl; a2 += (uint64_t)(uint32_t)(v.z * ch) << 32;
+                a3 += (uint64_t)v.w * cl; a3 += (uint64_t)(uint32_t)(v.w * ch) << 32;
+            }
+            FCand c0{a0, k}, c1{a1, k + 1}, c2{a2, k + 2}, c3{a3, k + 3};
+            if (fbetter<N>(C, x, c0, best)) best = c0;
+            if (fbetter<N>(C, x, c1, best)) best = c1;
+            if (fbetter<N>(C, x, c2, best)) best = c2;
+            if (fbetter<N>(C, x, c3, best)) best = c3;
+        }
+        for (int64_t k = 4 * quads + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count;
+             k += (int64_t)gridDim.x * blockDim.x) {
+            FCand c{fx64<N>(C, [&](int i) { return x.load(k, i); }), k};
+            if (fbetter<N>(C, x, c, best)) best = c;
+        }
+    } else {
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count;
+             k += (int64_t)gridDim.x * blockDim.x) {
+            FCand c{fx64<N>(C, [&](int i) { return x.load(k, i); }), k};
+            if (fbetter<N>(C, x, c, best)) best = c;
+        }
     }
     best = fblock_reduce<N>(C, x, best, sm);
     if (threadIdx.x == 0) {

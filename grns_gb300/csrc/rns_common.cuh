@@ -22,6 +22,10 @@
 #define GRNS_HD inline
 #endif
 
+#ifndef __CUDACC__
+struct uint4 { uint32_t x, y, z, w; };
+#endif
+
 namespace grns {
 
 constexpr int kMaxModuli = 64;
@@ -47,14 +51,16 @@ struct Consts {
     int log2M;            // floor(log2 M), the RNS_MODULI_PRODUCT_LOG2 convention
     Er unit_low, unit_upp, inv_unit_low, inv_unit_upp;  // RNS_EVAL_UNIT, RNS_EVAL_INV_UNIT
     uint32_t m_pow2_res30;                // M mod 2^30
-    /* integer fast path */
-    uint32_t c64l[N], c64h[N];            // ceil(2^64 / m_i) = c64h * 2^32 + c64l
-    uint32_t c96_0[N], c96_1[N], c96_2[N];  // ceil(2^96 / m_i), 32-bit words
+    /* integer fast path: fixed-point reciprocals.  "w-folded" constants give
+     * frac(x_i w_i / m_i) directly from the residue x_i (frac(x w / m) = s / m). */
+    uint32_t c64l[N], c64h[N];            // ceil(2^64 w_i / m_i) mod 2^64 (w-folded)
+    uint32_t c96_0[N], c96_1[N], c96_2[N];  // ceil(2^96 / m_i), 32-bit words (applied to s_i)
     uint32_t t32[N], t32_sh[N];           // 2^32 mod m_i, Shoup companion
     uint32_t mrbits[N];                   // bit length of m_0 * ... * m_{t-1}
     uint64_t E;                           // sum_i (m_i - 1): fixed-point truncation error bound
     const uint32_t *pow2;       // [(log2M + 1) * N]  2^j mod m_i        (RNS_POW2)
     const uint32_t *pow2_sh;    // [(log2M + 1) * N]  Shoup companions
+    const uint4 *c96k;          // [(log2M + 1) * N]  ceil(2^96 (2^k w_i mod m_i) / m_i) mod 2^96 (w-folded, x 2^k)
     const uint32_t *mrc_inv;    // [N * N]  [j * N + i] = m_j^-1 mod m_i (MRC_MULT_INV)
     const uint32_t *mrc_inv_sh; // [N * N]  Shoup companions
     const uint32_t *mi_pow2;    // [30 * N] M_i mod 2^(j+1)             (RNS_PART_MODULI_PRODUCT_POW2_RESIDUES)

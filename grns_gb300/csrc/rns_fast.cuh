@@ -75,20 +75,23 @@ GRNS_HD uint32_t reduce64(const Consts<N> &C, int i, uint64_t v) {
 
 /* ---------------- fixed-point sums ---------------- */
 
-/* sum_i s_i * ceil(2^64/m_i) mod 2^64, s_i = get(i) * w_i mod m_i */
+/* sum_i x_i * ceil(2^64 w_i / m_i) mod 2^64: within E above 2^64 * frac(X/M)
+ * (frac(x w / m) = s / m, so folding w_i into the constant needs no modular
+ * multiplication; the truncation error is below sum x_i <= E) */
 template <int N, class Get>
 GRNS_HD uint64_t fx64(const Consts<N> &C, Get get) {
     uint64_t a = 0;
 #pragma unroll
     for (int i = 0; i < N; i++) {
-        uint32_t s = mulmod_shoup(get(i), C.w[i], C.w_sh[i], C.m[i]);
-        a += (uint64_t)s * C.c64l[i];
-        a += (uint64_t)(uint32_t)(s * C.c64h[i]) << 32;
+        const uint32_t x = get(i);
+        a += (uint64_t)x * C.c64l[i];
+        a += (uint64_t)(uint32_t)(x * C.c64h[i]) << 32;
     }
     return a;
 }
 
-/* sum_i s_i * ceil(2^96/m_i) exactly (no wrap); s_i = gets(i) given directly */
+/* sum_i s_i * ceil(2^96/m_i) exactly (no wrap; integer part in bits 96..);
+ * s_i = gets(i) given directly -- used where the integer part is needed */
 template <int N, class GetS>
 GRNS_HD u128 fx96_s(const Consts<N> &C, GetS gets) {
     uint64_t S0 = 0, S1 = 0, S2 = 0;
@@ -105,9 +108,32 @@ GRNS_HD u128 fx96_s(const Consts<N> &C, GetS gets) {
     return (u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64);
 }
 
+/* sum_i x_i * c96k[k][i] mod 2^96: within E above 2^96 * frac(X 2^k / M) */
+template <int N, class Get>
+GRNS_HD u128 fx96_k(const Consts<N> &C, Get get, int k) {
+    const uint4 *row = C.c96k + (int64_t)k * N;
+    uint64_t S0 = 0, S1 = 0;
+    uint32_t S2 = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t x = get(i);
+#ifdef __CUDA_ARCH__
+        const uint4 c = __ldg(row + i);
+#else
+        const uint4 c = row[i];
+#endif
+        uint64_t p0 = (uint64_t)x * c.x;
+        uint64_t p1 = (uint64_t)x * c.y;
+        S0 += (uint32_t)p0;
+        S1 += (p0 >> 32) + (uint32_t)p1;
+        S2 += (uint32_t)(p1 >> 32) + x * c.z;
+    }
+    return ((u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64)) & kMask96;
+}
+
 template <int N, class Get>
 GRNS_HD u128 fx96(const Consts<N> &C, Get get) {
-    return fx96_s<N>(C, [&](int i) { return mulmod_shoup(get(i), C.w[i], C.w_sh[i], C.m[i]); });
+    return fx96_k<N>(C, get, 0);
 }
 
 /* ---------------- mixed-radix conversion (exact) ---------------- */
@@ -155,7 +181,7 @@ GRNS_HD int fx64_order(uint64_t a, uint64_t b, uint64_t E) {
 
 template <int N, class GetX, class GetY>
 GRNS_HD int cmp_fx96_then_exact(const Consts<N> &C, GetX gx, GetY gy) {
-    u128 tx = fx96<N>(C, gx) & kMask96, ty = fx96<N>(C, gy) & kMask96;
+    u128 tx = fx96<N>(C, gx), ty = fx96<N>(C, gy);
     const u128 E = C.E;
     if (tx >= E && ty >= E) {
         if (tx - E > ty) return 1;
@@ -192,12 +218,7 @@ GRNS_HD Norm norm96(const Consts<N> &C, Get get, int k0, uint32_t &flags) {
 #pragma unroll 1
     for (int guard = 0; guard < 64; guard++) {
         if (k < 0 || k > C.log2M) break;
-        const uint32_t *p2 = C.pow2 + (int64_t)k * N;
-        const uint32_t *p2s = C.pow2_sh + (int64_t)k * N;
-        u128 U = fx96_s<N>(C, [&](int i) {
-                     uint32_t s = mulmod_shoup(get(i), C.w[i], C.w_sh[i], C.m[i]);
-                     return k ? mulmod_shoup(s, ldg_u32(p2 + i), ldg_u32(p2s + i), C.m[i]) : s;
-                 }) & kMask96;
+        u128 U = fx96_k<N>(C, get, k);
         if (U >= lower) return Norm{U, k, 0};
         if (U >= E) {
             k += 89 - bitlen128(U);
@@ -283,7 +304,17 @@ GRNS_HD bool floor_scaled_residues(const Consts<N> &C, uint64_t F, int s, uint32
     const uint32_t *p2s = C.pow2_sh + (int64_t)e * N;
 #pragma unroll 1
     for (int i = 0; i < N; i++) {
-        uint32_t v = reduce64<N>(C, i, base);
+        uint32_t v;
+        if (C.b[i] >= 27) {  /* base < 2^53: hi * (2^32 mod m) + lo < 2^54 <= 2^(2b), one Barrett step */
+            uint64_t p = (uint64_t)(uint32_t)(base >> 32) * C.t32[i] + (uint32_t)base;
+            uint32_t t = (uint32_t)(p >> (C.b[i] - 1));
+            uint32_t q = (uint32_t)(((uint64_t)t * C.mu[i]) >> (C.b[i] + 1));
+            uint32_t r = (uint32_t)p - q * C.m[i];
+            r = umin32(r, r - C.m[i]);
+            v = umin32(r, r - C.m[i]);
+        } else {
+            v = reduce64<N>(C, i, base);
+        }
         pq[i] = e ? mulmod_shoup(v, ldg_u32(p2 + i), ldg_u32(p2s + i), C.m[i]) : v;
     }
     return true;

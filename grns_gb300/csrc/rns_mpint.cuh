@@ -1,0 +1,79 @@
+/*
+ * grns_gb300 -- multiple-precision integers (mp_int_t, reference layout
+ * src/types.cuh:45): add / sub / mul with the interval evaluation derived
+ * from the operands' evaluations, as cuda::mpint_add / mpint_sub /
+ * mpint_mul (reference src/mpint.cuh:336/:407/:478).  Overflow becomes flag
+ * bits (the reference prints from the device).
+ */
+#pragma once
+
+#include "rns_device.cuh"
+
+namespace grns {
+
+template <int N>
+struct MpInt {  // byte layout of the reference mp_int_t for n = N (N even: 4 bytes of padding)
+    uint32_t digits[N];
+    int32_t sign;
+    int32_t pad;  // written as 0
+    Er eval[2];
+};
+static_assert(sizeof(MpInt<8>) == 72 && sizeof(MpInt<32>) == 168 && sizeof(MpInt<64>) == 296, "mp_int_t layout");
+
+__device__ __forceinline__ double neg_if(double v, bool neg) { return neg ? -v : v; }
+
+template <int N>
+__device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, const MpInt<N> &x, const MpInt<N> &y,
+                                             bool sub, uint32_t &flags) {
+    const int sx = x.sign, sy = sub ? (y.sign ^ 1) : y.sign;
+    Er evx[2] = {x.eval[0], x.eval[1]}, evy[2] = {y.eval[0], y.eval[1]};
+    uint32_t dig[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = C.m[i], a = x.digits[i], b = y.digits[i];
+        flags |= (a >= m || b >= m) ? kFlagInvalidInput : 0u;
+        uint32_t sa = sx ? submod(0u, a, m) : a;
+        uint32_t sb = sy ? submod(0u, b, m) : b;
+        dig[i] = addmod(sa, sb, m);
+    }
+    evx[0].frac = neg_if(evx[0].frac, sx);
+    evx[1].frac = neg_if(evx[1].frac, sx);
+    evy[0].frac = neg_if(evy[0].frac, sy);
+    evy[1].frac = neg_if(evy[1].frac, sy);
+    Er lo = er_add_dir<false>(evx[sx], evy[sy]);
+    Er up = er_add_dir<true>(evx[1 - sx], evy[1 - sy]);
+    const bool minus = lo.frac < 0 && up.frac < 0;
+    res.sign = minus;
+    if (minus) {
+#pragma unroll
+        for (int i = 0; i < N; i++) dig[i] = dig[i] ? C.m[i] - dig[i] : 0u;
+        Er t = lo;
+        lo = Er{-up.frac, up.exp};
+        up = Er{-t.frac, t.exp};
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++) res.digits[i] = dig[i];
+    res.eval[0] = lo;
+    res.eval[1] = up;
+    flags |= overflow_flags<N>(C, lo, up);
+}
+
+template <int N>
+__device__ __forceinline__ void mpint_mul(const Consts<N> &C, MpInt<N> &res, const MpInt<N> &x, const MpInt<N> &y,
+                                          uint32_t &flags) {
+    res.eval[0] = er_md<false>(x.eval[0], y.eval[0], C.unit_upp);
+    res.eval[1] = er_md<true>(x.eval[1], y.eval[1], C.unit_low);
+    bool zero = true;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = C.m[i], a = x.digits[i], b = y.digits[i];
+        flags |= (a >= m || b >= m) ? kFlagInvalidInput : 0u;
+        uint32_t v = mulmod_barrett(a, b, m, C.mu[i], C.b[i]);
+        res.digits[i] = v;
+        zero &= v == 0;
+    }
+    res.sign = zero ? 0 : (x.sign ^ y.sign);
+    flags |= overflow_flags<N>(C, res.eval[0], res.eval[1]);
+}
+
+}  // namespace grns

@@ -34,10 +34,34 @@ SIGNATURES = {
     "grns_max_scratch_size": (c_int, [c_void_p, c_int64, ctypes.POINTER(c_size_t)]),
     "grns_max": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "grns_max_noalloc": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "grns_batch_create": (c_int, [c_void_p, c_void_p, c_int, c_int, ctypes.POINTER(c_void_p)]),
+    "grns_batch_update": (c_int, [c_void_p, c_void_p, c_int]),
+    "grns_batch_launch": (c_int, [c_void_p, c_void_p]),
+    "grns_batch_destroy": (c_int, [c_void_p]),
+    "grns_batch_chunks": (c_int64, [c_void_p]),
+    "grns_batch_grid": (c_int, [c_void_p]),
+    "grns_ctx_get_schedule": (c_int, [c_void_p, c_int, c_void_p]),
+    "grns_ctx_set_schedule": (c_int, [c_void_p, c_int, c_void_p]),
+    "grns_autotune": (c_int, [c_void_p, c_int, c_int64, ctypes.c_char_p, c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "grns_autotune_load": (c_int, [c_void_p, ctypes.c_char_p, ctypes.POINTER(c_int)]),
     "grns_gen_uniform": (c_int, [c_void_p, ctypes.c_uint64, c_uint32, c_int64, c_int, c_void_p, c_void_p]),
     "grns_gen_divisors": (c_int, [c_void_p, ctypes.c_uint64, c_int64, c_int, c_void_p, c_void_p]),
     "grns_gen_shifts": (c_int, [ctypes.c_uint64, c_int64, c_uint32, c_void_p, c_void_p]),
 }
+
+
+class Job(ctypes.Structure):
+    """grns_job (include/grns/grns.h)"""
+    _fields_ = [("op", ctypes.c_int32), ("layout", ctypes.c_int32), ("count", ctypes.c_int64),
+                ("a", c_void_p), ("b", c_void_p), ("out0", c_void_p), ("out1", c_void_p),
+                ("flags", c_void_p), ("D_uniform", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class Schedule(ctypes.Structure):
+    _fields_ = [("coop", ctypes.c_int32), ("chunk", ctypes.c_int32)]
+
+
+OP_EVAL, OP_CMP, OP_DIV, OP_SCALE2POW, OP_MAX, OP_MPINT_ADD, OP_MPINT_SUB, OP_MPINT_MUL = range(8)
 
 
 class GrnsError(RuntimeError):

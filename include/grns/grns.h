@@ -170,6 +170,62 @@ grns_status grns_max_noalloc(grns_ctx *ctx, const int32_t *x, int64_t count, int
                              int64_t *out_index, void *stream);
 
 
+/* ---- batching: many uneven-length arrays in one persistent launch ----
+ * No counterpart in the reference, whose callers launch one kernel per array
+ * (e.g. tests/test_perf_rnscmp.cu:156).  A batch fixes a list of jobs; each
+ * launch runs all of them in ONE persistent kernel (warps pull chunks with an
+ * atomic counter; evaluations stay in registers; heaviest jobs first),
+ * optionally replayed from a CUDA graph captured on the first launch (needs a
+ * non-NULL stream).  Per job: */
+typedef enum {
+    GRNS_OP_EVAL = 0,       /* a: x;  out0: interval_t[count] */
+    GRNS_OP_CMP = 1,        /* a: x, b: y;  out0: int32[count] */
+    GRNS_OP_DIV = 2,        /* a: x, b: d;  out0: q, out1: r */
+    GRNS_OP_SCALE2POW = 3,  /* a: x, b: uint32 D[count] or NULL (D_uniform);  out0: result */
+    GRNS_OP_MAX = 4,        /* a: x;  out0: int32[n] value, out1: int64 index (or NULL) */
+    GRNS_OP_MPINT_ADD = 5,  /* a, b, out0: mp_int_t arrays */
+    GRNS_OP_MPINT_SUB = 6,
+    GRNS_OP_MPINT_MUL = 7
+} grns_op;
+
+typedef struct {
+    int32_t op;       /* grns_op */
+    int32_t layout;   /* GRNS_LAYOUT_SOA / GRNS_LAYOUT_AOS for RNS arrays */
+    int64_t count;
+    const void *a, *b;
+    void *out0, *out1;
+    uint8_t *flags;   /* optional per-element flags */
+    uint32_t D_uniform;
+    uint32_t reserved;
+} grns_job;
+
+typedef struct grns_batch grns_batch;
+grns_status grns_batch_create(grns_ctx *ctx, const grns_job *jobs, int njobs, int use_graph, grns_batch **out);
+/* new pointers for the same job shapes (op, count, layout); keeps the graph */
+grns_status grns_batch_update(grns_batch *batch, const grns_job *jobs, int njobs);
+grns_status grns_batch_launch(grns_batch *batch, void *stream);
+grns_status grns_batch_destroy(grns_batch *batch);
+int64_t grns_batch_chunks(const grns_batch *batch);
+int grns_batch_grid(const grns_batch *batch);
+
+/* Per-op schedule of the batched kernel: coop = 0 one thread per number
+ * ("serial"), 1 the n residues of a number spread over a lane group
+ * ("n-threaded", cmp and max only); chunk = numbers per warp claim. */
+typedef struct {
+    int32_t coop;
+    int32_t chunk;
+} grns_schedule;
+grns_status grns_ctx_get_schedule(const grns_ctx *ctx, int op, grns_schedule *out);
+grns_status grns_ctx_set_schedule(grns_ctx *ctx, int op, const grns_schedule *sched);
+
+/* Autotuner: times the candidate schedules of `op` on `count` synthetic
+ * numbers of this moduli set in a single-job batch, keeps the fastest in the
+ * context and appends it to the text cache `cache_path` (may be NULL);
+ * grns_autotune_load applies the cached choices for this GPU and moduli count. */
+grns_status grns_autotune(grns_ctx *ctx, int op, int64_t count, const char *cache_path, grns_schedule *chosen,
+                          double *best_ms);
+grns_status grns_autotune_load(grns_ctx *ctx, const char *cache_path, int *applied);
+
 /* ---- seeded synthetic inputs in device memory ----
  * No counterpart in the reference (its tests draw from GMP's Mersenne
  * Twister seeded with time(NULL), tests/tsthelper.cuh:33).  Counter-based

@@ -253,3 +253,17 @@ def test_invalid_input_flag(case):
     out = ctx.rns_eval_compute(to_dev(x, "aos"), layout="aos", flags=flags)
     f = flags.cpu().numpy()
     assert f[0] == 0 and f[1] & 1
+
+
+@pytest.mark.parametrize("count", [1, 2, 3, 5, 4097])
+def test_vector_paths_with_tails(case, count):
+    """SoA counts not divisible by 4 (the 128-bit load paths plus scalar tails)"""
+    tag, ctx, orc, g = case
+    x = W.uniform_residues(orc.moduli, count, seed=31, stream=W.S_X, layout="aos")
+    y = W.uniform_residues(orc.moduli, count, seed=31, stream=W.S_Y, layout="aos")
+    y[count // 2] = x[count // 2]
+    got = ctx.rns_cmp(to_dev(x, "soa"), to_dev(y, "soa"), layout="soa").cpu().numpy()
+    assert np.array_equal(got, orc.cmp(x, y, path=O.PATH_DEVICE))
+    x[count - 1] = x[0]  # a repeated value at the tail
+    val, idx = ctx.rns_max(to_dev(x, "soa"), layout="soa")
+    assert int(idx.item()) == orc.max(x)
