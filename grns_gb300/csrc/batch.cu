@@ -34,9 +34,11 @@ namespace grns {
 struct JobDev {
     int32_t op, layout;
     int64_t count;
+    int64_t ld;  // SoA input leading dimension
     const uint32_t *a, *b;
     void *out0, *out1;
     uint8_t *flags;
+    const Er *eval_a, *eval_b;  // cmp: optional cached evaluations (2 Er per number)
     uint32_t D_uniform;
     int32_t coop;
     int64_t chunk_begin;   // first global chunk of this job
@@ -121,8 +123,9 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
                                           unsigned *done, Part *partials) {
     const int64_t start = (c - J.chunk_begin) * (int64_t)J.chunk_elems;
     const int64_t end = min(start + (int64_t)J.chunk_elems, J.count);
-    const int64_t ld = J.layout == GRNS_LAYOUT_SOA ? (J.count > 0 ? J.count : 1) : 0;
-    const Operand<N> x{J.a, ld}, y{J.b, ld};
+    const int64_t ld = J.layout == GRNS_LAYOUT_SOA ? (J.count > 0 ? J.count : 1) : 0;   // outputs
+    const int64_t ldi = J.layout == GRNS_LAYOUT_SOA ? J.ld : 0;                            // inputs
+    const Operand<N> x{J.a, ldi}, y{J.b, ldi};
     switch (J.op) {
         case GRNS_OP_EVAL:
             for (int64_t k = start + lane; k < end; k += 32) {
@@ -153,6 +156,16 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
                 }
             } else {
                 for (int64_t k = start + lane; k < end; k += 32) {
+                    if (J.eval_a && J.eval_b) {  /* cached evaluations decide almost every pair */
+                        const Er xl = J.eval_a[2 * k], xu = J.eval_a[2 * k + 1];
+                        const Er yl = J.eval_b[2 * k], yu = J.eval_b[2 * k + 1];
+                        const int r = cmp_intervals<N>(xl, xu, yl, yu);
+                        if (r != 2) {
+                            ((int32_t *)J.out0)[k] = r;
+                            if (J.flags) J.flags[k] = 0;
+                            continue;
+                        }
+                    }
                     uint64_t a = 0, b = 0;
                     uint32_t bad = 0;
 #pragma unroll
@@ -329,6 +342,7 @@ double op_cost(int op, int n) {
 
 bool job_ok(const grns_ctx *c, const grns_job &jb) {
     if (jb.op < GRNS_OP_EVAL || jb.op > GRNS_OP_MPINT_MUL || jb.count < 0) return false;
+    if (jb.ld != 0 && jb.ld < jb.count) return false;
     if (jb.layout != GRNS_LAYOUT_SOA && jb.layout != GRNS_LAYOUT_AOS) return false;
     if (jb.count == 0) return jb.op != GRNS_OP_MAX || jb.out0;
     if (!jb.a || !jb.out0) return false;
@@ -379,6 +393,9 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
         J.op = u.op;
         J.layout = u.layout;
         J.count = u.count;
+        J.ld = u.ld > 0 ? u.ld : (u.count > 0 ? u.count : 1);
+        J.eval_a = (const Er *)u.eval_a;
+        J.eval_b = (const Er *)u.eval_b;
         J.a = (const uint32_t *)u.a;
         J.b = (const uint32_t *)u.b;
         J.out0 = u.out0;
@@ -407,6 +424,61 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
 }
 
 }  // namespace
+
+namespace grns {
+
+/* One-shot batch for the server: everything stream-ordered on `s`.  The
+ * device job table is staged through `staging` (pinned, at least
+ * batch_staging_bytes(njobs) bytes, not reused until the launch completes),
+ * allocated with cudaMallocAsync and freed with cudaFreeAsync after the
+ * kernel, so nothing here synchronises with other streams. */
+size_t batch_staging_bytes(int njobs) { return sizeof(JobDev) * (size_t)(njobs > 0 ? njobs : 1); }
+
+grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *staging, cudaStream_t s) {
+    grns_batch b;
+    b.ctx = c;
+    b.njobs = njobs;
+    b.order.resize(njobs);
+    for (int t = 0; t < njobs; t++) b.order[t] = t;
+    std::stable_sort(b.order.begin(), b.order.end(), [&](int p, int q) {
+        return op_cost(jobs[p].op, c->n) * (double)jobs[p].count > op_cost(jobs[q].op, c->n) * (double)jobs[q].count;
+    });
+    b.host_jobs.resize(njobs);
+    fill_jobs(&b, jobs);
+    std::memcpy(staging, b.host_jobs.data(), sizeof(JobDev) * njobs);
+    b.counters_bytes = sizeof(unsigned long long) + sizeof(unsigned) * (size_t)(njobs > 0 ? njobs : 1);
+    cudaError_t e = cudaMallocAsync((void **)&b.d_counter, b.counters_bytes, s);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&b.d_jobs, sizeof(JobDev) * (njobs > 0 ? njobs : 1), s);
+    if (e == cudaSuccess && b.nparts) e = cudaMallocAsync((void **)&b.d_parts, sizeof(Part) * b.nparts, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_jobs, staging, sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, s);
+    grns_status st = cuda_status(e);
+    if (st == GRNS_OK) {
+        b.d_done = (unsigned *)(b.d_counter + 1);
+        int per_sm = 1;
+#define C_(n) per_sm = occupancy_blocks<n>(); break
+        switch (c->n) {
+            case 4: C_(4);
+            case 8: C_(8);
+            case 12: C_(12);
+            case 16: C_(16);
+            case 32: C_(32);
+            case 64: C_(64);
+            default: break;
+        }
+#undef C_
+        b.grid = c->sm_count * per_sm;
+        st = enqueue(&b, s);
+    }
+    if (b.d_jobs) cudaFreeAsync(b.d_jobs, s);
+    if (b.d_counter) cudaFreeAsync(b.d_counter, s);
+    if (b.d_parts) cudaFreeAsync(b.d_parts, s);
+    b.d_jobs = nullptr;
+    b.d_counter = nullptr;
+    b.d_parts = nullptr;
+    return st;
+}
+
+}  // namespace grns
 
 extern "C" {
 

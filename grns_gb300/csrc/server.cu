@@ -1,0 +1,528 @@
+/*
+ * grns_gb300 -- serving: a stream of vector-op requests with continuous
+ * batching over device-resident operands.
+ *
+ * No counterpart in the reference (a header-only library with no runtime).
+ * Clients put arrays into server-owned device memory once (handles) and
+ * submit requests that name them; outputs become new resident handles, and an
+ * eval request's output is remembered as that array's evaluation so later
+ * comparisons read 32-byte intervals instead of the residues.  A scheduler
+ * thread:
+ *   - admits pending requests in arrival order while their HBM footprint
+ *     (output arrays) fits the budget, allocating outputs from the server's
+ *     memory pool (stream-ordered, no device-wide synchronisation);
+ *   - packs the admitted requests of one moduli set into ONE launch of the
+ *     persistent batched kernel on a free launch slot (stream); with several
+ *     slots, requests arriving while launches are in flight are admitted and
+ *     launched alongside them, so their work overlaps on the device;
+ *   - marks requests done from a host callback at the end of each launch and
+ *     records submit-to-completion latency (p50/p99 in grns_server_stats).
+ * Every per-element computation is independent of its neighbours, so a
+ * result does not depend on what else shares its launch.
+ */
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double now_us() {
+    return std::chrono::duration<double, std::micro>(Clock::now().time_since_epoch()).count();
+}
+
+struct Array {
+    void *p = nullptr;
+    int ctx = 0;
+    int kind = 0;
+    int64_t count = 0;
+    int layout = GRNS_LAYOUT_SOA;
+    size_t bytes = 0;
+    uint64_t eval = 0;      // handle of this array's evaluation (RNS arrays), 0 if none
+    uint64_t producer = 0;  // request that writes it (0: put by the client)
+};
+
+struct Req {
+    grns_request r{};
+    int state = 0;  // 0 pending, 1 in flight, 2 done
+    int32_t status = GRNS_OK;
+    uint64_t out0 = 0, out1 = 0;
+    size_t footprint = 0;
+    int64_t count = 0;
+    double t_submit = 0, t_done = 0;
+};
+
+struct Slot {
+    cudaStream_t s = nullptr;
+    void *staging = nullptr;  // pinned job-table staging
+    bool busy = false;
+    std::vector<uint64_t> reqs;
+    std::atomic<int> done{0};
+    double t_done = 0;
+    struct grns_server *srv = nullptr;
+};
+
+size_t elem_bytes(int kind, int n) {
+    switch (kind) {
+        case GRNS_ARRAY_RNS: return 4 * (size_t)n;
+        case GRNS_ARRAY_U32: return 4;
+        case GRNS_ARRAY_MPINT: return GRNS_MPINT_BYTES(n);
+        case GRNS_ARRAY_INTERVAL: return sizeof(interval_t);
+        default: return 0;
+    }
+}
+
+}  // namespace
+
+struct grns_server {
+    grns_server_options opt{};
+    std::vector<grns_ctx *> ctxs;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::unordered_map<uint64_t, Array> arrays;
+    std::unordered_map<uint64_t, Req> reqs;
+    std::deque<uint64_t> pending;
+    std::vector<Slot *> slots;
+    uint64_t next_handle = 1, next_req = 1;
+    size_t in_use = 0;
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t copy = nullptr;
+    int device = 0;
+    bool stop = false;
+    std::thread worker;
+    // stats
+    std::vector<double> lat;
+    uint64_t completed = 0, rejected = 0, launches = 0, jobs_launched = 0;
+    double numbers = 0, t_first = 0, t_last = 0;
+};
+
+namespace {
+
+void CUDART_CB on_launch_done(void *arg) {
+    Slot *sl = (Slot *)arg;
+    sl->t_done = now_us();
+    sl->done.store(1);
+    grns_server *sv = sl->srv;
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->cv.notify_all();
+}
+
+grns_status alloc_array(grns_server *sv, cudaStream_t s, int ctx, int kind, int64_t count, int layout, Array &a) {
+    const grns_ctx *c = sv->ctxs[ctx];
+    size_t bytes = elem_bytes(kind, c->n) * (size_t)count;
+    if (kind == GRNS_ARRAY_MAXOUT) bytes = ((4 * (size_t)c->n + 7) / 8) * 8 + 8;
+    cudaError_t e = cudaMallocFromPoolAsync(&a.p, bytes ? bytes : 16, sv->pool, s);
+    if (e != cudaSuccess) return grns::cuda_status(e);
+    a.ctx = ctx;
+    a.kind = kind;
+    a.count = count;
+    a.layout = layout;
+    a.bytes = bytes;
+    return GRNS_OK;
+}
+
+/* output arrays of a request: sizes only (for admission) */
+size_t footprint_of(const grns_server *sv, const Req &q) {
+    const grns_ctx *c = sv->ctxs[q.r.ctx_index];
+    const int n = c->n;
+    const int64_t k = q.count;
+    switch (q.r.op) {
+        case GRNS_OP_EVAL: return sizeof(interval_t) * k;
+        case GRNS_OP_CMP: return 4 * (size_t)k;
+        case GRNS_OP_DIV: return 2 * 4 * (size_t)n * k;
+        case GRNS_OP_SCALE2POW: return 4 * (size_t)n * k;
+        case GRNS_OP_MAX: return ((4 * (size_t)n + 7) / 8) * 8 + 8;
+        default: return GRNS_MPINT_BYTES(n) * (size_t)k;
+    }
+}
+
+/* scheduler: completions, admission, packing, launch (caller holds mu) */
+void schedule_locked(grns_server *sv) {
+    for (Slot *sl : sv->slots) {
+        if (!sl->busy || !sl->done.load()) continue;
+        for (uint64_t id : sl->reqs) {
+            Req &q = sv->reqs[id];
+            q.state = 2;
+            q.t_done = sl->t_done;
+            sv->lat.push_back(q.t_done - q.t_submit);
+            sv->completed++;
+            sv->numbers += (double)q.count;
+            sv->t_last = std::max(sv->t_last, q.t_done);
+        }
+        sl->reqs.clear();
+        sl->busy = false;
+        sl->done.store(0);
+    }
+    const double now = now_us();
+    while (!sv->pending.empty()) {  /* requests that waited too long for memory */
+        Req &q = sv->reqs[sv->pending.front()];
+        if (now - q.t_submit < 1e3 * sv->opt.admission_timeout_ms) break;
+        q.state = 2;
+        q.status = GRNS_ERR_REJECTED;
+        q.t_done = now;
+        sv->rejected++;
+        sv->pending.pop_front();
+    }
+    for (Slot *sl : sv->slots) {
+        if (sl->busy || sv->pending.empty()) continue;
+        const int ctx = sv->reqs[sv->pending.front()].r.ctx_index;
+        std::vector<grns_job> jobs;
+        while (!sv->pending.empty() && (int)jobs.size() < sv->opt.max_jobs_per_launch) {
+            const uint64_t id = sv->pending.front();
+            Req &q = sv->reqs[id];
+            if (q.r.ctx_index != ctx) break;
+            if (sv->in_use + q.footprint > sv->opt.hbm_budget_bytes) break;  // wait for memory (arrival order kept)
+            const grns_ctx *c = sv->ctxs[ctx];
+            const Array &A = sv->arrays[q.r.a];
+            const Array *B = q.r.b ? &sv->arrays[q.r.b] : nullptr;
+            Array o0, o1;
+            grns_status st = GRNS_OK;
+            switch (q.r.op) {
+                case GRNS_OP_EVAL: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_INTERVAL, q.count, 0, o0); break;
+                case GRNS_OP_CMP: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_U32, q.count, 0, o0); break;
+                case GRNS_OP_DIV:
+                    st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, GRNS_LAYOUT_SOA, o0);
+                    if (st == GRNS_OK) st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, GRNS_LAYOUT_SOA, o1);
+                    break;
+                case GRNS_OP_SCALE2POW: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, GRNS_LAYOUT_SOA, o0); break;
+                case GRNS_OP_MAX: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_MAXOUT, 1, 0, o0); break;
+                default: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_MPINT, q.count, 0, o0); break;
+            }
+            sv->pending.pop_front();
+            if (st != GRNS_OK) {
+                if (o0.p) cudaFreeAsync(o0.p, sl->s);
+                q.state = 2;
+                q.status = st;
+                q.t_done = now_us();
+                continue;
+            }
+            sv->in_use += q.footprint;
+            o0.producer = id;
+            q.out0 = sv->next_handle++;
+            sv->arrays[q.out0] = o0;
+            if (o1.p) {
+                o1.producer = id;
+                q.out1 = sv->next_handle++;
+                sv->arrays[q.out1] = o1;
+            }
+            grns_job j{};
+            j.op = q.r.op;
+            j.layout = A.layout;
+            j.count = q.count;
+            j.ld = A.layout == GRNS_LAYOUT_SOA ? A.count : 0;
+            j.a = A.p;
+            j.b = B ? B->p : nullptr;
+            j.out0 = o0.p;
+            j.D_uniform = q.r.D_uniform;
+            if (q.r.op == GRNS_OP_DIV) {
+                j.out1 = o1.p;
+                j.layout = GRNS_LAYOUT_SOA;
+            } else if (q.r.op == GRNS_OP_MAX) {
+                j.out1 = (char *)o0.p + ((4 * (size_t)c->n + 7) / 8) * 8;
+            } else if (q.r.op == GRNS_OP_CMP && A.eval && B && B->eval && sv->arrays[A.eval].count >= q.count &&
+                       sv->arrays[B->eval].count >= q.count) {
+                j.eval_a = (const interval_t *)sv->arrays[A.eval].p;
+                j.eval_b = (const interval_t *)sv->arrays[B->eval].p;
+            }
+            if (q.r.op == GRNS_OP_EVAL && q.count == A.count) sv->arrays[q.r.a].eval = q.out0;
+            q.state = 1;
+            sl->reqs.push_back(id);
+            jobs.push_back(j);
+        }
+        if (jobs.empty()) continue;
+        grns_status st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
+        if (st == GRNS_OK) st = grns::cuda_status(cudaLaunchHostFunc(sl->s, on_launch_done, sl));
+        if (st != GRNS_OK) {
+            for (uint64_t id : sl->reqs) {
+                Req &q = sv->reqs[id];
+                q.state = 2;
+                q.status = st;
+                q.t_done = now_us();
+            }
+            sl->reqs.clear();
+            continue;
+        }
+        sl->busy = true;
+        sv->launches++;
+        sv->jobs_launched += jobs.size();
+    }
+}
+
+void worker_main(grns_server *sv) {
+    cudaSetDevice(sv->device);
+    std::unique_lock<std::mutex> lk(sv->mu);
+    while (!sv->stop) {
+        schedule_locked(sv);
+        sv->cv.wait_for(lk, std::chrono::microseconds(200));
+    }
+}
+
+bool wait_done(grns_server *sv, std::unique_lock<std::mutex> &lk, uint64_t id, int64_t timeout_us) {
+    auto until = Clock::now() + std::chrono::microseconds(timeout_us < 0 ? (int64_t)1 << 40 : timeout_us);
+    while (sv->reqs[id].state != 2) {
+        if (sv->cv.wait_until(lk, until) == std::cv_status::timeout && sv->reqs[id].state != 2) return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+grns_status grns_server_create(const grns_server_options *opt, grns_server **out) {
+    if (!out) return GRNS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    grns_server *sv = new (std::nothrow) grns_server();
+    if (!sv) return GRNS_ERR_OUT_OF_MEMORY;
+    if (opt) sv->opt = *opt;
+    if (sv->opt.launch_slots <= 0) sv->opt.launch_slots = 4;
+    if (sv->opt.max_jobs_per_launch <= 0) sv->opt.max_jobs_per_launch = 256;
+    if (sv->opt.admission_timeout_ms <= 0) sv->opt.admission_timeout_ms = 10000;
+    cudaError_t e = cudaGetDevice(&sv->device);
+    size_t fr = 0, tot = 0;
+    if (e == cudaSuccess) e = cudaMemGetInfo(&fr, &tot);
+    if (e == cudaSuccess && sv->opt.hbm_budget_bytes == 0) sv->opt.hbm_budget_bytes = (size_t)(0.8 * (double)fr);
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = sv->device;
+    if (e == cudaSuccess) e = cudaMemPoolCreate(&sv->pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t keep = ~0ull;  // keep freed memory in the pool
+        e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->copy, cudaStreamNonBlocking);
+    for (int i = 0; e == cudaSuccess && i < sv->opt.launch_slots; i++) {
+        Slot *sl = new Slot();
+        sl->srv = sv;
+        e = cudaStreamCreateWithFlags(&sl->s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMallocHost(&sl->staging, grns::batch_staging_bytes(sv->opt.max_jobs_per_launch));
+        sv->slots.push_back(sl);
+    }
+    if (e != cudaSuccess) {
+        grns_server_destroy(sv);
+        return grns::cuda_status(e);
+    }
+    sv->worker = std::thread(worker_main, sv);
+    *out = sv;
+    return GRNS_OK;
+}
+
+grns_status grns_server_destroy(grns_server *sv) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->stop = true;
+        sv->cv.notify_all();
+    }
+    if (sv->worker.joinable()) sv->worker.join();
+    for (Slot *sl : sv->slots) {
+        if (sl->s) cudaStreamSynchronize(sl->s);
+    }
+    for (auto &kv : sv->arrays)
+        if (kv.second.p) cudaFreeAsync(kv.second.p, sv->copy ? sv->copy : nullptr);
+    if (sv->copy) cudaStreamSynchronize(sv->copy);
+    for (Slot *sl : sv->slots) {
+        if (sl->staging) cudaFreeHost(sl->staging);
+        if (sl->s) cudaStreamDestroy(sl->s);
+        delete sl;
+    }
+    if (sv->copy) cudaStreamDestroy(sv->copy);
+    if (sv->pool) cudaMemPoolDestroy(sv->pool);
+    delete sv;
+    return GRNS_OK;
+}
+
+grns_status grns_server_add_context(grns_server *sv, grns_ctx *c, int *index) {
+    if (!sv || !c || !index) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->ctxs.push_back(c);
+    *index = (int)sv->ctxs.size() - 1;
+    return GRNS_OK;
+}
+
+grns_status grns_server_put(grns_server *sv, int ctx, int kind, const void *src, int src_on_device, int64_t count,
+                            int layout, uint64_t *handle) {
+    if (!sv || !handle || count < 0 || (count > 0 && !src)) return GRNS_ERR_INVALID_ARGUMENT;
+    if (kind != GRNS_ARRAY_RNS && kind != GRNS_ARRAY_U32 && kind != GRNS_ARRAY_MPINT) return GRNS_ERR_INVALID_ARGUMENT;
+    if (layout != GRNS_LAYOUT_SOA && layout != GRNS_LAYOUT_AOS) return GRNS_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (ctx < 0 || ctx >= (int)sv->ctxs.size()) return GRNS_ERR_INVALID_ARGUMENT;
+    const size_t bytes = elem_bytes(kind, sv->ctxs[ctx]->n) * (size_t)count;
+    if (sv->in_use + bytes > sv->opt.hbm_budget_bytes) return GRNS_ERR_REJECTED;
+    Array a;
+    grns_status st = alloc_array(sv, sv->copy, ctx, kind, count, layout, a);
+    if (st != GRNS_OK) return st;
+    sv->in_use += bytes;
+    lk.unlock();
+    cudaError_t e = cudaSuccess;
+    if (bytes)
+        e = cudaMemcpyAsync(a.p, src, bytes, src_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, sv->copy);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sv->copy);
+    lk.lock();
+    if (e != cudaSuccess) {
+        cudaFreeAsync(a.p, sv->copy);
+        sv->in_use -= bytes;
+        return grns::cuda_status(e);
+    }
+    *handle = sv->next_handle++;
+    sv->arrays[*handle] = a;
+    return GRNS_OK;
+}
+
+grns_status grns_server_array_info(grns_server *sv, uint64_t h, int64_t *count, size_t *bytes, void **device_ptr) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    auto it = sv->arrays.find(h);
+    if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
+    if (count) *count = it->second.count;
+    if (bytes) *bytes = it->second.bytes;
+    if (device_ptr) *device_ptr = it->second.p;
+    return GRNS_OK;
+}
+
+grns_status grns_server_get(grns_server *sv, uint64_t h, void *host_dst, size_t bytes) {
+    if (!sv || !host_dst) return GRNS_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->arrays.find(h);
+    if (it == sv->arrays.end() || bytes > it->second.bytes) return GRNS_ERR_INVALID_ARGUMENT;
+    const uint64_t prod = it->second.producer;
+    if (prod && !wait_done(sv, lk, prod, -1)) return GRNS_ERR_TIMEOUT;
+    void *p = sv->arrays[h].p;
+    lk.unlock();
+    cudaError_t e = cudaMemcpyAsync(host_dst, p, bytes, cudaMemcpyDeviceToHost, sv->copy);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sv->copy);
+    return grns::cuda_status(e);
+}
+
+grns_status grns_server_free(grns_server *sv, uint64_t h) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->arrays.find(h);
+    if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
+    const uint64_t prod = it->second.producer;
+    if (prod && !wait_done(sv, lk, prod, -1)) return GRNS_ERR_TIMEOUT;
+    it = sv->arrays.find(h);
+    if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
+    cudaFreeAsync(it->second.p, sv->copy);
+    sv->in_use -= std::min(sv->in_use, it->second.bytes);
+    for (auto &kv : sv->arrays)
+        if (kv.second.eval == h) kv.second.eval = 0;
+    sv->arrays.erase(it);
+    sv->cv.notify_all();
+    return GRNS_OK;
+}
+
+grns_status grns_server_submit(grns_server *sv, const grns_request *r, uint64_t *request_id) {
+    if (!sv || !r || !request_id) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    if (r->ctx_index < 0 || r->ctx_index >= (int)sv->ctxs.size()) return GRNS_ERR_INVALID_ARGUMENT;
+    if (r->op < GRNS_OP_EVAL || r->op > GRNS_OP_MPINT_MUL) return GRNS_ERR_INVALID_ARGUMENT;
+    auto ia = sv->arrays.find(r->a);
+    if (ia == sv->arrays.end() || ia->second.ctx != r->ctx_index) return GRNS_ERR_INVALID_ARGUMENT;
+    const bool mp = r->op >= GRNS_OP_MPINT_ADD;
+    if ((mp ? GRNS_ARRAY_MPINT : GRNS_ARRAY_RNS) != ia->second.kind) return GRNS_ERR_INVALID_ARGUMENT;
+    const int64_t count = r->count > 0 ? r->count : ia->second.count;
+    if (count > ia->second.count) return GRNS_ERR_INVALID_ARGUMENT;
+    const bool needs_b = r->op == GRNS_OP_CMP || r->op == GRNS_OP_DIV || mp;
+    if (needs_b || r->b) {
+        auto ib = sv->arrays.find(r->b);
+        if (ib == sv->arrays.end() || ib->second.count < count) return GRNS_ERR_INVALID_ARGUMENT;
+        const int want = r->op == GRNS_OP_SCALE2POW ? GRNS_ARRAY_U32 : (mp ? GRNS_ARRAY_MPINT : GRNS_ARRAY_RNS);
+        if (ib->second.kind != want) return GRNS_ERR_INVALID_ARGUMENT;
+        if (want == GRNS_ARRAY_RNS && (ib->second.layout != ia->second.layout || ib->second.count != ia->second.count))
+            return GRNS_ERR_INVALID_ARGUMENT;  // one leading dimension per job
+    }
+    if (r->op == GRNS_OP_DIV && ia->second.layout != GRNS_LAYOUT_SOA) return GRNS_ERR_INVALID_ARGUMENT;
+    const uint64_t id = sv->next_req++;
+    Req &q = sv->reqs[id];
+    q.r = *r;
+    q.count = count;
+    q.footprint = footprint_of(sv, q);
+    q.t_submit = now_us();
+    if (sv->t_first == 0) sv->t_first = q.t_submit;
+    *request_id = id;
+    if (q.footprint > sv->opt.hbm_budget_bytes) {  // can never be admitted
+        q.state = 2;
+        q.status = GRNS_ERR_REJECTED;
+        q.t_done = q.t_submit;
+        sv->rejected++;
+        return GRNS_OK;
+    }
+    sv->pending.push_back(id);
+    sv->cv.notify_all();
+    return GRNS_OK;
+}
+
+grns_status grns_server_poll(grns_server *sv, uint64_t id, int *done, int32_t *status, uint64_t *out0, uint64_t *out1) {
+    if (!sv || !done) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return GRNS_ERR_INVALID_ARGUMENT;
+    *done = it->second.state == 2;
+    if (status) *status = it->second.status;
+    if (out0) *out0 = it->second.out0;
+    if (out1) *out1 = it->second.out1;
+    return GRNS_OK;
+}
+
+grns_status grns_server_wait(grns_server *sv, uint64_t id, int64_t timeout_us, int32_t *status, uint64_t *out0,
+                             uint64_t *out1) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    if (sv->reqs.find(id) == sv->reqs.end()) return GRNS_ERR_INVALID_ARGUMENT;
+    if (!wait_done(sv, lk, id, timeout_us)) return GRNS_ERR_TIMEOUT;
+    const Req &q = sv->reqs[id];
+    if (status) *status = q.status;
+    if (out0) *out0 = q.out0;
+    if (out1) *out1 = q.out1;
+    return GRNS_OK;
+}
+
+grns_status grns_server_stats_get(grns_server *sv, grns_server_stats *st) {
+    if (!sv || !st) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    *st = grns_server_stats{};
+    st->completed = sv->completed;
+    st->rejected = sv->rejected;
+    st->pending = sv->pending.size();
+    for (const Slot *sl : sv->slots) st->inflight += sl->reqs.size();
+    st->launches = sv->launches;
+    st->mean_jobs_per_launch = sv->launches ? (double)sv->jobs_launched / (double)sv->launches : 0.0;
+    st->bytes_in_use = sv->in_use;
+    st->budget = sv->opt.hbm_budget_bytes;
+    if (!sv->lat.empty()) {
+        std::vector<double> v(sv->lat);
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double p) { return v[std::min(v.size() - 1, (size_t)(p * (double)(v.size() - 1) + 0.5))]; };
+        st->p50_us = pct(0.50);
+        st->p99_us = pct(0.99);
+        double s = 0;
+        for (double x : v) s += x;
+        st->mean_us = s / (double)v.size();
+    }
+    if (sv->t_last > sv->t_first) st->numbers_per_s = sv->numbers / ((sv->t_last - sv->t_first) * 1e-6);
+    return GRNS_OK;
+}
+
+grns_status grns_server_reset_stats(grns_server *sv) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->lat.clear();
+    sv->completed = sv->rejected = sv->launches = sv->jobs_launched = 0;
+    sv->numbers = 0;
+    sv->t_first = sv->t_last = 0;
+    return GRNS_OK;
+}
+
+}  // extern "C"

@@ -44,6 +44,21 @@ SIGNATURES = {
     "grns_ctx_set_schedule": (c_int, [c_void_p, c_int, c_void_p]),
     "grns_autotune": (c_int, [c_void_p, c_int, c_int64, ctypes.c_char_p, c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "grns_autotune_load": (c_int, [c_void_p, ctypes.c_char_p, ctypes.POINTER(c_int)]),
+    "grns_server_create": (c_int, [c_void_p, ctypes.POINTER(c_void_p)]),
+    "grns_server_destroy": (c_int, [c_void_p]),
+    "grns_server_add_context": (c_int, [c_void_p, c_void_p, ctypes.POINTER(c_int)]),
+    "grns_server_put": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, c_int64, c_int, ctypes.POINTER(ctypes.c_uint64)]),
+    "grns_server_get": (c_int, [c_void_p, ctypes.c_uint64, c_void_p, c_size_t]),
+    "grns_server_array_info": (c_int, [c_void_p, ctypes.c_uint64, ctypes.POINTER(c_int64), ctypes.POINTER(c_size_t),
+                                       ctypes.POINTER(c_void_p)]),
+    "grns_server_free": (c_int, [c_void_p, ctypes.c_uint64]),
+    "grns_server_submit": (c_int, [c_void_p, c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "grns_server_poll": (c_int, [c_void_p, ctypes.c_uint64, ctypes.POINTER(c_int), ctypes.POINTER(ctypes.c_int32),
+                                 ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+    "grns_server_wait": (c_int, [c_void_p, ctypes.c_uint64, c_int64, ctypes.POINTER(ctypes.c_int32),
+                                 ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
+    "grns_server_stats_get": (c_int, [c_void_p, c_void_p]),
+    "grns_server_reset_stats": (c_int, [c_void_p]),
     "grns_gen_uniform": (c_int, [c_void_p, ctypes.c_uint64, c_uint32, c_int64, c_int, c_void_p, c_void_p]),
     "grns_gen_divisors": (c_int, [c_void_p, ctypes.c_uint64, c_int64, c_int, c_void_p, c_void_p]),
     "grns_gen_shifts": (c_int, [ctypes.c_uint64, c_int64, c_uint32, c_void_p, c_void_p]),
@@ -53,13 +68,35 @@ SIGNATURES = {
 class Job(ctypes.Structure):
     """grns_job (include/grns/grns.h)"""
     _fields_ = [("op", ctypes.c_int32), ("layout", ctypes.c_int32), ("count", ctypes.c_int64),
-                ("a", c_void_p), ("b", c_void_p), ("out0", c_void_p), ("out1", c_void_p),
-                ("flags", c_void_p), ("D_uniform", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("ld", ctypes.c_int64), ("a", c_void_p), ("b", c_void_p), ("out0", c_void_p),
+                ("out1", c_void_p), ("flags", c_void_p), ("eval_a", c_void_p), ("eval_b", c_void_p),
+                ("D_uniform", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class Schedule(ctypes.Structure):
     _fields_ = [("coop", ctypes.c_int32), ("chunk", ctypes.c_int32)]
 
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_size_t), ("launch_slots", ctypes.c_int32),
+                ("max_jobs_per_launch", ctypes.c_int32), ("admission_timeout_ms", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int32), ("ctx_index", ctypes.c_int32), ("count", ctypes.c_int64),
+                ("a", ctypes.c_uint64), ("b", ctypes.c_uint64), ("D_uniform", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("rejected", ctypes.c_uint64), ("pending", ctypes.c_uint64),
+                ("inflight", ctypes.c_uint64), ("launches", ctypes.c_uint64), ("p50_us", ctypes.c_double),
+                ("p99_us", ctypes.c_double), ("mean_us", ctypes.c_double), ("numbers_per_s", ctypes.c_double),
+                ("mean_jobs_per_launch", ctypes.c_double), ("bytes_in_use", c_size_t), ("budget", c_size_t)]
+
+
+ARRAY_RNS, ARRAY_U32, ARRAY_MPINT, ARRAY_INTERVAL, ARRAY_MAXOUT = range(5)
 
 OP_EVAL, OP_CMP, OP_DIV, OP_SCALE2POW, OP_MAX, OP_MPINT_ADD, OP_MPINT_SUB, OP_MPINT_MUL = range(8)
 

@@ -192,9 +192,14 @@ typedef struct {
     int32_t op;       /* grns_op */
     int32_t layout;   /* GRNS_LAYOUT_SOA / GRNS_LAYOUT_AOS for RNS arrays */
     int64_t count;
+    int64_t ld;       /* SoA inputs: residue i of number k at a[i*ld + k]; 0 means count
+                         (so a job can use the first `count` numbers of a longer array).
+                         Outputs are always dense with leading dimension count. */
     const void *a, *b;
     void *out0, *out1;
     uint8_t *flags;   /* optional per-element flags */
+    const interval_t *eval_a, *eval_b;  /* cmp: optional evaluations of a and b
+                         (as grns_eval produced them); the intervals decide first */
     uint32_t D_uniform;
     uint32_t reserved;
 } grns_job;
@@ -225,6 +230,71 @@ grns_status grns_ctx_set_schedule(grns_ctx *ctx, int op, const grns_schedule *sc
 grns_status grns_autotune(grns_ctx *ctx, int op, int64_t count, const char *cache_path, grns_schedule *chosen,
                           double *best_ms);
 grns_status grns_autotune_load(grns_ctx *ctx, const char *cache_path, int *applied);
+
+/* ---- serving: a request stream with continuous batching ----
+ * No counterpart in the reference.  Arrays live in server-owned device memory
+ * (handles); requests name operand handles and get output handles.  A
+ * scheduler thread admits requests in arrival order while their output
+ * footprint fits the HBM budget, packs the admitted requests of one moduli
+ * set into one launch of the batched kernel on a free launch slot, and keeps
+ * admitting and launching while earlier launches run.  An eval request's
+ * output is remembered as its operand's evaluation; comparisons of two
+ * evaluated arrays decide from the intervals first.  Latency = submit to
+ * completion (host callback), summarised as p50 / p99. */
+typedef struct grns_server grns_server;
+
+enum {  /* array kinds */
+    GRNS_ARRAY_RNS = 0,      /* int32 residues, n per number, SoA or AoS */
+    GRNS_ARRAY_U32 = 1,      /* one 32-bit value per number (exponents, comparison results) */
+    GRNS_ARRAY_MPINT = 2,    /* mp_int_t */
+    GRNS_ARRAY_INTERVAL = 3, /* interval_t (outputs of eval) */
+    GRNS_ARRAY_MAXOUT = 4    /* max output: int32[n] value, then int64 index at offset 8*ceil(n/2) */
+};
+
+typedef struct {
+    size_t hbm_budget_bytes;     /* 0: 80 % of the free device memory at creation */
+    int32_t launch_slots;        /* concurrent launches (streams); 0: 4 */
+    int32_t max_jobs_per_launch; /* 0: 256 */
+    int32_t admission_timeout_ms;/* a request not admitted within this time completes with
+                                    GRNS_ERR_REJECTED (0: 10000) */
+    int32_t reserved;
+} grns_server_options;
+
+typedef struct {
+    int32_t op;         /* grns_op */
+    int32_t ctx_index;  /* from grns_server_add_context */
+    int64_t count;      /* numbers to process from the start of a (0: all) */
+    uint64_t a, b;      /* operand handles (b = 0 when unused; scale2pow: U32 exponents or 0) */
+    uint32_t D_uniform;
+    uint32_t reserved;
+} grns_request;
+
+typedef struct {
+    uint64_t completed, rejected, pending, inflight, launches;
+    double p50_us, p99_us, mean_us;
+    double numbers_per_s;         /* numbers completed / (last completion - first submit) */
+    double mean_jobs_per_launch;  /* requests packed per launch */
+    size_t bytes_in_use, budget;
+} grns_server_stats;
+
+grns_status grns_server_create(const grns_server_options *opt, grns_server **out);
+grns_status grns_server_destroy(grns_server *srv);
+grns_status grns_server_add_context(grns_server *srv, grns_ctx *ctx, int *index);
+/* copy an array in (host or device source); GRNS_ERR_REJECTED when over budget */
+grns_status grns_server_put(grns_server *srv, int ctx_index, int kind, const void *src, int src_on_device,
+                            int64_t count, int layout, uint64_t *handle);
+/* copy an array out; waits for the request that produces it */
+grns_status grns_server_get(grns_server *srv, uint64_t handle, void *host_dst, size_t bytes);
+grns_status grns_server_array_info(grns_server *srv, uint64_t handle, int64_t *count, size_t *bytes, void **device_ptr);
+grns_status grns_server_free(grns_server *srv, uint64_t handle);
+/* non-blocking; a request whose footprint can never fit completes at once with GRNS_ERR_REJECTED */
+grns_status grns_server_submit(grns_server *srv, const grns_request *req, uint64_t *request_id);
+grns_status grns_server_poll(grns_server *srv, uint64_t request_id, int *done, int32_t *status, uint64_t *out0,
+                             uint64_t *out1);
+grns_status grns_server_wait(grns_server *srv, uint64_t request_id, int64_t timeout_us, int32_t *status,
+                             uint64_t *out0, uint64_t *out1);
+grns_status grns_server_stats_get(grns_server *srv, grns_server_stats *stats);
+grns_status grns_server_reset_stats(grns_server *srv);
 
 /* ---- seeded synthetic inputs in device memory ----
  * No counterpart in the reference (its tests draw from GMP's Mersenne

@@ -1,0 +1,166 @@
+"""GPU: serving -- device-resident arrays, continuous batching of a request
+stream over two resident moduli sets (n = 32 and n = 64), admission by HBM
+footprint, cached evaluations, latency stats.  Every request's result must be
+the same alone (through the per-call entry points, and alone through the
+server) and inside the mix."""
+import ctypes
+import random
+
+import numpy as np
+import pytest
+
+from oracle.oracle import greedy_moduli
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def env():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import grns_gb300 as G
+    from grns_gb300 import native
+    native.lib(build_if_missing=True)
+    ctxs = {n: G.RNSContext(greedy_moduli(n)) for n in (32, 64)}
+    return G, native, ctxs
+
+
+def P(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def gen(native, ctx, count, stream_id, seed, divisors=False):
+    x = torch.empty((ctx.n, count), dtype=torch.int32, device="cuda")
+    fn = native.lib().grns_gen_divisors if divisors else None
+    if divisors:
+        native.check(fn(ctx.handle, seed, count, 0, P(x), None))
+    else:
+        native.check(native.lib().grns_gen_uniform(ctx.handle, seed, stream_id, count, 0, P(x), None))
+    torch.cuda.synchronize()
+    return x
+
+
+def per_call(native, ctx, op, x, y, count):
+    """the op through the per-call entry points on the first `count` numbers"""
+    L = native.lib()
+    xs = x[:, :count].contiguous()
+    ys = y[:, :count].contiguous() if y is not None and y.dim() == 2 else y
+    if op == "eval":
+        o = torch.empty(count * 32, dtype=torch.uint8, device="cuda")
+        native.check(L.grns_eval(ctx.handle, P(xs), count, 0, P(o), None, None))
+        return [o]
+    if op == "cmp":
+        o = torch.empty(count, dtype=torch.int32, device="cuda")
+        native.check(L.grns_cmp(ctx.handle, P(xs), P(ys), count, 0, P(o), None, None))
+        return [o]
+    if op == "div":
+        q, r = torch.empty_like(xs), torch.empty_like(xs)
+        native.check(L.grns_div(ctx.handle, P(xs), P(ys), count, 0, P(q), P(r), None, None))
+        return [q, r]
+    if op == "scale2pow":
+        o = torch.empty_like(xs)
+        D = y[:count].contiguous()
+        native.check(L.grns_scale2pow(ctx.handle, P(xs), P(D), 0, count, 0, P(o), None, None))
+        return [o]
+    if op == "max":
+        v = torch.zeros(ctx.n, dtype=torch.int32, device="cuda")
+        i = torch.zeros(1, dtype=torch.int64, device="cuda")
+        native.check(L.grns_max(ctx.handle, P(xs), count, 0, P(v), P(i), None, 0, None))
+        return [v, i]
+    raise ValueError(op)
+
+
+def as_bytes(ts):
+    torch.cuda.synchronize()
+    return b"".join(t.cpu().numpy().tobytes() for t in ts)
+
+
+def server_bytes(srv, rid, op, n):
+    st, o0, o1 = srv.wait(rid)
+    assert st == 0
+    if op == "max":
+        raw = srv.get(o0)
+        off = ((4 * n + 7) // 8) * 8
+        return raw[:4 * n].tobytes() + raw[off:off + 8].tobytes()
+    out = srv.get(o0).tobytes()
+    if o1:
+        out += srv.get(o1).tobytes()
+    return out
+
+
+def test_results_alone_and_in_the_mix(env):
+    G, native, ctxs = env
+    from grns_gb300.serve import Server
+    srv = Server(slots=4, max_jobs=64)
+    try:
+        arrays = {}
+        for n, ctx in ctxs.items():
+            ci = srv.add_context(ctx)
+            cnt = 60000 if n == 32 else 30000
+            x = gen(native, ctx, cnt, 1, 100 + n)
+            y = gen(native, ctx, cnt, 2, 100 + n)
+            d = gen(native, ctx, cnt, 0, 200 + n, divisors=True)
+            D = torch.randint(1, 900, (cnt,), dtype=torch.int32, device="cuda")
+            arrays[n] = dict(ci=ci, ctx=ctx, x=x, y=y, d=d, D=D, cnt=cnt,
+                             hx=srv.put(ci, x), hy=srv.put(ci, y), hd=srv.put(ci, d),
+                             hD=srv.put(ci, D, kind=native.ARRAY_U32))
+        rng = random.Random(3)
+        reqs = []
+        for t in range(60):
+            n = rng.choice([32, 64])
+            A = arrays[n]
+            op = rng.choice(["eval", "cmp", "div", "scale2pow", "max"])
+            count = rng.choice([1, 7, 100, 1000, 10000, A["cnt"]]) if op not in ("div",) else rng.choice([1, 50, 2000])
+            a, b = A["hx"], {"cmp": A["hy"], "div": A["hd"], "scale2pow": A["hD"]}.get(op, 0)
+            reqs.append((n, op, count, a, b))
+        # the mix: everything submitted back to back (they overlap on the device)
+        ids = [srv.submit(op, arrays[n]["ci"], a, b, count) for (n, op, count, a, b) in reqs]
+        mixed = [server_bytes(srv, rid, op, n) for rid, (n, op, count, a, b) in zip(ids, reqs)]
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["rejected"] == 0
+        assert 0 < st["p50_us"] <= st["p99_us"]
+        assert st["launches"] < len(reqs)  # requests were packed into shared launches
+        # each alone: through the server with nothing else queued, and through the per-call API
+        for (n, op, count, a, b), got in zip(reqs, mixed):
+            A = arrays[n]
+            alone = server_bytes(srv, srv.submit(op, A["ci"], a, b, count), op, n)
+            assert alone == got, (n, op, count)
+            y = {"cmp": A["y"], "div": A["d"], "scale2pow": A["D"]}.get(op)
+            assert as_bytes(per_call(native, A["ctx"], op, A["x"], y, count)) == got, (n, op, count)
+    finally:
+        srv.close()
+
+
+def test_cached_evaluations_and_admission(env):
+    G, native, ctxs = env
+    from grns_gb300.serve import Server
+    ctx = ctxs[32]
+    cnt = 50000
+    x = gen(native, ctx, cnt, 1, 7)
+    y = gen(native, ctx, cnt, 2, 7)
+    y[:, ::5] = x[:, ::5]
+    srv = Server(slots=2)
+    try:
+        ci = srv.add_context(ctx)
+        hx, hy = srv.put(ci, x), srv.put(ci, y)
+        plain = server_bytes(srv, srv.submit("cmp", ci, hx, hy), "cmp", 32)
+        for h in (hx, hy):
+            st, ev, _ = srv.wait(srv.submit("eval", ci, h))
+            assert st == 0
+        cached = server_bytes(srv, srv.submit("cmp", ci, hx, hy), "cmp", 32)
+        assert cached == plain
+    finally:
+        srv.close()
+    # a budget that fits the operands but not a division's outputs next to them: the division
+    # is refused after the admission timeout (never hangs), and the queue moves on
+    small = Server(budget_bytes=2 * 4 * 32 * cnt + 4 * cnt + (1 << 20), slots=1, admission_timeout_ms=300)
+    try:
+        ci = small.add_context(ctx)
+        hx, hy = small.put(ci, x), small.put(ci, y)
+        st, _, _ = small.wait(small.submit("div", ci, hx, hy), timeout_us=30_000_000)
+        assert st == 6  # GRNS_ERR_REJECTED
+        st, o0, _ = small.wait(small.submit("cmp", ci, hx, hy), timeout_us=30_000_000)
+        assert st == 0
+    finally:
+        small.close()
