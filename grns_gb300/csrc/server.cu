@@ -183,8 +183,13 @@ void schedule_locked(grns_server *sv) {
             if (q.r.ctx_index != ctx) break;
             if (sv->in_use + q.footprint > sv->opt.hbm_budget_bytes) break;  // wait for memory (arrival order kept)
             const grns_ctx *c = sv->ctxs[ctx];
-            const Array &A = sv->arrays[q.r.a];
-            const Array *B = q.r.b ? &sv->arrays[q.r.b] : nullptr;
+            const Array A = sv->arrays[q.r.a];  /* copies: inserting outputs below may rehash the map */
+            Array Bv;
+            const Array *B = nullptr;
+            if (q.r.b) {
+                Bv = sv->arrays[q.r.b];
+                B = &Bv;
+            }
             Array o0, o1;
             grns_status st = GRNS_OK;
             switch (q.r.op) {
@@ -194,7 +199,7 @@ void schedule_locked(grns_server *sv) {
                     st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, GRNS_LAYOUT_SOA, o0);
                     if (st == GRNS_OK) st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, GRNS_LAYOUT_SOA, o1);
                     break;
-                case GRNS_OP_SCALE2POW: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, GRNS_LAYOUT_SOA, o0); break;
+                case GRNS_OP_SCALE2POW: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_RNS, q.count, A.layout, o0); break;
                 case GRNS_OP_MAX: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_MAXOUT, 1, 0, o0); break;
                 default: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_MPINT, q.count, 0, o0); break;
             }
