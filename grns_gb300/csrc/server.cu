@@ -108,13 +108,16 @@ struct grns_server {
 
 namespace {
 
+/* Runs on CUDA's callback thread after a launch.  It must not take the
+ * server mutex: the scheduler holds that mutex across stream-ordered CUDA
+ * calls, and a call that waits for stream work (which includes this callback)
+ * would deadlock.  So: atomic flag, timestamp, notify without the lock (the
+ * scheduler and waiters also wake on a short timeout). */
 void CUDART_CB on_launch_done(void *arg) {
     Slot *sl = (Slot *)arg;
     sl->t_done = now_us();
-    sl->done.store(1);
-    grns_server *sv = sl->srv;
-    std::lock_guard<std::mutex> g(sv->mu);
-    sv->cv.notify_all();
+    sl->done.store(1, std::memory_order_release);
+    sl->srv->cv.notify_all();
 }
 
 grns_status alloc_array(grns_server *sv, cudaStream_t s, int ctx, int kind, int64_t count, int layout, Array &a) {
@@ -149,7 +152,7 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
 /* scheduler: completions, admission, packing, launch (caller holds mu) */
 void schedule_locked(grns_server *sv) {
     for (Slot *sl : sv->slots) {
-        if (!sl->busy || !sl->done.load()) continue;
+        if (!sl->busy || !sl->done.load(std::memory_order_acquire)) continue;
         for (uint64_t id : sl->reqs) {
             Req &q = sv->reqs[id];
             q.state = 2;
@@ -182,6 +185,13 @@ void schedule_locked(grns_server *sv) {
             Req &q = sv->reqs[id];
             if (q.r.ctx_index != ctx) break;
             if (sv->in_use + q.footprint > sv->opt.hbm_budget_bytes) break;  // wait for memory (arrival order kept)
+            {  /* operands written by requests still in flight: wait for them (arrival order kept) */
+                auto busy = [&](uint64_t h) {
+                    auto it = sv->arrays.find(h);
+                    return it != sv->arrays.end() && it->second.producer && sv->reqs[it->second.producer].state != 2;
+                };
+                if (busy(q.r.a) || (q.r.b && busy(q.r.b))) break;
+            }
             const grns_ctx *c = sv->ctxs[ctx];
             const Array A = sv->arrays[q.r.a];  /* copies: inserting outputs below may rehash the map */
             Array Bv;
@@ -235,7 +245,9 @@ void schedule_locked(grns_server *sv) {
             } else if (q.r.op == GRNS_OP_MAX) {
                 j.out1 = (char *)o0.p + ((4 * (size_t)c->n + 7) / 8) * 8;
             } else if (q.r.op == GRNS_OP_CMP && A.eval && B && B->eval && sv->arrays[A.eval].count >= q.count &&
-                       sv->arrays[B->eval].count >= q.count) {
+                       sv->arrays[B->eval].count >= q.count &&
+                       sv->reqs[sv->arrays[A.eval].producer].state == 2 &&
+                       sv->reqs[sv->arrays[B->eval].producer].state == 2) {  /* finished evaluations only */
                 j.eval_a = (const interval_t *)sv->arrays[A.eval].p;
                 j.eval_b = (const interval_t *)sv->arrays[B->eval].p;
             }
@@ -272,10 +284,14 @@ void worker_main(grns_server *sv) {
     }
 }
 
+/* waits (bounded) for a request; the short wait slices also cover notifications
+ * that raced ahead of the wait */
 bool wait_done(grns_server *sv, std::unique_lock<std::mutex> &lk, uint64_t id, int64_t timeout_us) {
-    auto until = Clock::now() + std::chrono::microseconds(timeout_us < 0 ? (int64_t)1 << 40 : timeout_us);
+    const int64_t cap = (int64_t)600 * 1000 * 1000;  // 10 minutes
+    auto until = Clock::now() + std::chrono::microseconds(timeout_us < 0 || timeout_us > cap ? cap : timeout_us);
     while (sv->reqs[id].state != 2) {
-        if (sv->cv.wait_until(lk, until) == std::cv_status::timeout && sv->reqs[id].state != 2) return false;
+        if (Clock::now() >= until) return false;
+        sv->cv.wait_for(lk, std::chrono::milliseconds(1));
     }
     return true;
 }

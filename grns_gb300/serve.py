@@ -68,7 +68,7 @@ class Server:
         check(self.L.grns_server_submit(self.h, ctypes.byref(r), ctypes.byref(rid)), "grns_server_submit")
         return rid.value
 
-    def wait(self, rid, timeout_us=-1):
+    def wait(self, rid, timeout_us=120_000_000):
         st, o0, o1 = ctypes.c_int32(), ctypes.c_uint64(), ctypes.c_uint64()
         check(self.L.grns_server_wait(self.h, rid, timeout_us, ctypes.byref(st), ctypes.byref(o0), ctypes.byref(o1)),
               "grns_server_wait")
