@@ -167,7 +167,8 @@ def greedy(n):
 
 
 def run_only(args):
-    """one op on a (small) seeded case, for ncu captures"""
+    """one op on a seeded case, timed per call with CUDA events (also the
+    command line for ncu captures)"""
     import ctypes
     import torch
     import grns_gb300 as G
@@ -198,7 +199,7 @@ def run_only(args):
         ma = torch.zeros(cnt * mb, dtype=torch.uint8, device="cuda")
         mc = torch.zeros_like(ma)
         mo = torch.zeros_like(ma)
-    for _ in range(args.warmup + args.steps):
+    def call():
         if args.only == "div":
             native.check(L.grns_div(ctx.handle, P(x), P(y), cnt, 0, P(a), P(b), None, sp))
         elif args.only == "scale":
@@ -211,8 +212,21 @@ def run_only(args):
             native.check(L.grns_eval(ctx.handle, P(x), cnt, 0, P(out), None, sp))
         elif args.only == "mpint64":
             native.check(L.grns_mpint_mul(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
-    torch.cuda.synchronize()
-    print(f"ok: {args.only} on {cnt} numbers x {args.warmup + args.steps}")
+
+    for _ in range(args.warmup):
+        call()
+    times = []
+    stream = torch.cuda.current_stream()
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times) if times else 0.0
+    print(json.dumps({"only": args.only, "count": cnt, "calls": args.warmup + args.steps, "ms_median": ms,
+                      "Mnum_s": cnt / (ms * 1e-3) / 1e6 if ms else None}))
 
 
 def main():

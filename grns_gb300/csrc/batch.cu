@@ -24,6 +24,7 @@
 #include <string>
 #include <vector>
 
+#include "div_warp.cuh"
 #include "internal.h"
 #include "rns_device.cuh"
 #include "rns_fast.cuh"
@@ -39,6 +40,8 @@ struct JobDev {
     void *out0, *out1;
     uint8_t *flags;
     const Er *eval_a, *eval_b;  // cmp: optional cached evaluations (2 Er per number)
+    uint2 *rec;                 // div: pass-A records (one per number)
+    int32_t *order;             // div: longest-first order (one per number)
     uint32_t D_uniform;
     int32_t coop;
     int64_t chunk_begin;   // first global chunk of this job
@@ -52,7 +55,15 @@ struct Part {  // max: best of one chunk
     int64_t idx;
 };
 
-constexpr int kBatchBlock = 256;
+/* block shape per moduli count: 256 threads x 2 blocks per SM, or 128 x 2 at
+ * n = 64; division jobs keep their residues in shared-memory columns
+ * (div_warp.cuh), allocated only when the batch holds a division */
+template <int N>
+struct BatchCfg {
+    static constexpr int kBlock = N > 32 ? 128 : 256;
+    static constexpr int kMinBlocks = 2;
+    static constexpr size_t kDivSmem = div_smem_bytes<N>(kBlock);
+};
 
 __device__ __forceinline__ int find_job(const JobDev *jobs, int njobs, int64_t c) {
     int lo = 0, hi = njobs - 1;
@@ -120,7 +131,7 @@ __device__ __forceinline__ uint64_t fx64_coop(const Consts<N> &C, const Operand<
 
 template <int N>
 __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, int j, int64_t c, int lane,
-                                          unsigned *done, Part *partials) {
+                                          unsigned *done, Part *partials, uint32_t *smem) {
     const int64_t start = (c - J.chunk_begin) * (int64_t)J.chunk_elems;
     const int64_t end = min(start + (int64_t)J.chunk_elems, J.count);
     const int64_t ld = J.layout == GRNS_LAYOUT_SOA ? (J.count > 0 ? J.count : 1) : 0;   // outputs
@@ -185,44 +196,32 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
             }
             break;
         case GRNS_OP_DIV:
+        {
+            uint32_t *hist = smem + sizeof(DivK) / 4 * N;
+            uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
+            div_range<N>(reinterpret_cast<const DivK *>(smem), C, x, y, J.rec, J.order,
+                         Output<N>{(uint32_t *)J.out0, ld}, Output<N>{(uint32_t *)J.out1, ld}, J.flags, start, end,
+                         cols + threadIdx.x, blockDim.x, hist + (threadIdx.x / 32) * kDivBins);
+        }
+            break;
         case GRNS_OP_SCALE2POW:
             for (int64_t k = start + lane; k < end; k += 32) {
-                uint32_t xa[N], ya[N], r0[N], r1[N], f = 0;
+                uint32_t xa[N], r0[N], f = 0;
 #pragma unroll
                 for (int i = 0; i < N; i++) {
                     xa[i] = x.load(k, i);
                     f |= xa[i] >= C.m[i] ? kFlagInvalidInput : 0u;
                 }
-                if (J.op == GRNS_OP_DIV) {
+                const unsigned D = J.b ? __ldg(J.b + k) : J.D_uniform;
+                if (f) {
 #pragma unroll
-                    for (int i = 0; i < N; i++) {
-                        ya[i] = y.load(k, i);
-                        f |= ya[i] >= C.m[i] ? kFlagInvalidInput : 0u;
-                    }
-                    if (f) {
-#pragma unroll
-                        for (int i = 0; i < N; i++) r0[i] = r1[i] = 0;
-                    } else {
-                        div_fast<N>(C, r0, r1, xa, ya, f);
-                    }
-                    const Output<N> q{(uint32_t *)J.out0, ld}, r{(uint32_t *)J.out1, ld};
-#pragma unroll
-                    for (int i = 0; i < N; i++) {
-                        q.store(k, i, r0[i]);
-                        r.store(k, i, r1[i]);
-                    }
+                    for (int i = 0; i < N; i++) r0[i] = 0;
                 } else {
-                    const unsigned D = J.b ? __ldg(J.b + k) : J.D_uniform;
-                    if (f) {
-#pragma unroll
-                        for (int i = 0; i < N; i++) r0[i] = 0;
-                    } else {
-                        scale_fast<N>(C, r0, xa, D);
-                    }
-                    const Output<N> o{(uint32_t *)J.out0, ld};
-#pragma unroll
-                    for (int i = 0; i < N; i++) o.store(k, i, r0[i]);
+                    scale_fast<N>(C, r0, xa, D);
                 }
+                const Output<N> o{(uint32_t *)J.out0, ld};
+#pragma unroll
+                for (int i = 0; i < N; i++) o.store(k, i, r0[i]);
                 if (J.flags) J.flags[k] = (uint8_t)f;
             }
             break;
@@ -287,10 +286,16 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
 }
 
 template <int N>
-__global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const __grid_constant__ Consts<N> C,
+__global__ void __launch_bounds__(BatchCfg<N>::kBlock, BatchCfg<N>::kMinBlocks) k_batch(const __grid_constant__ Consts<N> C,
                                                           const JobDev *__restrict__ jobs, int njobs,
                                                           int64_t total_chunks, unsigned long long *counter,
-                                                          unsigned *done, Part *partials) {
+                                                          unsigned *done, Part *partials, int has_div) {
+    extern __shared__ uint4 batch_smem4[];
+    uint32_t *batch_smem = reinterpret_cast<uint32_t *>(batch_smem4);
+    if (has_div) {  // the division constants (DivK table) for every block
+        divk_fill<N>(C, reinterpret_cast<DivK *>(batch_smem));
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned long long c = 0;
@@ -299,7 +304,7 @@ __global__ void __launch_bounds__(kBatchBlock, 2) k_batch(const __grid_constant_
         if ((int64_t)c >= total_chunks) break;
         const int j = find_job(jobs, njobs, (int64_t)c);
         const JobDev J = jobs[j];
-        run_chunk<N>(C, J, j, (int64_t)c, lane, done, partials);
+        run_chunk<N>(C, J, j, (int64_t)c, lane, done, partials, batch_smem);
     }
 }
 
@@ -312,6 +317,8 @@ struct grns_batch {
     int njobs = 0;
     int64_t total_chunks = 0;
     int64_t nparts = 0;
+    int64_t nrec = 0;                // division records
+    uint2 *d_rec = nullptr;
     std::vector<JobDev> host_jobs;   // execution order
     std::vector<int> order;          // host_jobs[t] = user job order[t]
     JobDev *d_jobs = nullptr;
@@ -320,6 +327,7 @@ struct grns_batch {
     Part *d_parts = nullptr;
     size_t counters_bytes = 0;
     int grid = 0;
+    size_t smem = 0;  // dynamic shared memory of the launch (division jobs present)
     std::vector<int64_t *> empty_max_index;  // count-0 max jobs: index written as -1
     bool use_graph = false;
     cudaGraphExec_t exec = nullptr;
@@ -358,8 +366,8 @@ bool job_ok(const grns_ctx *c, const grns_job &jb) {
 
 template <int N>
 grns_status launch_batch_kernel(grns_batch *b, cudaStream_t s) {
-    k_batch<N><<<b->grid, kBatchBlock, 0, s>>>(consts_of<N>(b->ctx), b->d_jobs, b->njobs, b->total_chunks,
-                                              b->d_counter, b->d_done, b->d_parts);
+    k_batch<N><<<b->grid, BatchCfg<N>::kBlock, b->smem, s>>>(consts_of<N>(b->ctx), b->d_jobs, b->njobs, b->total_chunks,
+                                              b->d_counter, b->d_done, b->d_parts, b->smem ? 1 : 0);
     return cuda_status(cudaGetLastError());
 }
 
@@ -377,16 +385,40 @@ grns_status enqueue(grns_batch *b, cudaStream_t s) {
 }
 
 template <int N>
-int occupancy_blocks() {
+int occupancy_blocks(size_t smem) {
+    if (BatchCfg<N>::kDivSmem > 48 * 1024)  // per device: set on every shape computation
+        cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BatchCfg<N>::kDivSmem);
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, kBatchBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, BatchCfg<N>::kBlock, smem);
     return nb > 0 ? nb : 1;
+}
+
+/* launch shape of a batch: grid (SMs x resident blocks) and shared memory */
+void batch_shape(grns_batch *b) {
+    bool has_div = false;
+    for (const JobDev &J : b->host_jobs) has_div |= J.op == GRNS_OP_DIV && J.count > 0;
+    int per_sm = 1;
+#define C_(n)                                                  \
+    b->smem = has_div ? BatchCfg<n>::kDivSmem : 0;             \
+    per_sm = occupancy_blocks<n>(b->smem);                     \
+    break
+    switch (b->ctx->n) {
+        case 4: C_(4);
+        case 8: C_(8);
+        case 12: C_(12);
+        case 16: C_(16);
+        case 32: C_(32);
+        case 64: C_(64);
+        default: break;
+    }
+#undef C_
+    b->grid = b->ctx->sm_count * per_sm;
 }
 
 /* fill the device-side descriptors from user jobs (fixed order) */
 grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
     const grns_ctx *c = b->ctx;
-    int64_t chunk = 0, parts = 0;
+    int64_t chunk = 0, parts = 0, recs = 0;
     for (int t = 0; t < b->njobs; t++) {
         const grns_job &u = jobs[b->order[t]];
         JobDev &J = b->host_jobs[t];
@@ -402,6 +434,12 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
         J.out1 = u.out1;
         J.flags = u.flags;
         J.D_uniform = u.D_uniform;
+        J.rec = nullptr;
+        J.order = nullptr;
+        if (u.op == GRNS_OP_DIV) {
+            J.rec = b->d_rec ? b->d_rec + recs : nullptr;
+            recs += u.count;
+        }
         const int op = u.op;
         const Sched &sc = c->sched[op];
         J.coop = (op == GRNS_OP_CMP || op == GRNS_OP_MAX) ? sc.coop : 0;
@@ -415,6 +453,15 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
     }
     b->total_chunks = chunk;
     b->nparts = parts;
+    b->nrec = recs;
+    /* the orders follow the records in the same allocation */
+    if (b->d_rec) {
+        int32_t *ord = (int32_t *)(b->d_rec + recs);
+        for (int t = 0; t < b->njobs; t++) {
+            JobDev &J = b->host_jobs[t];
+            if (J.op == GRNS_OP_DIV) J.order = ord + (J.rec - b->d_rec);
+        }
+    }
     b->empty_max_index.clear();
     for (int t = 0; t < b->njobs; t++) {
         const grns_job &u = jobs[b->order[t]];
@@ -445,33 +492,29 @@ grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *
     });
     b.host_jobs.resize(njobs);
     fill_jobs(&b, jobs);
-    std::memcpy(staging, b.host_jobs.data(), sizeof(JobDev) * njobs);
     b.counters_bytes = sizeof(unsigned long long) + sizeof(unsigned) * (size_t)(njobs > 0 ? njobs : 1);
-    cudaError_t e = cudaMallocAsync((void **)&b.d_counter, b.counters_bytes, s);
+    cudaError_t e = cudaSuccess;
+    if (b.nrec) {
+        e = cudaMallocAsync((void **)&b.d_rec, kDivScratchPerNumber * b.nrec, s);
+        if (e != cudaSuccess) return cuda_status(e);
+        fill_jobs(&b, jobs);
+    }
+    std::memcpy(staging, b.host_jobs.data(), sizeof(JobDev) * njobs);
+    e = cudaMallocAsync((void **)&b.d_counter, b.counters_bytes, s);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&b.d_jobs, sizeof(JobDev) * (njobs > 0 ? njobs : 1), s);
     if (e == cudaSuccess && b.nparts) e = cudaMallocAsync((void **)&b.d_parts, sizeof(Part) * b.nparts, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_jobs, staging, sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, s);
     grns_status st = cuda_status(e);
     if (st == GRNS_OK) {
         b.d_done = (unsigned *)(b.d_counter + 1);
-        int per_sm = 1;
-#define C_(n) per_sm = occupancy_blocks<n>(); break
-        switch (c->n) {
-            case 4: C_(4);
-            case 8: C_(8);
-            case 12: C_(12);
-            case 16: C_(16);
-            case 32: C_(32);
-            case 64: C_(64);
-            default: break;
-        }
-#undef C_
-        b.grid = c->sm_count * per_sm;
+        batch_shape(&b);
         st = enqueue(&b, s);
     }
     if (b.d_jobs) cudaFreeAsync(b.d_jobs, s);
     if (b.d_counter) cudaFreeAsync(b.d_counter, s);
     if (b.d_parts) cudaFreeAsync(b.d_parts, s);
+    if (b.d_rec) cudaFreeAsync(b.d_rec, s);
+    b.d_rec = nullptr;
     b.d_jobs = nullptr;
     b.d_counter = nullptr;
     b.d_parts = nullptr;
@@ -518,6 +561,10 @@ grns_status grns_batch_create(grns_ctx *c, const grns_job *jobs, int njobs, int 
     cudaError_t e = cudaMalloc(&b->d_counter, b->counters_bytes);
     if (e == cudaSuccess && njobs) e = cudaMalloc(&b->d_jobs, sizeof(JobDev) * njobs);
     if (e == cudaSuccess && b->nparts) e = cudaMalloc(&b->d_parts, sizeof(Part) * b->nparts);
+    if (e == cudaSuccess && b->nrec) {
+        e = cudaMalloc(&b->d_rec, kDivScratchPerNumber * b->nrec);
+        if (e == cudaSuccess) fill_jobs(b, jobs);
+    }
     if (e == cudaSuccess && njobs)
         e = cudaMemcpy(b->d_jobs, b->host_jobs.data(), sizeof(JobDev) * njobs, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -525,19 +572,7 @@ grns_status grns_batch_create(grns_ctx *c, const grns_job *jobs, int njobs, int 
         return cuda_status(e);
     }
     b->d_done = (unsigned *)(b->d_counter + 1);
-    int per_sm = 1;
-#define C_(n) per_sm = occupancy_blocks<n>(); break
-    switch (c->n) {
-        case 4: C_(4);
-        case 8: C_(8);
-        case 12: C_(12);
-        case 16: C_(16);
-        case 32: C_(32);
-        case 64: C_(64);
-        default: break;
-    }
-#undef C_
-    b->grid = c->sm_count * per_sm;
+    batch_shape(b);
     *out = b;
     return GRNS_OK;
 }
@@ -584,6 +619,7 @@ grns_status grns_batch_destroy(grns_batch *b) {
     if (b->d_jobs) cudaFree(b->d_jobs);
     if (b->d_counter) cudaFree(b->d_counter);
     if (b->d_parts) cudaFree(b->d_parts);
+    if (b->d_rec) cudaFree(b->d_rec);
     delete b;
     return GRNS_OK;
 }

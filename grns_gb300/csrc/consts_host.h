@@ -33,6 +33,8 @@ struct HostTables {
     std::vector<uint32_t> mi_pow2, m_pow2, pow2_inv, pow2_inv_sh;  // 30 x n, 30, 30 x n, 30 x n
     std::vector<uint32_t> c64l, c64h, c96_0, c96_1, c96_2, t32, t32_sh, mrbits;
     std::vector<uint32_t> c96k;  // (log2M+1) x n x 4 words: ceil(2^96 (2^k w_i mod m_i)/m_i) mod 2^96, 0
+    std::vector<uint32_t> b48, b48_sh;           // 2^kDivB mod m_i
+    std::vector<uint32_t> pow2neg, pow2neg_sh;   // (kDivB+1) x n: 2^-j mod m_i
     uint64_t E = 0;  // sum_i (m_i - 1)
 };
 
@@ -195,6 +197,24 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
             row[2] = (uint32_t)(c >> 64);
         }
     }
+    /* division: 2^kDivB mod m_i and 2^-j mod m_i for j = 0..kDivB */
+    T.b48.resize(n);
+    T.b48_sh.resize(n);
+    T.pow2neg.resize((size_t)(kDivB + 1) * n);
+    T.pow2neg_sh.resize(T.pow2neg.size());
+    for (int i = 0; i < n; i++) {
+        uint64_t v = 1;
+        for (int j = 0; j < kDivB; j++) v = (v * 2) % m[i];
+        T.b48[i] = (uint32_t)v;
+        T.b48_sh[i] = shoup((uint32_t)v, m[i]);
+        const uint64_t half = (m[i] + 1) / 2;  // 2^-1 mod m_i (m_i odd)
+        uint64_t u = 1;
+        for (int j = 0; j <= kDivB; j++) {
+            T.pow2neg[(size_t)j * n + i] = (uint32_t)u;
+            T.pow2neg_sh[(size_t)j * n + i] = shoup((uint32_t)u, m[i]);
+            u = (u * half) % m[i];
+        }
+    }
     /* MRC_MULT_INV as [j*n + i] = m_j^-1 mod m_i for j < i */
     T.mrc_inv.assign((size_t)n * n, 0);
     T.mrc_inv_sh.assign((size_t)n * n, 0);
@@ -230,7 +250,7 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
 inline std::vector<uint32_t> table_blob(const HostTables &T) {
     std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows */
     for (const auto *v : {&T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
-                          &T.pow2_inv_sh})
+                          &T.pow2_inv_sh, &T.pow2neg, &T.pow2neg_sh})
         blob.insert(blob.end(), v->begin(), v->end());
     return blob;
 }
@@ -251,6 +271,11 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
         C.c96_0[i] = T.c96_0[i];
         C.c96_1[i] = T.c96_1[i];
         C.c96_2[i] = T.c96_2[i];
+        C.c96w_0[i] = T.c96k[(size_t)i * 4 + 0];  // row k = 0 of the magnification table
+        C.c96w_1[i] = T.c96k[(size_t)i * 4 + 1];
+        C.c96w_2[i] = T.c96k[(size_t)i * 4 + 2];
+        C.b48[i] = T.b48[i];
+        C.b48_sh[i] = T.b48_sh[i];
         C.t32[i] = T.t32[i];
         C.t32_sh[i] = T.t32_sh[i];
         C.mrbits[i] = T.mrbits[i];
@@ -273,7 +298,9 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     C.mi_pow2 = blob + off;     off += T.mi_pow2.size();
     C.m_pow2 = blob + off;      off += T.m_pow2.size();
     C.pow2_inv = blob + off;    off += T.pow2_inv.size();
-    C.pow2_inv_sh = blob + off;
+    C.pow2_inv_sh = blob + off; off += T.pow2_inv_sh.size();
+    C.pow2neg = blob + off;     off += T.pow2neg.size();
+    C.pow2neg_sh = blob + off;
 }
 
 }  // namespace grns

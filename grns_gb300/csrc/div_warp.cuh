@@ -1,0 +1,449 @@
+/*
+ * grns_gb300 -- warp-level division driver (integer fast path).
+ *
+ * A warp divides a contiguous range of numbers in the two passes of the
+ * digit-recurrence division (rns_fast.cuh):
+ *   pass A  every lane normalises one number at a time -- divisor, then
+ *           dividend -- by fixed-point evaluations of values magnified by the
+ *           uniform constant 2^48, and writes an 8-byte record {status, s, e};
+ *   pass B  every lane runs one division's digit steps; a step is one
+ *           certified 48-bit digit from scalars, then R <- 2^48 R - q D,
+ *           Q <- 2^48 Q + q and the fixed-point evaluation of the new R, with
+ *           the same constants for every lane.
+ * In both passes a finished lane stores its result and the lanes take the
+ * next numbers of the range together once kDivRefill of them wait (one
+ * coalesced batch of loads instead of one divergent load per finishing lane).
+ *
+ * Memory layout: each thread owns a column of 3N words of shared memory
+ * (R, D, Q rows, [row][stride], conflict-free), and the block holds one DivK
+ * record of constants per modulus, read with broadcast 16-byte loads.  The
+ * residue loops are therefore rolled: the whole driver is a few kilobytes of
+ * code (fully unrolled register versions overflowed the instruction cache
+ * and stalled on instruction fetch) and uses few registers.
+ *
+ * Results are those of rns_div (reference src/rnsdiv.cuh:128): q = floor(x/d),
+ * r = x - q d; flags DIV_BY_ZERO (q = 0, r = x), INVALID_INPUT (q = r = 0).
+ */
+#pragma once
+
+#include "rns_device.cuh"
+#include "rns_fast.cuh"
+
+namespace grns {
+
+constexpr int kDivRefill = 8;
+
+/* per-modulus constants of the division loops (shared memory, one per modulus) */
+struct DivK {
+    uint4 a;  // m, mu, 2^48 mod m, Shoup companion
+    uint4 c;  // w-folded ceil(2^96 w / m) words 0..2, 2^32 mod m
+    uint4 s;  // b - 1, b + 1, Shoup companion of 2^32 mod m, b
+};
+
+/* block-wide: fill the DivK table (caller synchronises the block) */
+template <int N>
+__device__ __forceinline__ void divk_fill(const Consts<N> &C, DivK *K) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        DivK k;
+        k.a = make_uint4(C.m[i], C.mu[i], C.b48[i], C.b48_sh[i]);
+        k.c = make_uint4(C.c96w_0[i], C.c96w_1[i], C.c96w_2[i], C.t32[i]);
+        k.s = make_uint4(C.b[i] - 1, C.b[i] + 1, C.t32_sh[i], C.b[i]);
+        K[i] = k;
+    }
+}
+
+/* bits [s, s + 32) of a 64-bit value for s <= 32 (one funnel shift) */
+__device__ __forceinline__ uint32_t shr64(uint64_t v, uint32_t s) {
+    return __funnelshift_rc((uint32_t)v, (uint32_t)(v >> 32), s);
+}
+__device__ __forceinline__ uint32_t kmulmod(uint32_t x, uint32_t y, const DivK &k) {  // Barrett x y mod m
+    const uint64_t p = (uint64_t)x * y;
+    const uint32_t t = shr64(p, k.s.x);                          // b - 1 <= 30
+    const uint32_t q = shr64((uint64_t)t * k.a.y, k.s.y);        // b + 1 <= 32
+    uint32_t r = (uint32_t)p - q * k.a.x;
+    r = umin32(r, r - k.a.x);
+    return umin32(r, r - k.a.x);
+}
+__device__ __forceinline__ uint32_t kmag(uint32_t x, const DivK &k) {  // x 2^48 mod m
+    return mulmod_shoup(x, k.a.z, k.a.w, k.a.x);
+}
+__device__ __forceinline__ uint32_t kred32(uint32_t v, const DivK &k) {  // v mod m
+    return k.s.w >= 16 ? kmulmod(v, 1u, k) : v % k.a.x;
+}
+__device__ __forceinline__ uint32_t kred53(uint64_t v, const DivK &k) {  // v mod m, v < 2^53
+    if (k.s.w >= 27) {  // hi * (2^32 mod m) + lo < 2^54 <= 2^(2b): one Barrett step
+        const uint64_t p = (uint64_t)(uint32_t)(v >> 32) * k.c.w + (uint32_t)v;
+        const uint32_t t = shr64(p, k.s.x);
+        const uint32_t q = shr64((uint64_t)t * k.a.y, k.s.y);
+        uint32_t r = (uint32_t)p - q * k.a.x;
+        r = umin32(r, r - k.a.x);
+        return umin32(r, r - k.a.x);
+    }
+    const uint32_t hi = mulmod_shoup(kred32((uint32_t)(v >> 32), k), k.c.w, k.s.z, k.a.x);
+    return addmod(hi, kred32((uint32_t)v, k), k.a.x);
+}
+/* fixed-point accumulation of one residue (fx96w) */
+struct Fx96 {
+    uint64_t S0 = 0, S1 = 0;
+    uint32_t S2 = 0;
+    __device__ __forceinline__ void add(uint32_t x, const DivK &k) {
+        const uint64_t p0 = (uint64_t)x * k.c.x;
+        const uint64_t p1 = (uint64_t)x * k.c.y;
+        S0 += (uint32_t)p0;
+        S1 += (p0 >> 32) + (uint32_t)p1;
+        S2 += (uint32_t)(p1 >> 32) + x * k.c.z;
+    }
+    __device__ __forceinline__ u128 value() const {
+        return ((u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64)) & kMask96;
+    }
+};
+
+constexpr int kDivUnroll = 4;
+
+/* pass A over [begin, end): rec[k] = record of number k.  Column rows: the
+ * working value in rows [0, N), the dividend in rows [2N, 3N). */
+template <int N>
+__device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
+                                              const Operand<N> &d, uint2 *rec, int64_t begin, int64_t end,
+                                              uint32_t *col, int stride) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    enum { Idle, ChainD, ChainX, Done, Dead };
+    uint32_t *__restrict__ W = col;
+    uint32_t *__restrict__ X = col + 2 * N * stride;
+    int ph = Idle, k = 0, guard = 0, s = 0;
+    bool xz = false;
+    int64_t idx = 0, next = begin;
+    uint2 out = make_uint2(0, 0);
+    for (;;) {
+        const unsigned lv = __ballot_sync(FULL, ph == ChainD || ph == ChainX);
+        const unsigned wt = __ballot_sync(FULL, ph == Done || ph == Idle);
+        if (lv == 0 || __popc(wt) >= kDivRefill) {
+            if (ph == Done) {
+                rec[idx] = out;
+                ph = Idle;
+            }
+            const unsigned need = __ballot_sync(FULL, ph == Idle);
+            const int64_t my = next + __popc(need & lt);
+            next += __popc(need);
+            if (ph == Idle) {
+                if (my < end) {
+                    idx = my;
+                    uint32_t bad = 0, dnz = 0, xnz = 0;
+#pragma unroll 4
+                    for (int i = 0; i < N; i++) {
+                        const uint32_t dv = d.load(idx, i), xv = x.load(idx, i), m = K[i].a.x;
+                        W[i * stride] = dv;
+                        X[i * stride] = xv;
+                        bad |= (uint32_t)(dv >= m) | (uint32_t)(xv >= m);
+                        dnz |= dv;
+                        xnz |= xv;
+                    }
+                    xz = xnz == 0;
+                    k = 0;
+                    guard = 0;
+                    ph = ChainD;
+                    if (bad) {
+                        out = dv_pack(kDnBad, 0, 0, false);
+                        ph = Done;
+                    } else if (!dnz) {
+                        out = dv_pack(kDnZero, 0, 0, false);
+                        ph = Done;
+                    }
+                } else {
+                    ph = Dead;
+                }
+            }
+            if (__ballot_sync(FULL, ph != Dead) == 0) break;
+            if (__ballot_sync(FULL, ph == ChainD || ph == ChainX) == 0) continue;
+        }
+        const bool live = ph == ChainD || ph == ChainX;
+        Fx96 fx;
+#pragma unroll 8
+        for (int i = 0; i < N; i++) fx.add(W[i * stride], K[i]);
+        const u128 U = fx.value();
+        bool more = false, tox = false;
+        if (live) {
+            const int k0 = k;
+            const int ns = dn_step<N>(C, U, k, guard);
+            if (ns == kNormMore) {
+                more = true;
+            } else if (ph == ChainD) {
+                if (ns == kNormOk) {
+                    s = dv_shift(k0, bitlen128(U));
+                    if (xz) {
+                        out = dv_pack(kDnOk, s, s % kDivB - kDivB, false);
+                        ph = Done;
+                    } else {
+                        tox = true;
+                        k = 0;
+                        guard = 0;
+                        ph = ChainX;
+                    }
+                } else {
+                    out = dv_pack(ns == kNormNear ? kDnNear : kDnCap, 0, 0, false);
+                    ph = Done;
+                }
+            } else {
+                if (ns == kNormOk) out = dv_pack(kDnOk, s, dv_skip(s, k0, bitlen128(U)), false);
+                else if (ns == kNormNear) out = dv_pack(kDnOk, s, s % kDivB - kDivB, true);
+                else out = dv_pack(kDnCap, 0, 0, false);
+                ph = Done;
+            }
+        }
+        /* magnify by 2^48 (lanes that go on), or start the dividend's chain */
+        if (__any_sync(FULL, more || tox)) {
+#pragma unroll 1
+            for (int i0 = 0; i0 < N; i0 += 4) {  // groups of 4: loads, arithmetic, stores
+                uint32_t w[4], xv[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    w[j] = W[(i0 + j) * stride];
+                    xv[j] = X[(i0 + j) * stride];
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) w[j] = tox ? xv[j] : (more ? kmag(w[j], K[i0 + j]) : w[j]);
+#pragma unroll
+                for (int j = 0; j < 4; j++) W[(i0 + j) * stride] = w[j];
+            }
+        }
+    }
+}
+
+/* pass B over [begin, end) with the records of pass A, numbers taken in the
+ * order of div_order.  Column rows: R in [0, N), the scaled divisor D in
+ * [N, 2N), the quotient Q in [2N, 3N). */
+template <int N>
+__device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
+                                              const Operand<N> &d, const uint2 *rec, const int32_t *order,
+                                              const Output<N> &qo, const Output<N> &ro, uint8_t *flags,
+                                              int64_t begin, int64_t end, uint32_t *col, int stride) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    enum { Idle, Iter, Final, Done, Dead };
+    uint32_t *__restrict__ Rc = col;
+    uint32_t *__restrict__ Dc = col + N * stride;
+    uint32_t *__restrict__ Qc = col + 2 * N * stride;
+
+    DivSt st;
+    st.f = 0;
+    st.left = 0;
+    st.b = kDivB;
+    u128 U = 0;
+    int ph = Idle;
+    int64_t idx = 0, next = begin;
+
+    for (;;) {
+        const unsigned lv = __ballot_sync(FULL, ph == Iter);
+        const unsigned wt = __ballot_sync(FULL, ph == Final || ph == Done || ph == Idle);
+        if (lv == 0 || __popc(wt) >= kDivRefill) {
+            if (ph == Final) {  // q = Q + c, r = x - q d
+                int c = dv_final_fx(st, U, C.E);
+                if (c < 0) {
+                    uint32_t a[N], b[N];
+                    for (int i = 0; i < N; i++) {
+                        a[i] = Rc[i * stride];
+                        b[i] = Dc[i * stride];
+                    }
+                    c = dv_final_exact<N>(C, a, b);
+                }
+#pragma unroll 4
+                for (int i = 0; i < N; i++) {
+                    const DivK k = K[i];
+                    const uint32_t m = k.a.x;
+                    const uint32_t qi = addmod(Qc[i * stride], (uint32_t)c % m, m);
+                    qo.store(idx, i, qi);
+                    ro.store(idx, i, submod(x.load(idx, i), kmulmod(qi, d.load(idx, i), k), m));
+                }
+                if (flags) flags[idx] = (uint8_t)st.f;
+                ph = Idle;
+            } else if (ph == Done) {  // results already in the R and Q rows
+#pragma unroll 4
+                for (int i = 0; i < N; i++) {
+                    qo.store(idx, i, Qc[i * stride]);
+                    ro.store(idx, i, Rc[i * stride]);
+                }
+                if (flags) flags[idx] = (uint8_t)st.f;
+                ph = Idle;
+            }
+            const unsigned need = __ballot_sync(FULL, ph == Idle);
+            const int64_t my = next + __popc(need & lt);
+            next += __popc(need);
+            if (ph == Idle) {
+                if (my < end) {
+                    idx = begin + order[my];
+                    const uint2 r2 = rec[idx];
+                    const uint32_t status = r2.x >> 16;
+                    uint32_t bad = 0, xnz = 0;
+#pragma unroll 4
+                    for (int i = 0; i < N; i++) {
+                        const uint32_t xv = x.load(idx, i);
+                        bad |= (uint32_t)(xv >= K[i].a.x);
+                        xnz |= xv;
+                        Rc[i * stride] = xv;  // the remainder when the quotient is 0
+                        Qc[i * stride] = 0u;
+                    }
+                    st.f = 0;
+                    ph = Done;
+                    if (bad || status == kDnBad) {
+                        st.f = kFlagInvalidInput;
+                        for (int i = 0; i < N; i++) Rc[i * stride] = 0;
+                    } else if (status == kDnZero) {
+                        st.f = kFlagDivByZero;
+                    } else if (status == kDnCap) {
+                        st.f = kFxIterCap;
+                    } else if (!xnz) {
+                        /* q = r = 0 */
+                    } else if (status == kDnNear) {  // d > M (1 - E / 2^96): the quotient is 0 or 1
+                        uint32_t a[N], b[N];
+                        for (int i = 0; i < N; i++) {
+                            a[i] = Rc[i * stride];
+                            b[i] = d.load(idx, i);
+                        }
+                        if (dv_cmp_vec<N>(C, a, b) >= 0) {
+                            for (int i = 0; i < N; i++) {
+                                Qc[i * stride] = 1u;
+                                Rc[i * stride] = submod(a[i], b[i], C.m[i]);
+                            }
+                        }
+                    } else {
+                        const int s = (int)(r2.x & 0xffffu), e = dv_rec_e(r2);
+                        const uint32_t *ps = C.pow2 + (int64_t)s * N, *pss = C.pow2_sh + (int64_t)s * N;
+                        const uint32_t *pe = e < 0 ? C.pow2neg + (int64_t)(-e) * N : C.pow2 + (int64_t)e * N;
+                        const uint32_t *pes =
+                            e < 0 ? C.pow2neg_sh + (int64_t)(-e) * N : C.pow2_sh + (int64_t)e * N;
+                        Fx96 fd, fxx, fr;
+#pragma unroll 4
+                        for (int i = 0; i < N; i++) {
+                            const DivK k = K[i];
+                            const uint32_t Dv = mulmod_shoup(d.load(idx, i), __ldg(ps + i), __ldg(pss + i), k.a.x);
+                            const uint32_t xv = Rc[i * stride];
+                            const uint32_t Rv = mulmod_shoup(xv, __ldg(pe + i), __ldg(pes + i), k.a.x);
+                            Dc[i * stride] = Dv;
+                            Rc[i * stride] = Rv;
+                            fd.add(Dv, k);
+                            fxx.add(xv, k);
+                            fr.add(Rv, k);
+                        }
+                        dv_setup(st, fd.value(), s, e);
+                        U = (r2.y >> 31) ? (((u128)1) << 96) : (e < 0 ? fxx.value() : fr.value());
+                        ph = Iter;
+                    }
+                } else {
+                    ph = Dead;
+                }
+            }
+            if (__ballot_sync(FULL, ph != Dead) == 0) break;
+            if (__ballot_sync(FULL, ph == Iter) == 0) continue;
+        }
+
+        /* one step: digit, residue update, evaluation of the new remainder */
+        const bool live = ph == Iter;
+        const uint64_t qd = live ? dv_digit(st, U, C.E, st.f) : 0;
+        Fx96 fx;
+#pragma unroll 1
+        for (int i0 = 0; i0 < N; i0 += 4) {  // groups of 4: loads, arithmetic, stores
+            uint32_t rv[4], dv[4], qv[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                rv[j] = Rc[(i0 + j) * stride];
+                dv[j] = Dc[(i0 + j) * stride];
+                qv[j] = Qc[(i0 + j) * stride];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const DivK k = K[i0 + j];
+                const uint32_t m = k.a.x;
+                const uint32_t qi = kred53(qd, k);
+                const uint32_t rn = submod(kmag(rv[j], k), kmulmod(qi, dv[j], k), m);
+                rv[j] = live ? rn : rv[j];
+                qv[j] = addmod(kmag(qv[j], k), qi, m);
+                fx.add(rv[j], k);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                Rc[(i0 + j) * stride] = rv[j];
+                if (live) Qc[(i0 + j) * stride] = qv[j];
+            }
+        }
+        if (live) {
+            U = fx.value();
+            st.b = kDivB;
+            if (--st.left == 0) ph = Final;
+        }
+    }
+}
+
+/* digit steps of a division from its record (0: no step loop) */
+__device__ __forceinline__ int dv_rec_steps(const uint2 &r) {
+    if ((r.x >> 16) != kDnOk) return 0;
+    const int s = (int)(r.x & 0xffffu), e = dv_rec_e(r);
+    const int t = s % kDivB, a = s / kDivB;
+    return a + 1 - (e < 0 ? 0 : (e - t) / kDivB + 1);
+}
+
+constexpr int kDivBins = 64;  // > log2(M) / 48 + 1 for every supported moduli set
+
+/* order[begin + p] (p = 0..) = offsets of the range's numbers by decreasing
+ * step count (a counting sort; hist: this warp's kDivBins shared counters),
+ * so a warp's last divisions are its shortest and the drain is short */
+__device__ __forceinline__ void div_order(const uint2 *rec, int32_t *order, int64_t begin, int64_t end,
+                                          uint32_t *hist) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    hist[lane] = 0;
+    hist[lane + 32] = 0;
+    __syncwarp();
+    for (int64_t e = begin + lane; e < end; e += 32) atomicAdd(&hist[dv_rec_steps(rec[e])], 1u);
+    __syncwarp();
+    /* exclusive prefix over bins in decreasing order: lane l holds bins 63 - l and 31 - l */
+    const uint32_t h0 = hist[63 - lane], h1 = hist[31 - lane];
+    uint32_t s0 = h0, s1 = h1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a0 = __shfl_up_sync(FULL, s0, o), a1 = __shfl_up_sync(FULL, s1, o);
+        if (lane >= o) {
+            s0 += a0;
+            s1 += a1;
+        }
+    }
+    s1 += __shfl_sync(FULL, s0, 31);
+    __syncwarp();
+    hist[63 - lane] = s0 - h0;
+    hist[31 - lane] = s1 - h1;
+    __syncwarp();
+    for (int64_t e = begin + lane; e < end; e += 32) {
+        const uint32_t p = atomicAdd(&hist[dv_rec_steps(rec[e])], 1u);
+        order[begin + p] = (int32_t)(e - begin);
+    }
+    __syncwarp();  // the order written by one lane is read by another
+}
+
+/* both passes for one warp's range; rec / order hold one entry per number of
+ * the range's index space (index k in [begin, end)); col: this thread's
+ * 3N-word shared-memory column (row stride `stride` words); hist: this
+ * warp's kDivBins shared counters */
+template <int N>
+__device__ __forceinline__ void div_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
+                                          const Operand<N> &d, uint2 *rec, int32_t *order, const Output<N> &qo,
+                                          const Output<N> &ro, uint8_t *flags, int64_t begin, int64_t end,
+                                          uint32_t *col, int stride, uint32_t *hist) {
+    divnorm_range<N>(K, C, x, d, rec, begin, end, col, stride);
+    __syncwarp();  // records written by one lane are read by another
+    div_order(rec, order, begin, end, hist);
+    divloop_range<N>(K, C, x, d, rec, order, qo, ro, flags, begin, end, col, stride);
+}
+
+/* shared memory of a block of `threads` threads running div_range: the DivK
+ * table, the warps' counters, then the columns */
+template <int N>
+constexpr size_t div_smem_bytes(int threads) {
+    return sizeof(DivK) * N + (size_t)(threads / 32) * kDivBins * 4 + (size_t)3 * N * 4 * threads;
+}
+
+/* scratch bytes per number of the global pass-A records and the order */
+constexpr size_t kDivScratchPerNumber = sizeof(uint2) + sizeof(int32_t);
+
+}  // namespace grns

@@ -1,10 +1,13 @@
 /*
- * grns_gb300 -- division and power-of-two scaling kernels (reference-faithful
- * forms; one thread per number, operands gathered into registers/local
- * arrays, results written per modulus slice).
- *   k_div  : q = floor(X/D), r = X - qD      (reference src/rnsdiv.cuh:128)
- *   k_scale: floor(X / 2^D)                  (reference src/rnsscal.cuh:207)
+ * grns_gb300 -- division and power-of-two scaling kernels.
+ *   k_div      : q = floor(X/D), r = X - qD (reference src/rnsdiv.cuh:128),
+ *                reference-faithful FP64 form, one thread per number
+ *   k_div_warp : the same results on the integer fast path; each warp runs a
+ *                contiguous range of numbers through the division state
+ *                machine (div_warp.cuh)
+ *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
  */
+#include "div_warp.cuh"
 #include "internal.h"
 #include "rns_device.cuh"
 #include "rns_fast.cuh"
@@ -39,6 +42,34 @@ __global__ void __launch_bounds__(128) k_div(const __grid_constant__ Consts<N> C
     }
 }
 
+constexpr int kDivBlock = 128;
+
+/* resident 128-thread blocks per SM the register budget must allow: shared
+ * memory (3N words per thread) allows 4 at n <= 32 and 2 at n = 64 */
+template <int N>
+constexpr int div_min_blocks() {
+    return N > 32 ? 2 : 4;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
+    k_div_warp(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
+               int32_t *__restrict__ order, int64_t count, int64_t per_warp, Output<N> q, Output<N> r,
+               uint8_t *__restrict__ flags) {
+    extern __shared__ uint4 div_smem[];
+    DivK *K = reinterpret_cast<DivK *>(div_smem);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(K + N);
+    uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
+    divk_fill<N>(C, K);
+    __syncthreads();
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t b = w * per_warp;
+    if (b >= count) return;  // whole warp
+    const int64_t e = b + per_warp < count ? b + per_warp : count;
+    div_range<N>(K, C, x, d, rec, order, q, r, flags, b, e, cols + threadIdx.x, blockDim.x,
+                 hist + (threadIdx.x / 32) * kDivBins);
+}
+
 template <int N, bool FAST>
 __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N> C, Operand<N> x,
                                                const uint32_t *__restrict__ D, uint32_t D_uniform, int64_t count,
@@ -69,13 +100,42 @@ template <int N>
 static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
                            uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s) {
     const int B = 128;
-    if (c->path == GRNS_PATH_REFERENCE)
+    if (c->path == GRNS_PATH_REFERENCE) {
         k_div<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
                                                                count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
-    else
-        k_div<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
-                                                              count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
-    return cuda_status(cudaGetLastError());
+        return cuda_status(cudaGetLastError());
+    }
+    /* fast path: warps over contiguous ranges, as many warps as fit at once */
+    const size_t smem = div_smem_bytes<N>(kDivBlock);
+    static int per_sm[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident blocks per SM, per device
+    int &occ = per_sm[c->device & 7];
+    if (occ == 0) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_div_warp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_div_warp<N>, kDivBlock, smem) != cudaSuccess ||
+            nb < 1)
+            nb = 1;
+        occ = nb;
+    }
+    const int64_t warps_cap = (int64_t)c->sm_count * occ * (kDivBlock / 32);
+    int64_t warps = (count + 31) / 32;
+    if (warps > warps_cap) warps = warps_cap;
+    if (warps < 1) warps = 1;
+    const int64_t per_warp = (count + warps - 1) / warps;
+    const unsigned grid = (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
+    /* pass-A records and the longest-first order (12 bytes per number), stream-ordered */
+    void *scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, (size_t)count * kDivScratchPerNumber, s);
+    if (e != cudaSuccess) return cuda_status(e);
+    uint2 *rec = (uint2 *)scratch;
+    int32_t *order = (int32_t *)(rec + count);
+    k_div_warp<N><<<grid, kDivBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld}, rec, order,
+                                                count, per_warp > 0 ? per_warp : 1, Output<N>{q, ld},
+                                                Output<N>{r, ld}, flags);
+    e = cudaGetLastError();
+    cudaFreeAsync(scratch, s);
+    return cuda_status(e);
 }
 
 template <int N>

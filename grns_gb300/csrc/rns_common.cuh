@@ -24,12 +24,14 @@
 
 #ifndef __CUDACC__
 struct uint4 { uint32_t x, y, z, w; };
+struct uint2 { uint32_t x, y; };
 #endif
 
 namespace grns {
 
 constexpr int kMaxModuli = 64;
 constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/params.h:22)
+constexpr int kDivB = 48;       // quotient bits per step of the integer division
 
 struct Er {  // er_float_t
     double frac;
@@ -55,6 +57,8 @@ struct Consts {
      * frac(x_i w_i / m_i) directly from the residue x_i (frac(x w / m) = s / m). */
     uint32_t c64l[N], c64h[N];            // ceil(2^64 w_i / m_i) mod 2^64 (w-folded)
     uint32_t c96_0[N], c96_1[N], c96_2[N];  // ceil(2^96 / m_i), 32-bit words (applied to s_i)
+    uint32_t c96w_0[N], c96w_1[N], c96w_2[N];  // ceil(2^96 w_i / m_i) mod 2^96 (w-folded, applied to x_i)
+    uint32_t b48[N], b48_sh[N];           // 2^kDivB mod m_i, Shoup companion
     uint32_t t32[N], t32_sh[N];           // 2^32 mod m_i, Shoup companion
     uint32_t mrbits[N];                   // bit length of m_0 * ... * m_{t-1}
     uint64_t E;                           // sum_i (m_i - 1): fixed-point truncation error bound
@@ -67,6 +71,8 @@ struct Consts {
     const uint32_t *m_pow2;     // [30]     M mod 2^(j+1)               (RNS_MODULI_PRODUCT_POW2_RESIDUES)
     const uint32_t *pow2_inv;   // [30 * N] (2^(j+1))^-1 mod m_i        (RNS_POW2_INVERSE)
     const uint32_t *pow2_inv_sh;// [30 * N]
+    const uint32_t *pow2neg;    // [(kDivB + 1) * N]  2^-j mod m_i
+    const uint32_t *pow2neg_sh; // [(kDivB + 1) * N]
 };
 
 /* ---------------- modular arithmetic ---------------- */

@@ -131,9 +131,27 @@ GRNS_HD u128 fx96_k(const Consts<N> &C, Get get, int k) {
     return ((u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64)) & kMask96;
 }
 
+/* sum_i x_i * ceil(2^96 w_i / m_i) mod 2^96 with the constants of the
+ * parameter block (fx96_k at k = 0 without the table) */
+template <int N, class Get>
+GRNS_HD u128 fx96w(const Consts<N> &C, Get get) {
+    uint64_t S0 = 0, S1 = 0;
+    uint32_t S2 = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t x = get(i);
+        const uint64_t p0 = (uint64_t)x * C.c96w_0[i];
+        const uint64_t p1 = (uint64_t)x * C.c96w_1[i];
+        S0 += (uint32_t)p0;
+        S1 += (p0 >> 32) + (uint32_t)p1;
+        S2 += (uint32_t)(p1 >> 32) + x * C.c96w_2[i];
+    }
+    return ((u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64)) & kMask96;
+}
+
 template <int N, class Get>
 GRNS_HD u128 fx96(const Consts<N> &C, Get get) {
-    return fx96_k<N>(C, get, 0);
+    return fx96w<N>(C, get);
 }
 
 /* ---------------- mixed-radix conversion (exact) ---------------- */
@@ -198,57 +216,10 @@ GRNS_HD int cmp_fast(const Consts<N> &C, GetX gx, GetY gy) {
     return cmp_fx96_then_exact<N>(C, gx, gy);
 }
 
-/* ---------------- normalised evaluation (for division) ---------------- */
-struct Norm {
-    u128 U;  // Z * 2^k / M * 2^96 lies in [U - E, U]; U >= 2^85 when kind == 0
-    int k;
-    int kind;  // 0 normal, 1 Z == 0, 2 Z > M (1 - E/2^96) (then U = 2^96, k = 0)
-};
-
 enum : uint32_t { kFxIterCap = 1u << 2 };
-
-/* Certified enclosure of Z * 2^k / M with relative width < 2^-47, starting
- * from a magnification k0 known not to wrap (Z * 2^k0 < M). */
-template <int N, class Get>
-GRNS_HD Norm norm96(const Consts<N> &C, Get get, int k0, uint32_t &flags) {
-    const u128 lower = ((u128)1) << 85;
-    const u128 E = C.E;
-    const int eb = bitlen64(C.E);
-    int k = k0;
-#pragma unroll 1
-    for (int guard = 0; guard < 64; guard++) {
-        if (k < 0 || k > C.log2M) break;
-        u128 U = fx96_k<N>(C, get, k);
-        if (U >= lower) return Norm{U, k, 0};
-        if (U >= E) {
-            k += 89 - bitlen128(U);
-        } else if (k > 0) {
-            k += 89 - eb;
-        } else {
-            uint32_t a[N];
-            mrc_hd<N>(C, get, a);
-            int t = N - 1;
-            while (t >= 0 && a[t] == 0) t--;
-            if (t < 0) return Norm{0, 0, 1};
-            if (t == N - 1) return Norm{((u128)1) << 96, 0, 2};
-            int bz = bitlen32(a[t] + 1) + (int)C.mrbits[t];
-            k = C.log2M - bz - 7;
-            if (k < 1) k = 1;
-        }
-    }
-    flags |= kFxIterCap;
-    return Norm{0, 0, 1};
-}
 
 /* ---------------- directed-rounding helpers for the quotient estimate ---------------- */
 
-/* double <= v (v < 2^128), exact when v has <= 53 significant bits */
-GRNS_HD double u128_to_double_rd(u128 v) {
-    int bl = bitlen128(v);
-    if (bl <= 53) return (double)(uint64_t)v;
-    uint64_t top = (uint64_t)(v >> (bl - 53));
-    return std::ldexp((double)top, bl - 53);
-}
 /* double >= v */
 GRNS_HD double u128_to_double_ru(u128 v) {
     int bl = bitlen128(v);
@@ -267,79 +238,261 @@ GRNS_HD double ddiv_rd_hd(double a, double b) {
 #endif
 }
 
-/* ---------------- division (exact q, r; the results of rns_div, src/rnsdiv.cuh:128) ---------------- */
+/* ---------------- division: scaled-remainder digit recurrence ----------------
+ *
+ * q = floor(x / d), r = x - q d (the results of rns_div, src/rnsdiv.cuh:128).
+ *
+ * Pass A (dv_record) normalises, by fixed-point evaluations at k = 0 of
+ * values magnified by the uniform constant 2^48 (dn_normalize):
+ *   - the divisor: a shift s with D = d 2^s in [M/16 (1 - 2^-8), M/8 (1 + 2^-8))
+ *     (s = 0 when d >= M/8 already);
+ *   - the dividend: its magnitude, to skip the leading quotient digits that
+ *     are certainly zero, and whether it lies within E / 2^96 of M.
+ * Pass B computes floor(x 2^s / D) = q digit by digit, kDivB = 48 bits per
+ * step; s = 48 a + t with 0 <= t < 48, k leading steps skipped (0 <= k <= a):
+ *     k = 0:  R = x 2^(t-48) mod M, first step magnifies by 2^48 with the
+ *             digit estimated from x itself (b = t);
+ *     k >= 1: R = x 2^e with e = t + 48 (k - 1) (x 2^e < D certain: the
+ *             skipped digits are 0), every step b = 48;
+ *     step:   q_j = certified lower bound of floor(2^b R / D),
+ *             R <- 2^48 R - q_j D,  Q <- 2^48 Q + q_j;
+ * after a + 1 - k steps R = 2^s (x - Q d).  Every q_j is within 3 of the true
+ * digit, which keeps 0 <= R < 4D < M/2: the residues of R (computed mod M)
+ * are exact although 2^48 R itself wraps.  A final certified correction
+ * c = floor(R / D) in {0..3} gives q = Q + c, and r = x - q d.
+ *
+ * Every residue operation of a step uses the same constants for all numbers
+ * (2^48 mod m_i and the fixed-point reciprocals of the kernel parameter
+ * block); the per-number tables (2^s, 2^e) are read once per division.  The
+ * digit estimate is integer-only: the divisor's 63-bit upper mantissa Dm gets
+ * a 53-bit reciprocal Rm <= 2^126 / Dm once (the single FP64 division), each
+ * step takes the high word of At * Rm, At the top 64 bits of the remainder's
+ * lower bound.  Digit error < 1.3 per step (ratio R / D < 4), < 2.3 on a
+ * k = 0 first step (ratio x / D < 16.1).
+ */
+enum : uint32_t { kDnOk = 0, kDnNear = 1, kDnZero = 2, kDnBad = 3, kDnCap = 4 };
 
-/* 0: r < d certain, 1: r >= d certain, 2: undecided */
-GRNS_HD int norm_order(const Norm &r, const Norm &d, uint64_t Eu) {
-    const u128 E = Eu;
-    const int sh = d.k - r.k;  // r/d = (Ur / Ud) * 2^sh
-    if (sh >= 13) return 1;    // Ur - E >= 2^84 and Ud <= 2^96
-    if (sh <= -13) return 0;
-    u128 rl = r.U - E, ru = r.U, dl = d.U - E, du = d.U;
-    if (sh >= 0) {
-        rl <<= sh;
-        ru <<= sh;
-    } else {
-        dl <<= -sh;
-        du <<= -sh;
-    }
-    if (rl >= du) return 1;
-    if (ru < dl) return 0;
-    return 2;
+#ifdef __CUDACC__
+#define GRNS_HD_RARE __host__ __device__ __noinline__
+#else
+#define GRNS_HD_RARE __attribute__((noinline))
+#endif
+
+GRNS_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((u128)a * b) >> 64);
+#endif
 }
 
-/* pq residues of floor(F * 2^s) for a 53-bit F */
+/* floor(2^126 / Dm) rounded down to 53 bits, for 2^62 < Dm <= 2^63 */
+GRNS_HD uint64_t dv_recip(uint64_t Dm) {
+#ifdef __CUDA_ARCH__
+    return __double2ull_rz(__ddiv_rd(0x1p126, __ull2double_ru(Dm)));
+#else
+    return (uint64_t)ddiv_rd_hd(std::ldexp(1.0, 126), u128_to_double_ru((u128)Dm));
+#endif
+}
+
+/* v mod m_i for v < 2^53 (one Barrett step when b_i >= 27) */
 template <int N>
-GRNS_HD bool floor_scaled_residues(const Consts<N> &C, uint64_t F, int s, uint32_t *pq, int &bits) {
-    uint64_t base = F;
-    int e = 0;
-    if (s < 0) {
-        base = (-s) >= 64 ? 0 : (F >> (-s));
-    } else {
-        e = s;
+GRNS_HD uint32_t reduce53(const Consts<N> &C, int i, uint64_t v) {
+    if (C.b[i] >= 27) {  // hi * (2^32 mod m) + lo < 2^54 <= 2^(2b)
+        const uint64_t p = (uint64_t)(uint32_t)(v >> 32) * C.t32[i] + (uint32_t)v;
+        const uint32_t t = (uint32_t)(p >> (C.b[i] - 1));
+        const uint32_t q = (uint32_t)(((uint64_t)t * C.mu[i]) >> (C.b[i] + 1));
+        uint32_t r = (uint32_t)p - q * C.m[i];
+        r = umin32(r, r - C.m[i]);
+        return umin32(r, r - C.m[i]);
     }
-    bits = base ? bitlen64(base) + e : 0;
-    if (e > C.log2M) return false;  // cannot happen for a certified lower bound of r/d < M
-    const uint32_t *p2 = C.pow2 + (int64_t)e * N;
-    const uint32_t *p2s = C.pow2_sh + (int64_t)e * N;
-#pragma unroll 1
-    for (int i = 0; i < N; i++) {
-        uint32_t v;
-        if (C.b[i] >= 27) {  /* base < 2^53: hi * (2^32 mod m) + lo < 2^54 <= 2^(2b), one Barrett step */
-            uint64_t p = (uint64_t)(uint32_t)(base >> 32) * C.t32[i] + (uint32_t)base;
-            uint32_t t = (uint32_t)(p >> (C.b[i] - 1));
-            uint32_t q = (uint32_t)(((uint64_t)t * C.mu[i]) >> (C.b[i] + 1));
-            uint32_t r = (uint32_t)p - q * C.m[i];
-            r = umin32(r, r - C.m[i]);
-            v = umin32(r, r - C.m[i]);
-        } else {
-            v = reduce64<N>(C, i, base);
-        }
-        pq[i] = e ? mulmod_shoup(v, ldg_u32(p2 + i), ldg_u32(p2s + i), C.m[i]) : v;
-    }
-    return true;
+    return reduce64<N>(C, i, v);
 }
 
+template <int N>
+GRNS_HD_RARE int dv_cmp_vec(const Consts<N> &C, const uint32_t *a, const uint32_t *b) {
+    return cmp_exact<N>(C, [&](int i) { return a[i]; }, [&](int i) { return b[i]; });
+}
+
+enum : int { kNormMore = 0, kNormOk = 1, kNormNear = 2, kNormCap = 3 };
+
+/* One normalisation step of a nonzero Z: U = fx96w(Z 2^k).  U >= 2^43 fixes
+ * the magnitude: Z 2^k / M in [U - E, U] / 2^96, U >= 2^43.  Below that Z 2^k
+ * < 2^-53 M, so 2^48 more cannot wrap (the caller then magnifies its residues
+ * and k grows by 48) -- unless k = 0 and U < E, where Z may instead be within
+ * E / 2^96 of M; a magnification tells them apart: a small value then has
+ * U < 2^91 + E, a value near M U > 2^96 (1 - 2^-13) (or it wraps again and
+ * the next magnification decides). */
+template <int N>
+GRNS_HD int dn_step(const Consts<N> &C, u128 U, int &k, int &guard) {
+    if (U >= (((u128)1) << 43)) {
+        if (k > 0 && U >= (((u128)1) << 95)) return kNormNear;
+        return kNormOk;
+    }
+    k += kDivB;
+    if (++guard > 64 || k > C.log2M) return kNormCap;
+    return kNormMore;
+}
+
+/* divisor shift s from the normalised divisor (magnification k, bit length bl of U) */
+GRNS_HD int dv_shift(int k, int bl) {
+    const int s = k + 93 - bl;
+    return s < 0 ? 0 : s;
+}
+
+/* first kept quotient step: returns e (x is replaced by x 2^e), e < 0 when no
+ * step is skipped; kx, blx describe the normalised dividend */
+GRNS_HD int dv_skip(int s, int kx, int blx) {
+    const int t = s % kDivB, a = s / kDivB;
+    const int num = 91 + kx - blx - t;  // x 2^e < D certain for e <= num
+    int k = num < 0 ? 0 : num / kDivB + 1;
+    if (k > a) k = a;
+    return t + kDivB * (k - 1);
+}
+
+/* pass-A record: x = status << 16 | s, y = xnear << 31 | (e & 0xffff) */
+GRNS_HD uint2 dv_pack(uint32_t status, int s, int e, bool xnear) {
+    uint2 r;
+    r.x = (status << 16) | (uint32_t)s;
+    r.y = (xnear ? 0x80000000u : 0u) | ((uint32_t)e & 0xffffu);
+    return r;
+}
+GRNS_HD int dv_rec_e(const uint2 &r) { return (int)(int16_t)(uint16_t)(r.y & 0xffffu); }
+
+template <int N>
+GRNS_HD int dn_normalize(const Consts<N> &C, const uint32_t *z, int &k, int &bl) {
+    uint32_t w[N];
+    for (int i = 0; i < N; i++) w[i] = z[i];
+    k = 0;
+    int guard = 0;
+    for (;;) {
+        const int k0 = k;
+        const u128 U = fx96w<N>(C, [&](int i) { return w[i]; });
+        const int ns = dn_step<N>(C, U, k, guard);
+        if (ns == kNormOk) {
+            bl = bitlen128(U);
+            k = k0;
+        }
+        if (ns != kNormMore) return ns;
+        for (int i = 0; i < N; i++) w[i] = mulmod_shoup(w[i], C.b48[i], C.b48_sh[i], C.m[i]);
+    }
+}
+
+/* pass A for one number (x, d canonical) */
+template <int N>
+GRNS_HD uint2 dv_record(const Consts<N> &C, const uint32_t *x, const uint32_t *d) {
+    bool dz = true, xz = true;
+    for (int i = 0; i < N; i++) {
+        dz &= d[i] == 0;
+        xz &= x[i] == 0;
+    }
+    if (dz) return dv_pack(kDnZero, 0, 0, false);
+    int kd, bld;
+    const int nd = dn_normalize<N>(C, d, kd, bld);
+    if (nd == kNormNear) return dv_pack(kDnNear, 0, 0, false);
+    if (nd == kNormCap) return dv_pack(kDnCap, 0, 0, false);
+    const int s = dv_shift(kd, bld);
+    if (xz) return dv_pack(kDnOk, s, s % kDivB - kDivB, false);
+    int kx, blx;
+    const int nx = dn_normalize<N>(C, x, kx, blx);
+    if (nx == kNormCap) return dv_pack(kDnCap, 0, 0, false);
+    if (nx == kNormNear) return dv_pack(kDnOk, s, s % kDivB - kDivB, true);
+    return dv_pack(kDnOk, s, dv_skip(s, kx, blx), false);
+}
+
+/* pass B state of one division */
+struct DivSt {
+    u128 UD;      // D / M * 2^96 in [UD - E, UD]
+    uint64_t Rm;  // <= 2^126 / Dm,  Dm = floor(UD / 2^sd) + 1
+    int sd;
+    int b;        // magnification of the next step's digit
+    int left;     // steps still to run
+    uint32_t f;
+};
+
+GRNS_HD void dv_setup(DivSt &st, u128 UD, int s, int e) {
+    st.UD = UD;
+    st.sd = bitlen128(UD) - 63;
+    st.Rm = dv_recip((uint64_t)(UD >> st.sd) + 1);
+    const int t = s % kDivB, a = s / kDivB;
+    const int k = e < 0 ? 0 : (e - t) / kDivB + 1;
+    st.b = e < 0 ? t : kDivB;
+    st.left = a + 1 - k;
+    st.f = 0;
+}
+
+/* lower bound of floor(2^b R / D) from U = fx96w(R) (U = 2^96 stands for R
+ * within E / 2^96 of M) */
+GRNS_HD uint64_t dv_digit(const DivSt &st, u128 U, uint64_t E, uint32_t &flags) {
+    if (U <= (u128)E) return 0;
+    const u128 A = U - E;
+    const int L = bitlen128(A);
+    const uint64_t At = L >= 64 ? (uint64_t)(A >> (L - 64)) : (uint64_t)A << (64 - L);
+    const uint64_t qt = umulhi64(At, st.Rm);
+    /* 2^b R / D >= 2^b A / UD >= qt 2^(b + (L - 64) - sd - 62) */
+    const int sh = st.b + (L - 64) - st.sd - 62;
+    if (sh >= 0) {  // a digit >= 2^62: not a reachable state
+        flags |= kFxIterCap;
+        return 0;
+    }
+    return -sh >= 64 ? 0 : qt >> (-sh);
+}
+
+/* c = floor(R / D) for 0 <= R < 4D from the fixed-point values; -1 when a
+ * comparison is too close to call (the exact path decides) */
+GRNS_HD int dv_final_fx(const DivSt &st, u128 UR, uint64_t Eu) {
+    const u128 E = Eu;
+    int c = 0;
+    for (int j = 1; j <= 3; j++) {
+        const u128 jD = (u128)j * st.UD, jDl = (u128)j * (st.UD - E);
+        if (UR >= E && UR - E >= jD) {
+            c = j;  // R >= j D certain
+        } else if (UR < jDl) {
+            return c;  // R < j D certain
+        } else {
+            return -1;
+        }
+    }
+    return c;
+}
+
+/* exact c = floor(R / D) (R < 4D): repeated exact comparison and subtraction */
+template <int N>
+GRNS_HD_RARE int dv_final_exact(const Consts<N> &C, const uint32_t *R, const uint32_t *D) {
+    uint32_t a[N];
+    for (int i = 0; i < N; i++) a[i] = R[i];
+    int c = 0;
+    while (c < 3 && dv_cmp_vec<N>(C, a, D) >= 0) {
+        for (int i = 0; i < N; i++) a[i] = submod(a[i], D[i], C.m[i]);
+        c++;
+    }
+    return c;
+}
+
+/* q, r of one division (both passes, one number); q, r, x, d: N canonical
+ * residues each */
 template <int N>
 GRNS_HD void div_fast(const Consts<N> &C, uint32_t *q, uint32_t *r, const uint32_t *x, const uint32_t *d,
                       uint32_t &flags) {
-    bool dz = true;
-#pragma unroll 1
+    bool xz = true;
     for (int i = 0; i < N; i++) {
         q[i] = 0;
         r[i] = x[i];
-        dz &= d[i] == 0;
+        xz &= x[i] == 0;
     }
-    if (dz) {
+    const uint2 rec = dv_record<N>(C, x, d);
+    const uint32_t status = rec.x >> 16;
+    if (status == kDnZero) {
         flags |= 1u << 1;  // division by zero
         return;
     }
-    auto gd = [&](int i) { return d[i]; };
-    auto gr = [&](int i) { return r[i]; };
-    Norm nd = norm96<N>(C, gd, 0, flags);
-    if (nd.kind == 2) {  // d > M (1 - 2^-59): the quotient is 0 or 1
-        if (cmp_exact<N>(C, gr, gd) >= 0) {
-#pragma unroll 1
+    if (status == kDnCap) {
+        flags |= kFxIterCap;
+        return;
+    }
+    if (xz) return;
+    if (status == kDnNear) {  // d > M (1 - E / 2^96): the quotient is 0 or 1
+        if (dv_cmp_vec<N>(C, x, d) >= 0) {
             for (int i = 0; i < N; i++) {
                 q[i] = 1;
                 r[i] = submod(r[i], d[i], C.m[i]);
@@ -347,58 +500,38 @@ GRNS_HD void div_fast(const Consts<N> &C, uint32_t *q, uint32_t *r, const uint32
         }
         return;
     }
-    const int bud = bitlen128(nd.U);
-    int kr = 0;
-    const int cap = C.log2M / 40 + 12;
-    uint32_t pq[N];
-#pragma unroll 1
-    for (int it = 0;; it++) {
-        if (it > cap) {
-            flags |= kFxIterCap;
-            return;
-        }
-        bool rz = true;
-#pragma unroll 1
-        for (int i = 0; i < N; i++) rz &= r[i] == 0;
-        if (rz) return;
-        Norm nr = norm96<N>(C, gr, kr, flags);
-        if (nr.kind == 1) return;
-        int ord = norm_order(nr, nd, C.E);
-        if (ord == 0) return;
-        int g;
-        if (ord == 2) {
-            if (cmp_exact<N>(C, gr, gd) < 0) return;
-#pragma unroll 1
-            for (int i = 0; i < N; i++) pq[i] = 1;
-            g = 1;
-        } else {
-            double a = u128_to_double_rd(nr.U - (u128)C.E);
-            double b = u128_to_double_ru(nd.U);
-            double ratio = ddiv_rd_hd(a, b);  // <= (Ur - E) / Ud
-            int ex;
-            double fr = std::frexp(ratio, &ex);  // ratio = fr * 2^ex, fr in [0.5, 1)
-            uint64_t F = (uint64_t)std::ldexp(fr, 53);
-            int bits;
-            if (!floor_scaled_residues<N>(C, F, ex - 53 + (nd.k - nr.k), pq, bits)) {
-                flags |= kFxIterCap;
-                return;
-            }
-            if (bits == 0) {
-#pragma unroll 1
-                for (int i = 0; i < N; i++) pq[i] = 1;
-                bits = 1;
-            }
-            g = (bits > 44 ? bits - 44 : 0) + 1;
-        }
-#pragma unroll 1
+    const int s = (int)(rec.x & 0xffffu), e = dv_rec_e(rec);
+    uint32_t D[N], R[N], Q[N];
+    const uint32_t *ps = C.pow2 + (int64_t)s * N, *pss = C.pow2_sh + (int64_t)s * N;
+    for (int i = 0; i < N; i++) D[i] = mulmod_shoup(d[i], ldg_u32(ps + i), ldg_u32(pss + i), C.m[i]);
+    DivSt st;
+    dv_setup(st, fx96w<N>(C, [&](int i) { return D[i]; }), s, e);
+    const uint32_t *pe = e < 0 ? C.pow2neg + (int64_t)(-e) * N : C.pow2 + (int64_t)e * N;
+    const uint32_t *pes = e < 0 ? C.pow2neg_sh + (int64_t)(-e) * N : C.pow2_sh + (int64_t)e * N;
+    for (int i = 0; i < N; i++) {
+        R[i] = mulmod_shoup(x[i], ldg_u32(pe + i), ldg_u32(pes + i), C.m[i]);
+        Q[i] = 0;
+    }
+    u128 U = (rec.y >> 31) ? (((u128)1) << 96) : fx96w<N>(C, [&](int i) { return e < 0 ? x[i] : R[i]; });
+    for (; st.left > 0; st.left--) {
+        const uint64_t qd = dv_digit(st, U, C.E, st.f);
         for (int i = 0; i < N; i++) {
             const uint32_t m = C.m[i];
-            q[i] = addmod(q[i], pq[i], m);
-            r[i] = submod(r[i], mulmod_barrett(pq[i], d[i], m, C.mu[i], C.b[i]), m);
+            const uint32_t qi = reduce53<N>(C, i, qd);
+            R[i] = submod(mulmod_shoup(R[i], C.b48[i], C.b48_sh[i], m), mulmod_barrett(qi, D[i], m, C.mu[i], C.b[i]), m);
+            Q[i] = addmod(mulmod_shoup(Q[i], C.b48[i], C.b48_sh[i], m), qi, m);
         }
-        kr = nd.k + 89 - g - bud;
-        if (kr < 0) kr = 0;
+        U = fx96w<N>(C, [&](int i) { return R[i]; });
+        st.b = kDivB;
     }
+    int c = dv_final_fx(st, U, C.E);
+    if (c < 0) c = dv_final_exact<N>(C, R, D);
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = C.m[i];
+        q[i] = addmod(Q[i], (uint32_t)c % m, m);
+        r[i] = submod(x[i], mulmod_barrett(q[i], d[i], m, C.mu[i], C.b[i]), m);
+    }
+    flags |= st.f;
 }
 
 /* ---------------- power-of-two scaling (results of rns_scale2pow, src/rnsscal.cuh:93) ---------------- */

@@ -134,7 +134,8 @@ grns_status alloc_array(grns_server *sv, cudaStream_t s, int ctx, int kind, int6
     return GRNS_OK;
 }
 
-/* output arrays of a request: sizes only (for admission) */
+/* output arrays of a request plus its launch scratch (division records):
+ * sizes only (for admission) */
 size_t footprint_of(const grns_server *sv, const Req &q) {
     const grns_ctx *c = sv->ctxs[q.r.ctx_index];
     const int n = c->n;
@@ -142,7 +143,7 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
     switch (q.r.op) {
         case GRNS_OP_EVAL: return sizeof(interval_t) * k;
         case GRNS_OP_CMP: return 4 * (size_t)k;
-        case GRNS_OP_DIV: return 2 * 4 * (size_t)n * k;
+        case GRNS_OP_DIV: return (2 * 4 * (size_t)n + 12) * k;
         case GRNS_OP_SCALE2POW: return 4 * (size_t)n * k;
         case GRNS_OP_MAX: return ((4 * (size_t)n + 7) / 8) * 8 + 8;
         default: return GRNS_MPINT_BYTES(n) * (size_t)k;

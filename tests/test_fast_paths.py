@@ -141,3 +141,59 @@ def test_random_and_special(fc, tag):
     S = [rng.randrange(1, min(901, L + 40)) for _ in range(len(X))]
     S[:5] = [1, 29, 30, 31, L]
     assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64"])
+def test_division_quotient_boundaries(fc, tag):
+    """dividends just below, at and above multiples of the divisor, divisors
+    near M and near powers of two: the certified quotient estimate must never
+    overshoot and the final correction must land exactly"""
+    f = FC(fc, moduli_for(tag))
+    M = f.M
+    L = M.bit_length() - 1
+    rng = random.Random(99)
+    X, Dv = [], []
+    for _ in range(150 if f.n <= 16 else 60):
+        b = rng.randrange(1, L + 1)
+        d = rng.randrange(1 << (b - 1), 1 << b)
+        qmax = (M - 1) // d
+        q = rng.randrange(qmax + 1)
+        for x in (q * d, q * d - 1, q * d + d - 1, q * d + 1):
+            if 0 <= x < M:
+                X.append(x)
+                Dv.append(d)
+    for d in (M - 1, M - 2, (M + 1) // 2, 1 << L, (1 << L) - 1, 3):
+        for x in (M - 1, d, d - 1, d + 1, 2 * d, 2 * d - 1):
+            if 0 <= x < M and 0 < d < M:
+                X.append(x)
+                Dv.append(d)
+    q, r, fl = f.div(X, Dv)
+    assert q == [a // b for a, b in zip(X, Dv)]
+    assert r == [a % b for a, b in zip(X, Dv)]
+    assert not fl.any()
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g8", "g32", "g64"])
+def test_division_short_and_extreme_dividends(fc, tag):
+    """dividends of every length (the leading zero digits are skipped), and
+    dividends within a hair of M or of 0 (where a fixed-point evaluation
+    alone cannot tell them apart)"""
+    f = FC(fc, moduli_for(tag))
+    M = f.M
+    L = M.bit_length() - 1
+    rng = random.Random(5)
+    X, Dv = [], []
+    for _ in range(200 if f.n <= 16 else 80):
+        bx, bd = rng.randrange(1, L + 1), rng.randrange(1, L + 1)
+        X.append(rng.randrange(1 << (bx - 1), 1 << bx))
+        Dv.append(rng.randrange(1 << (bd - 1), 1 << bd))
+    for delta in (1, 2, 3, 1 << 20, 1 << 40, 1 << 70, 1 << 130, 1 << 200):
+        for d in (1, 3, 1 << 17, (1 << 61) + 5, 1 << (L // 2), M // 7, M // 3):
+            for x in (M - delta, delta):
+                if 0 <= x < M and 0 < d < M:
+                    X.append(x)
+                    Dv.append(d)
+    q, r, fl = f.div(X, Dv)
+    assert q == [a // b for a, b in zip(X, Dv)]
+    assert r == [a % b for a, b in zip(X, Dv)]
+    assert not fl.any()
