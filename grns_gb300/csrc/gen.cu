@@ -8,10 +8,11 @@
  */
 #include "internal.h"
 #include "rns_device.cuh"
+#include "rns_mpint.cuh"
 
 namespace grns {
 
-enum : uint32_t { S_X = 1, S_Y = 2, S_DLEN = 3, S_DLIMB = 4, S_SHIFT = 5 };
+enum : uint32_t { S_X = 1, S_Y = 2, S_DLEN = 3, S_DLIMB = 4, S_SHIFT = 5, S_MAG = 6, S_SIGN = 7 };
 
 __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t z) {
     z += 0x9E3779B97F4A7C15ull;
@@ -65,6 +66,43 @@ __global__ void k_gen_divisors(const __grid_constant__ Consts<N> C, uint64_t key
     }
 }
 
+/* mp_int_t records of signed integers with magnitude uniform in [0, 2^bits)
+ * and a fair-coin sign (zero keeps sign 0), as workload.mpint_values: digits
+ * (residues of the magnitude), sign, and the interval evaluation of the
+ * digits by the device evaluation (the reference's mpint_set_mpz,
+ * src/mpint.cuh:74, evaluates on the host) */
+template <int N>
+__global__ void k_gen_mpint(const __grid_constant__ Consts<N> C, uint64_t key_mag, uint64_t key_sign, int bits,
+                            int64_t count, MpInt<N> *out) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        const int nl = (bits + 31) / 32;
+        MpInt<N> v;
+        uint32_t any = 0;
+#pragma unroll 1
+        for (int i = 0; i < N; i++) v.digits[i] = 0;
+#pragma unroll 1
+        for (int j = nl - 1; j >= 0; j--) {
+            uint32_t w = (uint32_t)draw(key_mag, (uint64_t)k * 64 + j);
+            if (j == nl - 1) {
+                const int top = bits - 32 * (nl - 1);
+                if (top < 32) w &= (1u << top) - 1u;
+            }
+            any |= w;
+#pragma unroll 1
+            for (int i = 0; i < N; i++) {
+                const uint32_t m = C.m[i];
+                const uint32_t t32 = (uint32_t)((1ull << 32) % m);
+                v.digits[i] = addmod(mulmod_barrett(v.digits[i], t32, m, C.mu[i], C.b[i]), w % m, m);
+            }
+        }
+        v.sign = (any && (draw(key_sign, (uint64_t)k) & 1u)) ? 1 : 0;
+        v.pad = 0;
+        uint32_t f = 0;
+        eval<N>(C, [&](int i) { return v.digits[i]; }, v.eval[0], v.eval[1], f);
+        out[k] = v;
+    }
+}
+
 __global__ void k_gen_shifts(uint64_t key, int64_t count, uint32_t dmax, uint32_t *out) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
         out[k] = (uint32_t)__umul64hi(draw(key, (uint64_t)k), (uint64_t)dmax) + 1u;
@@ -98,6 +136,18 @@ grns_status grns_gen_divisors(grns_ctx *c, uint64_t seed, int64_t count, int lay
 #define C_(n)                                                                                                  \
     k_gen_divisors<n><<<grid_for(c, count, 128), 128, 0, (cudaStream_t)s>>>(consts_of<n>(c), kl, kw, c->log2M, \
                                                                            count, Output<n>{(uint32_t *)out, ld}); \
+    return cuda_status(cudaGetLastError())
+    GRNS_DISPATCH_N(c->n, C_)
+#undef C_
+}
+
+grns_status grns_gen_mpint(grns_ctx *c, uint64_t seed, int64_t count, int bits, void *out, void *s) {
+    if (!c || !out || count < 0 || bits < 1 || bits > 32 * 64) return GRNS_ERR_INVALID_ARGUMENT;
+    if (count == 0) return GRNS_OK;
+    const uint64_t km = stream_key(seed, S_MAG), ks = stream_key(seed, S_SIGN);
+#define C_(n)                                                                                                   \
+    k_gen_mpint<n><<<grid_for(c, count, 128), 128, 0, (cudaStream_t)s>>>(consts_of<n>(c), km, ks, bits, count,  \
+                                                                        (MpInt<n> *)out);                       \
     return cuda_status(cudaGetLastError())
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_

@@ -302,11 +302,14 @@ grns_status grns_server_reset_stats(grns_server *srv);
  * splitmix64 streams, identical to grns_gb300/workload.py:
  *   grns_gen_uniform : numbers uniform in [0, M) (independent uniform residues)
  *   grns_gen_divisors: divisors of bit length L, L uniform in [1, log2 M]
- *   grns_gen_shifts  : exponents uniform in [1, dmax] */
+ *   grns_gen_shifts  : exponents uniform in [1, dmax]
+ *   grns_gen_mpint   : mp_int_t records of signed integers, magnitude uniform in
+ *                      [0, 2^bits), fair-coin sign, interval evaluation filled */
 grns_status grns_gen_uniform(grns_ctx *ctx, uint64_t seed, uint32_t stream, int64_t count, int layout, int32_t *out,
                              void *cuda_stream);
 grns_status grns_gen_divisors(grns_ctx *ctx, uint64_t seed, int64_t count, int layout, int32_t *out, void *cuda_stream);
 grns_status grns_gen_shifts(uint64_t seed, int64_t count, uint32_t dmax, uint32_t *out, void *cuda_stream);
+grns_status grns_gen_mpint(grns_ctx *ctx, uint64_t seed, int64_t count, int bits, void *out, void *cuda_stream);
 
 #ifdef __cplusplus
 }
