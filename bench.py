@@ -217,7 +217,10 @@ def run_only(args):
         call()
     times = []
     stream = torch.cuda.current_stream()
+    flush = torch.empty(64 << 20, dtype=torch.int32, device="cuda") if args.flush else None
     for _ in range(args.steps):
+        if flush is not None:
+            flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         call()
@@ -225,7 +228,8 @@ def run_only(args):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     ms = statistics.median(times) if times else 0.0
-    print(json.dumps({"only": args.only, "count": cnt, "calls": args.warmup + args.steps, "ms_median": ms,
+    print(json.dumps({"only": args.only, "count": cnt, "flush": bool(args.flush), "calls": args.warmup + args.steps,
+                      "ms_median": ms,
                       "Mnum_s": cnt / (ms * 1e-3) / 1e6 if ms else None}))
 
 
@@ -237,6 +241,7 @@ def main():
     ap.add_argument("--impl", default="grns_gb300")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
+    ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
     ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "mpint64"], default=None,
                     help="profiling: run just this op --warmup + --steps times on --pairs numbers, no JSON line")
     args = ap.parse_args()

@@ -34,6 +34,8 @@ struct HostTables {
     std::vector<uint32_t> c64l, c64h, c96_0, c96_1, c96_2, t32, t32_sh, mrbits;
     std::vector<uint32_t> c96k;  // (log2M+1) x n x 4 words: ceil(2^96 (2^k w_i mod m_i)/m_i) mod 2^96, 0
     std::vector<uint32_t> b48, b48_sh;           // 2^kDivB mod m_i
+    std::vector<uint64_t> evl_lo, evl_hi, evu_lo, evu_hi;  // recip_rd / recip_ru * 2^100
+    uint64_t acc_lo = 0, acc_hi = 0;             // ceil(acc * 2^100)
     std::vector<uint32_t> pow2neg, pow2neg_sh;   // (kDivB+1) x n: 2^-j mod m_i
     uint64_t E = 0;  // sum_i (m_i - 1)
 };
@@ -83,6 +85,23 @@ inline void round_ratio(uint64_t p, uint64_t q, bool up, double &frac, int64_t &
 
 inline uint32_t shoup(uint32_t v, uint32_t m) { return (uint32_t)(((uint64_t)v << 32) / m); }
 
+/* v * 2^100 for a positive double v, rounded up when not an integer */
+inline void fx100_of(double v, uint64_t &lo, uint64_t &hi) {
+    int e;
+    const double f = std::frexp(v, &e);  // v = f 2^e, f in [0.5, 1)
+    const uint64_t M = (uint64_t)std::ldexp(f, 53);
+    const int sh = e + 47;               // v 2^100 = M 2^(e + 47)
+    unsigned __int128 r;
+    if (sh >= 0) {
+        r = (unsigned __int128)M << sh;
+    } else {
+        r = (unsigned __int128)M >> (-sh);
+        if (M & ((((uint64_t)1) << (-sh)) - 1)) r += 1;
+    }
+    lo = (uint64_t)r;
+    hi = (uint64_t)(r >> 64);
+}
+
 }  // namespace hostdetail
 
 /* Fills every table for the moduli m[0..n-1] (odd, pairwise coprime, validated by the caller). */
@@ -111,6 +130,7 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
     T.w.resize(n); T.w_sh.resize(n); T.mu.resize(n); T.bits.resize(n); T.rrd.resize(n); T.rru.resize(n);
     T.c64l.resize(n); T.c64h.resize(n); T.c96_0.resize(n); T.c96_1.resize(n); T.c96_2.resize(n);
     T.t32.resize(n); T.t32_sh.resize(n); T.mrbits.resize(n);
+    T.evl_lo.resize(n); T.evl_hi.resize(n); T.evu_lo.resize(n); T.evu_hi.resize(n);
     T.E = 0;
     for (int i = 0; i < n; i++) {
         int64_t mi = 1;
@@ -124,6 +144,8 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
         T.mu[i] = (uint32_t)(((unsigned __int128)1 << (2 * b)) / m[i]);
         T.rrd[i] = recip_host((double)m[i], false);
         T.rru[i] = recip_host((double)m[i], true);
+        fx100_of(T.rrd[i], T.evl_lo[i], T.evl_hi[i]);
+        fx100_of(T.rru[i], T.evu_lo[i], T.evu_hi[i]);
         unsigned __int128 c64 = ((((unsigned __int128)T.w[i]) << 64) + m[i] - 1) / m[i];  /* w-folded */
         T.c64l[i] = (uint32_t)c64;
         T.c64h[i] = (uint32_t)(c64 >> 32);
@@ -159,6 +181,7 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
     acc = acc * (1 + 0.0000001 / 2);
     acc = acc / 0.0000001;
     T.acc = acc;
+    fx100_of(T.acc, T.acc_lo, T.acc_hi);
     T.ref_factor = (int)std::floor(std::log2(1 / (2 * T.acc)));
     /* RNS_EVAL_UNIT ~ 1/M53 and RNS_EVAL_INV_UNIT ~ 1 - 1/M53 (src/rnsbase.cuh:393-411) */
     round_ratio(1, Top, false, T.unit_low.frac, T.unit_low.exp);
@@ -276,11 +299,17 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
         C.c96w_2[i] = T.c96k[(size_t)i * 4 + 2];
         C.b48[i] = T.b48[i];
         C.b48_sh[i] = T.b48_sh[i];
+        C.evl_lo[i] = T.evl_lo[i];
+        C.evl_hi[i] = T.evl_hi[i];
+        C.evu_lo[i] = T.evu_lo[i];
+        C.evu_hi[i] = T.evu_hi[i];
         C.t32[i] = T.t32[i];
         C.t32_sh[i] = T.t32_sh[i];
         C.mrbits[i] = T.mrbits[i];
     }
     C.acc = T.acc;
+    C.acc_lo = T.acc_lo;
+    C.acc_hi = T.acc_hi;
     C.ref_factor = T.ref_factor;
     C.log2M = T.log2M;
     C.unit_low = T.unit_low;

@@ -32,6 +32,7 @@
 namespace grns {
 
 constexpr int kDivRefill = 8;
+constexpr int kDivPrefetch = 64;  // pass A prefetches the operands this many numbers ahead
 
 /* per-modulus constants of the division loops (shared memory, one per modulus) */
 struct DivK {
@@ -128,6 +129,10 @@ __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C,
             const int64_t my = next + __popc(need & lt);
             next += __popc(need);
             if (ph == Idle) {
+                if (my + kDivPrefetch < end) {  // the numbers this lane will take next, into L2
+                    d.prefetch_l2(my + kDivPrefetch);
+                    x.prefetch_l2(my + kDivPrefetch);
+                }
                 if (my < end) {
                     idx = my;
                     uint32_t bad = 0, dnz = 0, xnz = 0;

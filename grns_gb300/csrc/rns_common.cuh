@@ -33,6 +33,9 @@ constexpr int kMaxModuli = 64;
 constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/params.h:22)
 constexpr int kDivB = 48;       // quotient bits per step of the integer division
 
+/* levels of the pairwise summation tree over n leaves */
+constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c((n + 1) / 2); }
+
 struct Er {  // er_float_t
     double frac;
     int64_t exp;
@@ -59,6 +62,10 @@ struct Consts {
     uint32_t c96_0[N], c96_1[N], c96_2[N];  // ceil(2^96 / m_i), 32-bit words (applied to s_i)
     uint32_t c96w_0[N], c96w_1[N], c96w_2[N];  // ceil(2^96 w_i / m_i) mod 2^96 (w-folded, applied to x_i)
     uint32_t b48[N], b48_sh[N];           // 2^kDivB mod m_i, Shoup companion
+    /* integer-pipe interval evaluation: RNS_MODULI_RECIP_RD / _RU times 2^100
+     * (exact integers below 2^100) and ceil(RNS_EVAL_ACCURACY * 2^100) */
+    uint64_t evl_lo[N], evl_hi[N], evu_lo[N], evu_hi[N];
+    uint64_t acc_lo, acc_hi;
     uint32_t t32[N], t32_sh[N];           // 2^32 mod m_i, Shoup companion
     uint32_t mrbits[N];                   // bit length of m_0 * ... * m_{t-1}
     uint64_t E;                           // sum_i (m_i - 1): fixed-point truncation error bound

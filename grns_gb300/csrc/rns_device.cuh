@@ -19,6 +19,7 @@
 #pragma once
 
 #include "rns_common.cuh"
+#include "rns_fast.cuh"
 
 namespace grns {
 
@@ -44,6 +45,16 @@ struct Operand {
     __device__ __forceinline__ uint32_t load_cs(int64_t k, int i) const {  // streaming, evict-first
         return ld ? __ldcs(base + (int64_t)i * ld + k) : __ldcs(base + k * N + i);
     }
+    /* bring number k's residues into L2 ahead of their loads */
+    __device__ __forceinline__ void prefetch_l2(int64_t k) const {
+        if (ld) {
+#pragma unroll 4
+            for (int i = 0; i < N; i++) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (int64_t)i * ld + k));
+        } else {
+#pragma unroll
+            for (int i = 0; i < N; i += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + k * N + i));
+        }
+    }
 };
 
 template <int N>
@@ -57,7 +68,6 @@ struct Output {
 
 /* ---------------- the reference's pairwise tree as a streaming counter ---------------- */
 
-constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c((n + 1) / 2); }
 
 template <int N, bool UP>
 struct PTree {
@@ -172,43 +182,25 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
     upp.exp -= K;
 }
 
-/* Common path: streams the residues through both trees; falls back to
- * eval_full for zero-free ambiguous or small values (rare for uniform X). */
+/* Common path on the integer pipe (eval_int, rns_fast.cuh: the same doubles as
+ * the FP64 directed-rounding trees, computed exactly); falls back to eval_full
+ * for ambiguous integer parts or small values (rare for uniform X). */
 template <int N, class Get>
 __device__ __forceinline__ void eval(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &flags) {
-    PTree<N, false> tl;
-    PTree<N, true> tu;
     uint32_t bad = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        uint32_t xi = get(i);
-        bad |= (uint32_t)(xi >= C.m[i]);
-        uint32_t s = mulmod_shoup(xi, C.w[i], C.w_sh[i], C.m[i]);
-        double d = u32_to_double(s);
-        tl.push(i, __dmul_rd(d, C.rrd[i]));
-        tu.push(i, __dmul_ru(d, C.rru[i]));
-    }
+    const int st = eval_int<N>(C, get, low, upp, bad);
     if (bad) {
         flags |= kFlagInvalidInput;
         low = Er{0.0, 0};
         upp = Er{0.0, 0};
         return;
     }
-    double suml = tl.total(), sumu = tu.total();
-    if (suml == 0 && sumu == 0) {
+    if (st == kEvalZero) {
         low = Er{0.0, 0};
         upp = Er{0.0, 0};
         return;
     }
-    unsigned whl = __double2uint_rz(suml), whu = __double2uint_rz(sumu);
-    double fl = __dsub_rd(suml, u32_to_double(whl));
-    double fu = __dsub_ru(sumu, u32_to_double(whu));
-    if (whl != whu || fu < C.acc) {
-        eval_full<N>(C, get, low, upp, flags);
-        return;
-    }
-    low = er_from_double(fl);
-    upp = er_from_double(fu);
+    if (st == kEvalRare) eval_full<N>(C, get, low, upp, flags);
 }
 
 /* ---------------- comparison (src/rnscmp.cuh:55-74) ---------------- */

@@ -154,6 +154,123 @@ GRNS_HD u128 fx96(const Consts<N> &C, Get get) {
     return fx96w<N>(C, get);
 }
 
+/* ---------------- interval evaluation on the integer pipe (bit-exact) ----------------
+ *
+ * The common path of rns_eval_compute (src/rnseval.cuh:182-215) multiplies
+ * s_i = x_i w_i mod m_i by RNS_MODULI_RECIP_RD / _RU with rounding down / up
+ * and adds the products pairwise with rounding down / up.  Every value on it
+ * is 0 or a double in [2^-31, 64) with 53 significant bits, i.e. an integer
+ * multiple of 2^17 at scale 2^100 below 2^106.  So each operation is computed
+ * exactly as a 128-bit integer and rounded to 53 significant bits by masking
+ * (a nonzero value is >= 2^69 at this scale, so its bit length is 64 +
+ * bitlen(hi) and the rounding position 11 + bitlen(hi) lies in the low word):
+ * the same doubles as the FP64 directed-rounding instructions, at integer-pipe
+ * speed (GB300's FP64 rate is a small fraction of its integer rate).
+ */
+struct Fx100 {
+    uint64_t lo, hi;
+};
+
+GRNS_HD Fx100 fx100_round(Fx100 v, bool up) {
+    const int t = 11 + bitlen64(v.hi);
+    const uint64_t mask = (((uint64_t)1) << t) - 1;
+    if (up) {
+        if (v.lo & mask) {
+            v.lo = (v.lo | mask) + 1;
+            v.hi += v.lo == 0 ? 1 : 0;
+        }
+    } else {
+        v.lo &= ~mask;
+    }
+    return v;
+}
+GRNS_HD Fx100 fx100_add(Fx100 a, Fx100 b) {
+    Fx100 r;
+    r.lo = a.lo + b.lo;
+    r.hi = a.hi + b.hi + (r.lo < a.lo ? 1 : 0);
+    return r;
+}
+/* s * c for c = clo + chi 2^64 with the product below 2^106 */
+GRNS_HD Fx100 fx100_mul(uint32_t s, uint64_t clo, uint64_t chi) {
+    const uint64_t p0 = (uint64_t)s * (uint32_t)clo;
+    const uint64_t p1 = (uint64_t)s * (uint32_t)(clo >> 32);
+    Fx100 r;
+    r.lo = p0 + (p1 << 32);
+    r.hi = (p1 >> 32) + (uint64_t)s * chi + (r.lo < p0 ? 1 : 0);
+    return r;
+}
+GRNS_HD bool fx100_less(const Fx100 &a, uint64_t blo, uint64_t bhi) {
+    return a.hi < bhi || (a.hi == bhi && a.lo < blo);
+}
+/* er_set_d of the double a (a = value * 2^100) */
+GRNS_HD Er er_from_fx100(const Fx100 &a) {
+    if (!a.hi && !a.lo) return Er{0.0, 0};
+    const int L = a.hi ? 64 + bitlen64(a.hi) : bitlen64(a.lo);
+    const u128 v = ((u128)a.hi << 64) | a.lo;
+    const uint64_t mant = (uint64_t)(L > 53 ? (v >> (L - 53)) : (v << (53 - L)));  // exact: 53 bits
+    const uint64_t bits = (mant & ((((uint64_t)1) << 52) - 1)) | (((uint64_t)1023) << 52);
+    return Er{bitsd(bits), (int64_t)(L - 101)};
+}
+
+/* the reference's pairwise tree (psum_rd / psum_ru, src/pairwise.cuh) as a
+ * streaming binary counter, on exact integers */
+template <int N, bool UP>
+struct Fx100Tree {
+    static constexpr int L = ilog2c(N) + 1;
+    Fx100 lv[L];
+    GRNS_HD void push(int i, Fx100 v) {
+#pragma unroll
+        for (int k = 0; k < L; k++) {
+            if (!((i >> k) & 1)) {
+                lv[k] = v;
+                return;
+            }
+            v = fx100_round(fx100_add(lv[k], v), UP);
+        }
+    }
+    GRNS_HD Fx100 total() const {
+        Fx100 acc{0, 0};
+        bool have = false;
+#pragma unroll
+        for (int k = 0; k < L; k++) {
+            if ((N >> k) & 1) {
+                acc = have ? fx100_round(fx100_add(lv[k], acc), UP) : lv[k];
+                have = true;
+            }
+        }
+        return acc;
+    }
+};
+
+enum : int { kEvalOk = 0, kEvalRare = 1, kEvalZero = 2 };
+
+/* Common path of rns_eval_compute: kEvalOk with low / upp set, kEvalZero for
+ * X = 0, kEvalRare when the integer parts of the two sums differ or the upper
+ * fraction is below RNS_EVAL_ACCURACY (the reference's mixed-radix and
+ * refinement branches decide then).  bad collects residues >= m_i. */
+template <int N, class Get>
+GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
+    Fx100Tree<N, false> tl;
+    Fx100Tree<N, true> tu;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t xi = get(i);
+        bad |= (uint32_t)(xi >= C.m[i]);
+        const uint32_t s = mulmod_shoup(xi, C.w[i], C.w_sh[i], C.m[i]);
+        tl.push(i, fx100_round(fx100_mul(s, C.evl_lo[i], C.evl_hi[i]), false));
+        tu.push(i, fx100_round(fx100_mul(s, C.evu_lo[i], C.evu_hi[i]), true));
+    }
+    Fx100 sl = tl.total(), su = tu.total();
+    if (!sl.hi && !sl.lo && !su.hi && !su.lo) return kEvalZero;
+    const uint64_t whl = sl.hi >> 36, whu = su.hi >> 36;  // integer parts (scale 2^100 = 2^(64+36))
+    sl.hi &= (((uint64_t)1) << 36) - 1;
+    su.hi &= (((uint64_t)1) << 36) - 1;
+    if (whl != whu || fx100_less(su, C.acc_lo, C.acc_hi)) return kEvalRare;
+    low = er_from_fx100(sl);
+    upp = er_from_fx100(su);
+    return kEvalOk;
+}
+
 /* ---------------- mixed-radix conversion (exact) ---------------- */
 /* digits a_0..a_{N-1} with X = sum a_t * m_0...m_{t-1}; canonical (src/mrc.cuh:101) */
 template <int N, class Get>

@@ -74,6 +74,18 @@ int fc_fx(void *p, const uint32_t *x, long cnt, uint64_t *f64, uint64_t *f96lo, 
     return 0;
 }
 
+/* integer-pipe interval evaluation: status per number (kEvalOk / kEvalRare /
+ * kEvalZero, 8 for an invalid residue) and, for kEvalOk, the interval */
+int fc_eval(void *p, const uint32_t *x, long cnt, int32_t *status, Er *iv) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) { uint32_t bad = 0; Er lo{0, 0}, up{0, 0}; \
+        int st = eval_int<N>(K<N>(b), [&](int i) { return x[k * N + i]; }, lo, up, bad); \
+        status[k] = bad ? 8 : st; iv[2 * k] = lo; iv[2 * k + 1] = up; }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
 uint64_t fc_E(void *p) { return ((Box *)p)->T.E; }
 
 }

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from grns_gb300 import workload as W
-from tests.helpers import moduli_for
+from tests.helpers import IV_DTYPE as IV, moduli_for
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SMALL_SETS = [[3, 5, 7, 11], [3, 5, 7, 11, 13, 17, 19, 23], [3, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43]]
@@ -29,7 +29,7 @@ def fc(tmp_path_factory):
     L.fc_destroy.argtypes = [ctypes.c_void_p]
     L.fc_E.restype = ctypes.c_uint64
     L.fc_E.argtypes = [ctypes.c_void_p]
-    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx"):
+    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval"):
         getattr(L, f).argtypes = None
     return L
 
@@ -197,3 +197,29 @@ def test_division_short_and_extreme_dividends(fc, tag):
     assert q == [a // b for a, b in zip(X, Dv)]
     assert r == [a % b for a, b in zip(X, Dv)]
     assert not fl.any()
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+def test_integer_eval_is_bit_exact(fc, tag):
+    """the integer-pipe evaluation returns, on its common path, the same two
+    doubles as the reference's FP64 directed-rounding evaluation (device path
+    of rns_eval_compute as restated in the oracle), and hands every other
+    number (ambiguous integer part, small fraction) to the rare path"""
+    from oracle import oracle as O
+    mods = moduli_for(tag)
+    f, orc = FC(fc, mods), O.Oracle(mods)
+    M = f.M
+    rng = random.Random(41)
+    vals = [rng.randrange(M) for _ in range(3000)]
+    vals += [0, 1, 2, M - 1, M - 2, M // 2, M // 3, (M + 1) // 2] + [M >> j for j in range(1, 200, 7)]
+    vals += [rng.randrange(M >> 40) for _ in range(200)]
+    x = f.res(vals)
+    st = np.zeros(len(vals), np.int32)
+    iv = np.zeros(len(vals), IV)
+    fc.fc_eval(f.h, f.P(x), ctypes.c_long(len(vals)), f.P(st), f.P(iv))
+    want = orc.eval(x.view(np.int32), path=O.PATH_DEVICE)
+    ok = st == 0
+    assert ok.sum() > 2500
+    assert iv[ok].tobytes() == want[ok].tobytes()
+    assert all((s == 2) == (v == 0) for s, v in zip(st, vals))
+    assert not (st == 8).any()
