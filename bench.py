@@ -6,13 +6,22 @@ plus power-of-two scaling of 2^18 numbers with the n = 32 greedy moduli set
 [1, 959], scaling exponents uniform in [1, 900].  Metric: RNS numbers per
 second (a division pair counts as one number), whole job.
 
-Extra lines in the same JSON record: eval+cmp at n = 32 and n = 8 (2^20
-pairs), the reference-layout (AoS) form of the same calls, and the
-dominant kernel's roofline.  Inputs are generated on the device by the
-seeded generator; the timed region starts with them resident in HBM.  L2
-is flushed (256 MiB write) between timed steps, outside the events.
+The same JSON record carries the other workloads (skipped with --quick):
+  extra:      eval+cmp at n = 8 and n = 32 (2^20 pairs, SoA and the
+              reference's AoS layout), rns_eval_compute alone (n = 32, 2^22),
+              mp_int add/sub/mul at n = 64 (2^22 pairs, magnitudes < 2^950),
+              the maximum over 2^24 numbers at n = 64 -- each with its HBM
+              roofline fraction;
+  workloads:  4096 uneven jobs (log-uniform lengths in [1e2, 1e6]) in one
+              persistent launch captured as a CUDA graph vs one plain call per
+              job; a served request stream (n = 32 and n = 64 contexts,
+              log-uniform lengths in [1e3, 1e7], Poisson arrivals at swept
+              rates) with p50/p99 latency vs per-request plain calls.
+Inputs are generated on the device by the seeded generator; timed regions
+start with them resident in HBM.  L2 is flushed (256 MiB write) between timed
+calls, outside the events.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--quick] [--impl reference]
 """
 import argparse
 import json
@@ -28,6 +37,17 @@ sys.path.insert(0, ROOT)
 N32 = 32
 PAIRS = 1 << 18
 CMP_PAIRS = 1 << 20
+EVAL_COUNT = 1 << 22
+MP_PAIRS = 1 << 22          # mp_int pairs at n = 64
+MP_BITS = 950               # mp_int magnitudes uniform in [0, 2^950)
+MAX_COUNT = 1 << 24         # maximum over 2^24 numbers at n = 64
+BATCH_JOBS = 4096
+BATCH_LEN = (1e2, 1e6)      # log-uniform job lengths
+SERVE_REQS = 64
+SERVE_LEN = (1e3, 1e7)      # log-uniform request lengths
+SERVE_POOL = 10 ** 7        # device-resident operand pools
+SERVE_BUDGET = 48 << 30     # server HBM budget for outputs
+SERVE_LOADS = (0.5, 0.9)    # offered load as a fraction of the all-at-once throughput
 DMAX = 900
 SEED = 20260101
 
@@ -233,6 +253,351 @@ def run_only(args):
                       "Mnum_s": cnt / (ms * 1e-3) / 1e6 if ms else None}))
 
 
+# ---------------------------------------------------------------------------
+# timing helpers
+
+def _ev():
+    import torch
+    return torch.cuda.Event(enable_timing=True)
+
+
+def time_calls(fn, steps, stream, flush=None):
+    """per-call device time (ms) of fn() on `stream`, L2 flushed before each call"""
+    import torch
+    out = []
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        a, b = _ev(), _ev()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return out
+
+
+def log_uniform_lengths(rng, count, lo, hi):
+    import math
+    return [int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) for _ in range(count)]
+
+
+# ---------------------------------------------------------------------------
+# eval + cmp (n = 8 and n = 32), eval alone, mp_int and max (n = 64)
+
+def bench_eval_cmp(ctx_for, L, dev, stream, sp, P, seed, steps, flush, peak):
+    import torch
+    from grns_gb300 import native
+    from grns_gb300.workload import S_X, S_Y
+    res = {}
+    for n in (8, 32):
+        c2 = ctx_for(n)
+        a = torch.empty((n, CMP_PAIRS), dtype=torch.int32, device=dev)
+        bb = torch.empty_like(a)
+        native.check(L.grns_gen_uniform(c2.handle, seed, S_X, CMP_PAIRS, 0, P(a), sp))
+        native.check(L.grns_gen_uniform(c2.handle, seed, S_Y, CMP_PAIRS, 0, P(bb), sp))
+        out = torch.empty(CMP_PAIRS, dtype=torch.int32, device=dev)
+        for layout, lname in ((0, "soa"), (1, "aos")):
+            A = a if layout == 0 else a.t().contiguous()
+            B = bb if layout == 0 else bb.t().contiguous()
+            f = lambda: native.check(L.grns_cmp(c2.handle, P(A), P(B), CMP_PAIRS, layout, P(out), None, sp))  # noqa
+            time_calls(f, 3, stream)
+            m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+            rate = CMP_PAIRS / (m * 1e-3)
+            gbs = (8 * n + 4) * rate / 1e9
+            res[f"eval_cmp_n{n}_{lname}"] = {"Mnum_s": rate / 1e6, "GBps": gbs, "frac_hbm": gbs / peak,
+                                             "ms": m, "pairs": CMP_PAIRS}
+    # rns_eval_compute alone at n = 32: reads 128 B, writes one interval (32 B) per number
+    c32 = ctx_for(32)
+    cnt = EVAL_COUNT
+    x = torch.empty((32, cnt), dtype=torch.int32, device=dev)
+    native.check(L.grns_gen_uniform(c32.handle, seed, S_X, cnt, 0, P(x), sp))
+    iv = torch.empty(cnt * 32, dtype=torch.uint8, device=dev)
+    f = lambda: native.check(L.grns_eval(c32.handle, P(x), cnt, 0, P(iv), None, sp))  # noqa
+    time_calls(f, 3, stream)
+    m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+    gbs = (4 * 32 + 32) * cnt / (m * 1e-3) / 1e9
+    res["eval_n32_soa"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": gbs, "frac_hbm": gbs / peak, "ms": m,
+                           "count": cnt, "bytes_per_number": 160}
+    return res
+
+
+def bench_mpint_max(ctx_for, L, dev, stream, sp, P, seed, steps, flush, peak):
+    """mp_int add / sub / mul at n = 64 (2^22 pairs, magnitudes below 2^950, random
+    signs) and the maximum over 2^24 uniform numbers at n = 64"""
+    import torch
+    import grns_gb300 as G
+    from grns_gb300 import native
+    from grns_gb300.workload import S_X
+    c64 = ctx_for(64)
+    mb = G.mpint_bytes(64)
+    cnt = MP_PAIRS
+    ma = torch.empty(cnt * mb, dtype=torch.uint8, device=dev)
+    mc = torch.empty_like(ma)
+    mo = torch.empty_like(ma)
+    native.check(L.grns_gen_mpint(c64.handle, seed, cnt, MP_BITS, P(ma), sp))
+    native.check(L.grns_gen_mpint(c64.handle, seed + 1, cnt, MP_BITS, P(mc), sp))
+    res = {}
+    for op in ("add", "sub", "mul"):
+        fn = getattr(L, f"grns_mpint_{op}")
+        f = lambda: native.check(fn(c64.handle, P(ma), P(mc), cnt, P(mo), None, sp))  # noqa
+        time_calls(f, 3, stream)
+        m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+        gbs = 3 * mb * cnt / (m * 1e-3) / 1e9
+        res[f"mpint_{op}_n64"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": gbs, "frac_hbm": gbs / peak, "ms": m,
+                                  "pairs": cnt, "bytes_per_pair": 3 * mb}
+    del ma, mc, mo
+    cnt = MAX_COUNT
+    x = torch.empty((64, cnt), dtype=torch.int32, device=dev)
+    native.check(L.grns_gen_uniform(c64.handle, seed, S_X, cnt, 0, P(x), sp))
+    val = torch.empty(64, dtype=torch.int32, device=dev)
+    idx = torch.empty(1, dtype=torch.int64, device=dev)
+    scratch = torch.empty(c64.max_scratch_size(cnt), dtype=torch.uint8, device=dev)
+    f = lambda: native.check(L.grns_max(c64.handle, P(x), cnt, 0, P(val), P(idx), P(scratch),  # noqa
+                                        scratch.numel(), sp))
+    time_calls(f, 3, stream)
+    m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+    gbs = 4 * 64 * cnt / (m * 1e-3) / 1e9
+    res["max_n64_soa"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": gbs, "frac_hbm": gbs / peak, "ms": m,
+                          "count": cnt, "bytes_per_number": 256}
+    return res
+
+
+# ---------------------------------------------------------------------------
+# batched uneven workload (n = 32): one persistent launch (CUDA graph) vs one plain call per job
+
+def bench_batched(ctx_for, L, dev, stream, sp, P, seed, steps, flush):
+    import random
+    import ctypes
+    import torch
+    from grns_gb300 import native
+    from grns_gb300.workload import S_X, S_Y
+    c = ctx_for(32)
+    n = 32
+    rng = random.Random(seed)
+    lens = log_uniform_lengths(rng, BATCH_JOBS, *BATCH_LEN)
+    ops = [rng.choice((native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX)) for _ in lens]
+    pool = max(lens)
+    # operand pools in the reference's AoS layout: a job is a window [o, o + len) of them
+    X = torch.empty((pool, n), dtype=torch.int32, device=dev)
+    Y = torch.empty_like(X)
+    Dv = torch.empty_like(X)
+    Sh = torch.empty(pool, dtype=torch.int32, device=dev)
+    native.check(L.grns_gen_uniform(c.handle, seed, S_X, pool, 1, P(X), sp))
+    native.check(L.grns_gen_uniform(c.handle, seed, S_Y, pool, 1, P(Y), sp))
+    native.check(L.grns_gen_divisors(c.handle, seed, pool, 1, P(Dv), sp))
+    native.check(L.grns_gen_shifts(seed, pool, DMAX, P(Sh), sp))
+    offs = [rng.randrange(pool - ln + 1) for ln in lens]
+    # outputs: one region per kind, carved per job
+    tot = {op: sum(ln for ln, o in zip(lens, ops) if o == op) for op in set(ops)}
+    q_all = torch.empty(max(1, tot.get(native.OP_DIV, 0)) * n, dtype=torch.int32, device=dev)
+    r_all = torch.empty_like(q_all)
+    s_all = torch.empty(max(1, tot.get(native.OP_SCALE2POW, 0)) * n, dtype=torch.int32, device=dev)
+    c_all = torch.empty(max(1, tot.get(native.OP_CMP, 0)), dtype=torch.int32, device=dev)
+    nmax = sum(1 for o in ops if o == native.OP_MAX)
+    mv_all = torch.empty(max(1, nmax) * n, dtype=torch.int32, device=dev)
+    mi_all = torch.empty(max(1, nmax), dtype=torch.int64, device=dev)
+    jobs = (native.Job * BATCH_JOBS)()
+    calls = []
+    cur = {native.OP_DIV: 0, native.OP_SCALE2POW: 0, native.OP_CMP: 0, native.OP_MAX: 0}
+    for t, (ln, op, o) in enumerate(zip(lens, ops, offs)):
+        j = jobs[t]
+        j.op, j.layout, j.count, j.ld = op, 1, ln, 0
+        a = X.data_ptr() + 4 * n * o
+        j.a = a
+        k = cur[op]
+        if op == native.OP_CMP:
+            b, o0 = Y.data_ptr() + 4 * n * o, c_all.data_ptr() + 4 * k
+            j.b, j.out0 = b, o0
+            cur[op] += ln
+            calls.append((L.grns_cmp, (c.handle, a, b, ln, 1, o0, None, sp)))
+        elif op == native.OP_DIV:
+            b, o0, o1 = Dv.data_ptr() + 4 * n * o, q_all.data_ptr() + 4 * n * k, r_all.data_ptr() + 4 * n * k
+            j.b, j.out0, j.out1 = b, o0, o1
+            cur[op] += ln
+            calls.append((L.grns_div, (c.handle, a, b, ln, 1, o0, o1, None, sp)))
+        elif op == native.OP_SCALE2POW:
+            b, o0 = Sh.data_ptr() + 4 * o, s_all.data_ptr() + 4 * n * k
+            j.b, j.out0 = b, o0
+            cur[op] += ln
+            calls.append((L.grns_scale2pow, (c.handle, a, b, 0, ln, 1, o0, None, sp)))
+        else:
+            o0, o1 = mv_all.data_ptr() + 4 * n * k, mi_all.data_ptr() + 8 * k
+            j.out0, j.out1 = o0, o1
+            cur[op] += 1
+            calls.append((L.grns_max, (c.handle, a, ln, 1, o0, o1, None, 0, sp)))
+    total = sum(lens)
+
+    def per_call(sub=calls):
+        for fn, args in sub:
+            native.check(fn(*args))
+
+    # plain per-call form (integer fast path)
+    per_call()
+    torch.cuda.synchronize()
+    t_call = statistics.median(time_calls(per_call, max(2, steps // 2), stream, flush))
+    # autotuned schedules, then one persistent launch captured as a CUDA graph
+    tuned = {}
+    for op in (native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX):
+        sc, ms = native.Schedule(), ctypes.c_double()
+        native.check(L.grns_autotune(c.handle, op, 1 << 18, None, ctypes.byref(sc), ctypes.byref(ms)))
+        tuned[str(op)] = {"coop": sc.coop, "chunk": sc.chunk}
+    h = ctypes.c_void_p()
+    native.check(L.grns_batch_create(c.handle, jobs, BATCH_JOBS, 1, ctypes.byref(h)))
+    launch = lambda: native.check(L.grns_batch_launch(h, sp))  # noqa
+    for _ in range(2):
+        launch()
+    torch.cuda.synchronize()
+    t_batch = statistics.median(time_calls(launch, max(3, steps), stream, flush))
+    L.grns_batch_destroy(h)
+    # the reference-faithful per-call form on a sample: the 64 shortest jobs (its division is
+    # orders of magnitude slower, so the full job list would take minutes)
+    L.grns_ctx_set_path(c.handle, 1)
+    samp = sorted(range(BATCH_JOBS), key=lambda k: lens[k])[:64]
+    sub = [calls[k] for k in samp]
+    per_call(sub)
+    torch.cuda.synchronize()
+    t_ref = statistics.median(time_calls(lambda: per_call(sub), 2, stream, flush))
+    L.grns_ctx_set_path(c.handle, 0)
+    ref_numbers = sum(lens[k] for k in samp)
+    return {
+        "jobs": BATCH_JOBS, "numbers": total, "lengths": f"log-uniform [{BATCH_LEN[0]:g}, {BATCH_LEN[1]:g}]",
+        "ops": "uniform over eval+cmp, div, scale2pow, max; AoS operand windows",
+        "batched_Mnum_s": total / (t_batch * 1e-3) / 1e6, "batched_ms": t_batch,
+        "per_call_Mnum_s": total / (t_call * 1e-3) / 1e6, "per_call_ms": t_call,
+        "batched_vs_per_call": t_call / t_batch,
+        "reference_path_per_call_Mnum_s": ref_numbers / (t_ref * 1e-3) / 1e6,
+        "reference_path_sample": f"the {len(samp)} shortest jobs ({ref_numbers} numbers), reference-faithful "
+                                 "kernels, one plain call per job",
+        "batched_vs_reference_path_per_call": (total / t_batch) / (ref_numbers / t_ref),
+        "schedules": tuned, "graph": True,
+    }
+
+
+# ---------------------------------------------------------------------------
+# served stream: n = 32 and n = 64 contexts, Poisson arrivals, continuous batching
+
+def bench_served(ctx_for, L, dev, stream, sp, P, seed):
+    import random
+    import torch
+    import grns_gb300 as G
+    from grns_gb300 import native
+    from grns_gb300.serve import Server
+    from grns_gb300.workload import S_X, S_Y
+    c32, c64 = ctx_for(32), ctx_for(64)
+    pool = SERVE_POOL
+    X = torch.empty((32, pool), dtype=torch.int32, device=dev)
+    Y = torch.empty_like(X)
+    Dv = torch.empty_like(X)
+    Sh = torch.empty(pool, dtype=torch.int32, device=dev)
+    native.check(L.grns_gen_uniform(c32.handle, seed, S_X, pool, 0, P(X), sp))
+    native.check(L.grns_gen_uniform(c32.handle, seed, S_Y, pool, 0, P(Y), sp))
+    native.check(L.grns_gen_divisors(c32.handle, seed, pool, 0, P(Dv), sp))
+    native.check(L.grns_gen_shifts(seed, pool, DMAX, P(Sh), sp))
+    mb = G.mpint_bytes(64)
+    MA = torch.empty(pool * mb, dtype=torch.uint8, device=dev)
+    MC = torch.empty_like(MA)
+    native.check(L.grns_gen_mpint(c64.handle, seed, pool, MP_BITS, P(MA), sp))
+    native.check(L.grns_gen_mpint(c64.handle, seed + 1, pool, MP_BITS, P(MC), sp))
+    X64 = torch.empty((64, pool), dtype=torch.int32, device=dev)
+    native.check(L.grns_gen_uniform(c64.handle, seed, S_X, pool, 0, P(X64), sp))
+    torch.cuda.synchronize()
+    sv = Server(budget_bytes=SERVE_BUDGET, slots=4, max_jobs=256, admission_timeout_ms=0)
+    i32, i64 = sv.add_context(c32), sv.add_context(c64)
+    hX = sv.put(i32, X)
+    hY = sv.put(i32, Y)
+    hD = sv.put(i32, Dv)
+    hS = sv.put(i32, Sh, kind=native.ARRAY_U32, count=pool)
+    hMA = sv.put(i64, MA, kind=native.ARRAY_MPINT, count=pool)
+    hMC = sv.put(i64, MC, kind=native.ARRAY_MPINT, count=pool)
+    hX64 = sv.put(i64, X64)
+    rng = random.Random(seed + 7)
+    lens = log_uniform_lengths(rng, SERVE_REQS, *SERVE_LEN)
+    kinds = [rng.choice(("cmp", "div", "scale2pow", "mpint_mul", "max")) for _ in lens]
+    spec = {"cmp": (i32, hX, hY), "div": (i32, hX, hD), "scale2pow": (i32, hX, hS),
+            "mpint_mul": (i64, hMA, hMC), "max": (i64, hX64, 0)}
+
+    def run(rate):
+        """submit the request list at Poisson times (rate requests/s, 0: all at once), wait for all"""
+        sv.reset_stats()
+        gaps = [rng.expovariate(rate) if rate else 0.0 for _ in lens]
+        ids = []
+        t0 = time.perf_counter()
+        due = t0
+        for ln, kd, g in zip(lens, kinds, gaps):
+            due += g
+            now = time.perf_counter()
+            if due > now:
+                time.sleep(due - now)
+            ci, a, b = spec[kd]
+            ids.append(sv.submit(kd, ci, a, b, count=ln))
+        outs = []
+        for rid in ids:
+            st, o0, o1 = sv.wait(rid)
+            if st != 0:
+                raise RuntimeError(f"served request failed with status {st}")
+            outs.append((o0, o1))
+        wall = time.perf_counter() - t0
+        stats = sv.stats()
+        for o0, o1 in outs:
+            for hnd in (o0, o1):
+                if hnd:
+                    sv.free(hnd)
+        return wall, stats
+
+    run(0)  # warm-up
+    wall_all, st_all = run(0)
+    total = sum(lens)
+    cap_rps = len(lens) / wall_all
+    sweeps = []
+    for frac in SERVE_LOADS:
+        wall, st = run(frac * cap_rps)
+        sweeps.append({"offered_load": frac, "rate_req_s": frac * cap_rps, "Mnum_s": total / wall / 1e6,
+                       "p50_ms": st["p50_us"] / 1e3, "p99_ms": st["p99_us"] / 1e3,
+                       "mean_jobs_per_launch": st["mean_jobs_per_launch"], "launches": st["launches"]})
+    sv.close()
+    # the same requests as plain per-request calls, one after another
+    outs = {"cmp": torch.empty(pool, dtype=torch.int32, device=dev), "q": torch.empty_like(X),
+            "r": torch.empty_like(X), "s": torch.empty_like(X), "m": torch.empty_like(MA),
+            "mv": torch.empty(64, dtype=torch.int32, device=dev), "mi": torch.empty(1, dtype=torch.int64, device=dev)}
+    svc = []
+    for ln, kd in zip(lens, kinds):
+        if kd == "cmp":
+            xs, ys = X[:, :ln].contiguous(), Y[:, :ln].contiguous()
+            f = lambda: native.check(L.grns_cmp(c32.handle, P(xs), P(ys), ln, 0, P(outs["cmp"]), None, sp))  # noqa
+        elif kd == "div":
+            xs, ys = X[:, :ln].contiguous(), Dv[:, :ln].contiguous()
+            f = lambda: native.check(L.grns_div(c32.handle, P(xs), P(ys), ln, 0, P(outs["q"]), P(outs["r"]),  # noqa
+                                                None, sp))
+        elif kd == "scale2pow":
+            xs = X[:, :ln].contiguous()
+            f = lambda: native.check(L.grns_scale2pow(c32.handle, P(xs), P(Sh), 0, ln, 0, P(outs["s"]),  # noqa
+                                                      None, sp))
+        elif kd == "mpint_mul":
+            f = lambda: native.check(L.grns_mpint_mul(c64.handle, P(MA), P(MC), ln, P(outs["m"]), None, sp))  # noqa
+        else:
+            xs = X64[:, :ln].contiguous()
+            f = lambda: native.check(L.grns_max(c64.handle, P(xs), ln, 0, P(outs["mv"]), P(outs["mi"]),  # noqa
+                                                None, 0, sp))
+        f()
+        svc.append(time_calls(f, 1, stream)[0])
+    svc_sorted = sorted(svc)
+    t_plain = sum(svc)
+    return {
+        "requests": len(lens), "numbers": total, "lengths": f"log-uniform [{SERVE_LEN[0]:g}, {SERVE_LEN[1]:g}]",
+        "ops": "uniform over eval+cmp, div, scale2pow (n=32), mp_int mul, max (n=64)",
+        "all_at_once": {"Mnum_s": total / wall_all / 1e6, "p50_ms": st_all["p50_us"] / 1e3,
+                        "p99_ms": st_all["p99_us"] / 1e3, "mean_jobs_per_launch": st_all["mean_jobs_per_launch"]},
+        "poisson": sweeps,
+        "per_request_plain": {"Mnum_s": total / (t_plain * 1e-3) / 1e6,
+                              "p50_ms": svc_sorted[len(svc) // 2],
+                              "p99_ms": svc_sorted[min(len(svc) - 1, int(0.99 * len(svc)))],
+                              "note": "service time of each call alone (no queueing), device events"},
+    }
+
+
+# ---------------------------------------------------------------------------
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -240,6 +605,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="grns_gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
     ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "mpint64"], default=None,
@@ -259,14 +625,22 @@ def main():
     from grns_gb300.workload import S_X, S_Y
     import ctypes
 
-    ctx = G.RNSContext(greedy(N32))
+    ctxs = {}
+
+    def ctx_for(n):
+        if n not in ctxs:
+            ctxs[n] = G.RNSContext(greedy(n))
+        return ctxs[n]
+
+    ctx = ctx_for(N32)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     seed = SEED + rank
+    peak, peak_kind = load_peaks()
 
-    # ---- inputs resident in HBM (SoA) ----
+    # ---- headline: div + scale2pow at n = 32, inputs resident in HBM (SoA) ----
     x = torch.empty((N32, PAIRS), dtype=torch.int32, device=dev)
     d = torch.empty_like(x)
     xs = torch.empty_like(x)
@@ -277,8 +651,6 @@ def main():
     native.check(L.grns_gen_shifts(seed, PAIRS, DMAX, P(D), sp))
     q, r, so = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
     flush = torch.empty(64 << 20, dtype=torch.int32, device=dev)  # 256 MiB > L2
-
-    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
     def step(timers=None):
         e0, e1, e2 = (timers or (None, None, None))
@@ -296,85 +668,71 @@ def main():
     with Clocks(local) as clk:
         for _ in range(args.steps):
             flush.zero_()
-            t = (ev(), ev(), ev())
+            t = (_ev(), _ev(), _ev())
             step(t)
             torch.cuda.synchronize()
             div_ms.append(t[0].elapsed_time(t[1]))
             scale_ms.append(t[1].elapsed_time(t[2]))
             step_ms.append(t[0].elapsed_time(t[2]))
+        # ---- end to end through the C ABI with host buffers (pinned), copies inside the timed region ----
+        hx = x.cpu().pin_memory(); hd = d.cpu().pin_memory(); hxs = xs.cpu().pin_memory(); hD = D.cpu().pin_memory()
+        hq = torch.empty_like(hx).pin_memory(); hr = torch.empty_like(hx).pin_memory()
+        hso = torch.empty_like(hx).pin_memory()
+        e2e_ms = []
+        for i in range(args.warmup + args.steps):
+            flush.zero_()
+            a, b = _ev(), _ev()
+            a.record(stream)
+            x.copy_(hx, non_blocking=True); d.copy_(hd, non_blocking=True)
+            xs.copy_(hxs, non_blocking=True); D.copy_(hD, non_blocking=True)
+            step()
+            hq.copy_(q, non_blocking=True); hr.copy_(r, non_blocking=True); hso.copy_(so, non_blocking=True)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                e2e_ms.append(a.elapsed_time(b))
     total_ms = barrier_max(sum(step_ms), world)
     ms = total_ms / args.steps
     value = world * 2 * PAIRS / (ms * 1e-3) / 1e6
-
-    # ---- end to end through the C ABI with host buffers (pinned), copies inside the timed region ----
-    hx = x.cpu().pin_memory(); hd = d.cpu().pin_memory(); hxs = xs.cpu().pin_memory(); hD = D.cpu().pin_memory()
-    hq = torch.empty_like(hx).pin_memory(); hr = torch.empty_like(hx).pin_memory(); hso = torch.empty_like(hx).pin_memory()
-    e2e_ms = []
-    for i in range(args.warmup + args.steps):
-        flush.zero_()
-        a, b = ev(), ev()
-        a.record(stream)
-        x.copy_(hx, non_blocking=True); d.copy_(hd, non_blocking=True)
-        xs.copy_(hxs, non_blocking=True); D.copy_(hD, non_blocking=True)
-        step()
-        hq.copy_(q, non_blocking=True); hr.copy_(r, non_blocking=True); hso.copy_(so, non_blocking=True)
-        b.record(stream)
-        torch.cuda.synchronize()
-        if i >= args.warmup:
-            e2e_ms.append(a.elapsed_time(b))
     e2e = world * 2 * PAIRS / (barrier_max(sum(e2e_ms), world) / args.steps * 1e-3) / 1e6
     h2d = 4 * (x.numel() * 3 + D.numel())
     d2h = 4 * x.numel() * 3
+    del hx, hd, hxs, hD, hq, hr, hso
 
-    # ---- extra lines: eval+cmp (960-bit and 240-bit), SoA and the reference AoS layout ----
-    extra = {}
-    for n in (32, 8):
-        c2 = G.RNSContext(greedy(n))
-        a = torch.empty((n, CMP_PAIRS), dtype=torch.int32, device=dev)
-        bb = torch.empty_like(a)
-        native.check(L.grns_gen_uniform(c2.handle, seed, S_X, CMP_PAIRS, 0, P(a), sp))
-        native.check(L.grns_gen_uniform(c2.handle, seed, S_Y, CMP_PAIRS, 0, P(bb), sp))
-        out = torch.empty(CMP_PAIRS, dtype=torch.int32, device=dev)
-        for layout, lname in ((0, "soa"), (1, "aos")):
-            A = a if layout == 0 else a.t().contiguous()
-            B = bb if layout == 0 else bb.t().contiguous()
-            for _ in range(3):
-                native.check(L.grns_cmp(c2.handle, P(A), P(B), CMP_PAIRS, layout, P(out), None, sp))
-            tt = []
-            for _ in range(max(3, args.steps)):
-                flush.zero_()
-                s0, s1 = ev(), ev()
-                s0.record(stream)
-                native.check(L.grns_cmp(c2.handle, P(A), P(B), CMP_PAIRS, layout, P(out), None, sp))
-                s1.record(stream)
-                torch.cuda.synchronize()
-                tt.append(s0.elapsed_time(s1))
-            m = statistics.median(tt)
-            extra[f"eval_cmp_n{n}_{lname}_Mnum_s"] = CMP_PAIRS / (m * 1e-3) / 1e6
-            if lname == "soa":
-                bytes_pair = 8 * n + 4
-                extra[f"eval_cmp_n{n}_soa_GBps"] = bytes_pair * CMP_PAIRS / (m * 1e-3) / 1e9
-        c2.close()
+    # ---- the other workloads (rank 0 measurements, in the same JSON record) ----
+    extra, workloads = {}, {}
+    if not args.quick and rank == 0:
+        with Clocks(local) as clk2:
+            extra.update(bench_eval_cmp(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush, peak))
+            torch.cuda.empty_cache()
+            extra.update(bench_mpint_max(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush, peak))
+            torch.cuda.empty_cache()
+            workloads["batched_uneven_n32"] = bench_batched(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush)
+            torch.cuda.empty_cache()
+            workloads["served_stream_n32_n64"] = bench_served(ctx_for, L, dev, stream, sp, P, seed)
+            torch.cuda.empty_cache()
+        extra["clocks_other_workloads"] = clk2.summary()
 
-    peak, peak_kind = load_peaks()
     div_avg = statistics.mean(div_ms)
-    alg_bytes = 16 * N32 * PAIRS
+    alg_bytes = (4 * 4 * N32) * PAIRS  # x, d read; q, r written
     achieved = alg_bytes / (div_avg * 1e-3) / 1e9
     line = {
         "metric": "RNS Mnum/s div+scale2pow (960-bit, n=32)", "value": value, "unit": "Mnum/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+u64",
         "data": "synthetic (seeded splitmix64 generator, device-generated)",
         "config": {"workload": "div 2^18 pairs (divisor bits uniform in [1,959]) + scale2pow 2^18 numbers "
                                "(D uniform in [1,900]), n=32 greedy moduli from 2^30-1, SoA",
                    "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "k_div<32>", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_div_warp<32>", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "note": "division is compute-bound (FP64/INT pipes), not HBM-bound"},
-        "kernels_ms": {"k_div": div_avg, "k_scale": statistics.mean(scale_ms)},
+                     "note": "division is integer-pipe bound (48-bit digit steps); the HBM-bound kernels "
+                             "(eval, cmp, max, mp_int) carry their own fractions in extra"},
+        "kernels_ms": {"k_div_warp": div_avg, "k_scale": statistics.mean(scale_ms)},
         "e2e": {"value": e2e, "unit": "Mnum/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 2 * args.steps,
         "extra": extra,
+        "workloads": workloads,
     }
     line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu:
