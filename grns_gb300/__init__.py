@@ -144,6 +144,16 @@ class RNSContext:
                                      _stream(stream)), "grns_eval")
         return out
 
+    def rns_eval_tight(self, x, layout="soa", flags=None, stream=None):
+        """one-ulp certified enclosures of X/M, never wider than rns_eval_compute's
+        (not bit-identical to them)"""
+        import torch
+        count = self._count(x, layout)
+        out = torch.empty(count * 32, dtype=torch.uint8, device=x.device)
+        check(native.lib().grns_eval_tight(self._h, _ptr(x), count, LAYOUTS[layout], _ptr(out), _ptr(flags),
+                                           _stream(stream)), "grns_eval_tight")
+        return out
+
     def rns_cmp(self, x, y, layout="soa", flags=None, stream=None):
         import torch
         count = self._count(x, layout)

@@ -36,6 +36,7 @@ struct HostTables {
     std::vector<uint32_t> b48, b48_sh;           // 2^kDivB mod m_i
     std::vector<uint64_t> evl_lo, evl_hi, evu_lo, evu_hi;  // recip_rd / recip_ru * 2^100
     uint64_t acc_lo = 0, acc_hi = 0;             // ceil(acc * 2^100)
+    std::vector<uint32_t> c128w;                 // n x 4 words: ceil(2^128 w_i / m_i) mod 2^128
     std::vector<uint32_t> pow2neg, pow2neg_sh;   // (kDivB+1) x n: 2^-j mod m_i
     uint64_t E = 0;  // sum_i (m_i - 1)
 };
@@ -157,6 +158,22 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
         T.t32[i] = (uint32_t)((((uint64_t)1) << 32) % m[i]);
         T.t32_sh[i] = shoup(T.t32[i], m[i]);
         T.E += m[i] - 1;
+    }
+    /* ceil(2^128 w_i / m_i) by long division in 32-bit steps (w_i < m_i) */
+    T.c128w.assign((size_t)n * 4, 0);
+    for (int i = 0; i < n; i++) {
+        uint64_t r = T.w[i];
+        uint32_t q[4];
+        for (int j = 3; j >= 0; j--) {
+            const uint64_t v = r << 32;
+            q[j] = (uint32_t)(v / m[i]);
+            r = v % m[i];
+        }
+        if (r) {  // round up, carrying through the words (mod 2^128)
+            for (int j = 0; j < 4; j++)
+                if (++q[j] != 0) break;
+        }
+        for (int j = 0; j < 4; j++) T.c128w[(size_t)i * 4 + j] = q[j];
     }
     /* bit length of P_t = m_0 * ... * m_{t-1} */
     {
@@ -299,6 +316,10 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
         C.c96w_2[i] = T.c96k[(size_t)i * 4 + 2];
         C.b48[i] = T.b48[i];
         C.b48_sh[i] = T.b48_sh[i];
+        C.c128w_0[i] = T.c128w[(size_t)i * 4 + 0];
+        C.c128w_1[i] = T.c128w[(size_t)i * 4 + 1];
+        C.c128w_2[i] = T.c128w[(size_t)i * 4 + 2];
+        C.c128w_3[i] = T.c128w[(size_t)i * 4 + 3];
         C.evl_lo[i] = T.evl_lo[i];
         C.evl_hi[i] = T.evl_hi[i];
         C.evu_lo[i] = T.evu_lo[i];

@@ -58,6 +58,8 @@ inline unsigned grid_for(const grns_ctx *c, int64_t work, int block, int per_sm 
 }
 
 /* launchers (one translation unit per op family) */
+grns_status launch_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
+                              uint8_t *flags, cudaStream_t s);
 grns_status launch_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                         uint8_t *flags, cudaStream_t s);
 grns_status launch_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, int64_t ld, int64_t count,

@@ -24,6 +24,34 @@ __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> 
     }
 }
 
+/* one-ulp enclosure where certified (rns_fast.cuh eval_tight), the
+ * bit-exact evaluation otherwise (noinline: rare for uniform X) */
+template <int N>
+__device__ __noinline__ void eval_tight_fallback(const Consts<N> &C, const Operand<N> x, int64_t k, Er &lo, Er &up,
+                                                 uint32_t &f) {
+    eval<N>(C, [&](int i) { return x.load(k, i); }, lo, up, f);
+}
+
+template <int N>
+__global__ void __launch_bounds__(256) k_eval_tight(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+                                                    Er *__restrict__ out, uint8_t *__restrict__ flags) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t f = 0, bad = 0;
+        Er lo, up;
+        const bool ok = eval_tight<N>(C, [&](int i) { return x.load_cs(k, i); }, lo, up, bad);
+        if (bad) {
+            f = kFlagInvalidInput;
+            lo = Er{0.0, 0};
+            up = Er{0.0, 0};
+        } else if (!ok) {
+            eval_tight_fallback<N>(C, x, k, lo, up, f);
+        }
+        out[2 * k] = lo;
+        out[2 * k + 1] = up;
+        if (flags) flags[k] = (uint8_t)f;
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(256) k_cmp(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> y,
                                              int64_t count, int32_t *__restrict__ out, uint8_t *__restrict__ flags) {
@@ -168,6 +196,21 @@ static grns_status run_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t 
         k_cmp_fast<N><<<grid_for(c, count, B, 3), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{y, ld},
                                                             count, out, flags);
     return cuda_status(cudaGetLastError());
+}
+
+template <int N>
+static grns_status run_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
+                                  uint8_t *flags, cudaStream_t s) {
+    const int B = 256;
+    k_eval_tight<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out, flags);
+    return cuda_status(cudaGetLastError());
+}
+
+grns_status launch_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
+                              uint8_t *flags, cudaStream_t s) {
+#define C_(n) return run_eval_tight<n>(c, x, ld, count, out, flags, s)
+    GRNS_DISPATCH_N(c->n, C_)
+#undef C_
 }
 
 grns_status launch_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,

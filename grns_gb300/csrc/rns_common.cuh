@@ -66,6 +66,8 @@ struct Consts {
      * (exact integers below 2^100) and ceil(RNS_EVAL_ACCURACY * 2^100) */
     uint64_t evl_lo[N], evl_hi[N], evu_lo[N], evu_hi[N];
     uint64_t acc_lo, acc_hi;
+    /* one-ulp evaluation: ceil(2^128 w_i / m_i) mod 2^128, 32-bit words (w-folded) */
+    uint32_t c128w_0[N], c128w_1[N], c128w_2[N], c128w_3[N];
     uint32_t t32[N], t32_sh[N];           // 2^32 mod m_i, Shoup companion
     uint32_t mrbits[N];                   // bit length of m_0 * ... * m_{t-1}
     uint64_t E;                           // sum_i (m_i - 1): fixed-point truncation error bound

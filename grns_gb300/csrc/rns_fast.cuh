@@ -271,6 +271,73 @@ GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &ba
     return kEvalOk;
 }
 
+/* ---------------- one-ulp interval evaluation ----------------
+ *
+ * T = sum_i x_i ceil(2^128 w_i / m_i) mod 2^128 exceeds 2^128 frac(X/M) by
+ * less than E = sum_i x_i (frac(x w / m) = s / m), so when T >= E,
+ * X/M lies in ((T - E) / 2^128, T / 2^128] -- an interval of width < 2^-93.
+ * Rounded outward to 53-bit er_float bounds it is at most one unit in the last
+ * place wide whenever both ends round down to the same double.  X/M (M odd,
+ * X != 0) is never a dyadic rational, so no double enclosure of it -- the
+ * reference's included -- is narrower than one ulp: this interval is never
+ * wider than rns_eval_compute's (src/rnseval.cuh:182).  Otherwise (T < E: X
+ * near 0 or M; the ends in different ulps) the caller falls back to the
+ * bit-exact evaluation.
+ */
+template <int N, class Get>
+GRNS_HD u128 fx128w(const Consts<N> &C, Get get, uint64_t &sumx, uint32_t &bad) {
+    uint64_t S0 = 0, S1 = 0, S2 = 0;
+    uint32_t S3 = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t x = get(i);
+        bad |= (uint32_t)(x >= C.m[i]);
+        sumx += x;
+        const uint64_t p0 = (uint64_t)x * C.c128w_0[i];
+        const uint64_t p1 = (uint64_t)x * C.c128w_1[i];
+        const uint64_t p2 = (uint64_t)x * C.c128w_2[i];
+        S0 += (uint32_t)p0;
+        S1 += (p0 >> 32) + (uint32_t)p1;
+        S2 += (p1 >> 32) + (uint32_t)p2;
+        S3 += (uint32_t)(p2 >> 32) + x * C.c128w_3[i];
+    }
+    return (u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64) + ((u128)S3 << 96);
+}
+
+/* er_float of v / 2^128 rounded to 53 bits (down, or up), for v > 0; also
+ * the rounded-down mantissa and bit length (to compare two values' ulps) */
+GRNS_HD Er er_fx128(u128 v, bool up, uint64_t &mant, int &L) {
+    L = bitlen128(v);
+    uint64_t m;
+    if (L > 53) {
+        m = (uint64_t)(v >> (L - 53));
+        const bool inexact = (v & ((((u128)1) << (L - 53)) - 1)) != 0;
+        mant = m;
+        if (up && inexact && ++m == (((uint64_t)1) << 53)) {
+            m >>= 1;
+            return Er{bitsd(((m & ((((uint64_t)1) << 52) - 1)) | (((uint64_t)1023) << 52))), (int64_t)(L - 128)};
+        }
+    } else {
+        m = (uint64_t)v << (53 - L);
+        mant = m;
+    }
+    return Er{bitsd((m & ((((uint64_t)1) << 52) - 1)) | (((uint64_t)1023) << 52)), (int64_t)(L - 129)};
+}
+
+/* the one-ulp interval of X/M when certified (returns true), else false;
+ * bad collects residues >= m_i */
+template <int N, class Get>
+GRNS_HD bool eval_tight(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
+    uint64_t sumx = 0;
+    const u128 T = fx128w<N>(C, get, sumx, bad);
+    if (T <= (u128)sumx) return false;  // X near 0 or M (or X = 0)
+    uint64_t ml, mu;
+    int Ll, Lu;
+    low = er_fx128(T - sumx, false, ml, Ll);
+    upp = er_fx128(T, true, mu, Lu);
+    return Ll == Lu && ml == mu;
+}
+
 /* ---------------- mixed-radix conversion (exact) ---------------- */
 /* digits a_0..a_{N-1} with X = sum a_t * m_0...m_{t-1}; canonical (src/mrc.cuh:101) */
 template <int N, class Get>

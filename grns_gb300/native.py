@@ -25,6 +25,7 @@ SIGNATURES = {
     "grns_ctx_set_path": (c_int, [c_void_p, c_int]),
     "grns_device_ceil_log2": (c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
     "grns_eval": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "grns_eval_tight": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_cmp": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_div": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "grns_scale2pow": (c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_int64, c_int, c_void_p, c_void_p, c_void_p]),

@@ -106,6 +106,16 @@ grns_status grns_device_ceil_log2(const double *x, int32_t *out, int64_t count, 
 grns_status grns_eval(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, interval_t *out,
                       uint8_t *flags, void *stream);
 
+/* out[k] = the narrowest enclosure of X_k / M with er_float bounds: one unit
+ * in the last place wide wherever a 128-bit fixed-point evaluation certifies
+ * it, and grns_eval's interval elsewhere (X near 0 or M, bounds straddling
+ * two ulps).  Never wider than cuda::rns_eval_compute's interval (no double
+ * interval around a nonzero X/M with odd M is narrower than one ulp), but not
+ * bit-identical to it: the fast form of rns_eval_compute (reference
+ * src/rnseval.cuh:182) for callers that need a certified enclosure. */
+grns_status grns_eval_tight(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, interval_t *out,
+                            uint8_t *flags, void *stream);
+
 /* ---- magnitude comparison ----
  * out[k] = sign(X_k - Y_k) in {-1, 0, 1}, as cuda::rns_cmp
  * (reference src/rnscmp.cuh:55); the evaluations stay in registers. */

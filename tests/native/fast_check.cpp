@@ -86,6 +86,18 @@ int fc_eval(void *p, const uint32_t *x, long cnt, int32_t *status, Er *iv) {
     return 0;
 }
 
+/* one-ulp evaluation: 1 where certified (interval written), 0 where the
+ * bit-exact evaluation would be used */
+int fc_eval_tight(void *p, const uint32_t *x, long cnt, int32_t *ok, Er *iv) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) { uint32_t bad = 0; Er lo{0, 0}, up{0, 0}; \
+        ok[k] = eval_tight<N>(K<N>(b), [&](int i) { return x[k * N + i]; }, lo, up, bad) ? 1 : 0; \
+        iv[2 * k] = lo; iv[2 * k + 1] = up; }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
 uint64_t fc_E(void *p) { return ((Box *)p)->T.E; }
 
 }

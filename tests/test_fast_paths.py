@@ -29,7 +29,7 @@ def fc(tmp_path_factory):
     L.fc_destroy.argtypes = [ctypes.c_void_p]
     L.fc_E.restype = ctypes.c_uint64
     L.fc_E.argtypes = [ctypes.c_void_p]
-    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval"):
+    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight"):
         getattr(L, f).argtypes = None
     return L
 
@@ -223,3 +223,37 @@ def test_integer_eval_is_bit_exact(fc, tag):
     assert iv[ok].tobytes() == want[ok].tobytes()
     assert all((s == 2) == (v == 0) for s, v in zip(st, vals))
     assert not (st == 8).any()
+
+
+def er_fraction(frac, exp):
+    return Fraction(float(frac)) * Fraction(2) ** int(exp)
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+def test_one_ulp_evaluation(fc, tag):
+    """where the 128-bit evaluation certifies it, the interval encloses X/M
+    exactly, is at most one ulp wide, and is never wider than the reference's
+    interval (rns_eval_compute, device path restated in the oracle)"""
+    from oracle import oracle as O
+    mods = moduli_for(tag)
+    f, orc = FC(fc, mods), O.Oracle(mods)
+    M = f.M
+    rng = random.Random(43)
+    vals = [rng.randrange(M) for _ in range(1500)] + [rng.randrange(M >> 30) for _ in range(100)]
+    vals += [1, 2, M - 1, M // 2, M // 3, (M + 1) // 2] + [M >> j for j in range(1, 120, 9)]
+    x = f.res(vals)
+    ok = np.zeros(len(vals), np.int32)
+    iv = np.zeros(len(vals), IV)
+    fc.fc_eval_tight(f.h, f.P(x), ctypes.c_long(len(vals)), f.P(ok), f.P(iv))
+    ref = orc.eval(x.view(np.int32), path=O.PATH_DEVICE)
+    assert ok.sum() > 1400
+    for k in np.nonzero(ok)[0]:
+        v = Fraction(vals[k], M)
+        lo = er_fraction(iv[k]["low"]["frac"], iv[k]["low"]["exp"])
+        up = er_fraction(iv[k]["upp"]["frac"], iv[k]["upp"]["exp"])
+        assert lo < v <= up
+        ulp = Fraction(2) ** (int(iv[k]["low"]["exp"]) - 52)
+        assert up - lo <= ulp
+        rlo = er_fraction(ref[k]["low"]["frac"], ref[k]["low"]["exp"])
+        rup = er_fraction(ref[k]["upp"]["frac"], ref[k]["upp"]["exp"])
+        assert up - lo <= rup - rlo

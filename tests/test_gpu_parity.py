@@ -267,3 +267,37 @@ def test_vector_paths_with_tails(case, count):
     x[count - 1] = x[0]  # a repeated value at the tail
     val, idx = ctx.rns_max(to_dev(x, "soa"), layout="soa")
     assert int(idx.item()) == orc.max(x)
+
+
+def _erf(frac, exp):
+    from fractions import Fraction
+    return Fraction(float(frac)) * Fraction(2) ** int(exp)
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_eval_tight(case, layout):
+    """grns_eval_tight: every interval encloses X/M and is never wider than
+    grns_eval's (the reference's) interval; most are one ulp wide; where it
+    could not certify one ulp it returns grns_eval's interval bit for bit"""
+    from fractions import Fraction
+    tag, ctx, orc, g = case
+    M = orc.exact.M
+    rng = random.Random(7)
+    vals = [rng.randrange(M) for _ in range(1500)] + [0, 1, M - 1, M // 2] + [rng.randrange(M >> 40) for _ in range(60)]
+    x = to_dev(W.to_residues(vals, moduli_for(tag), layout="aos"), layout)
+    tight = ctx.rns_eval_tight(x, layout=layout).cpu().numpy().view(IV_DTYPE)
+    ref = ctx.rns_eval_compute(x, layout=layout).cpu().numpy().view(IV_DTYPE)
+    one_ulp = 0
+    for k, v in enumerate(vals):
+        lo, up = _erf(*tight[k]["low"]), _erf(*tight[k]["upp"])
+        rlo, rup = _erf(*ref[k]["low"]), _erf(*ref[k]["upp"])
+        if v == 0:
+            assert tight[k].tobytes() == ref[k].tobytes()
+            continue
+        assert lo <= Fraction(v, M) <= up
+        assert up - lo <= rup - rlo
+        if up - lo <= Fraction(2) ** (int(tight[k]["low"]["exp"]) - 52):
+            one_ulp += 1
+        else:
+            assert tight[k].tobytes() == ref[k].tobytes()
+    assert one_ulp > 1400
