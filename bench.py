@@ -195,7 +195,7 @@ def run_only(args):
     from grns_gb300 import native
     from grns_gb300.workload import S_X, S_Y
     L = native.lib(build_if_missing=True)
-    n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "mpint64": 64}[args.only]
+    n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32, "mpint64": 64}[args.only]
     ctx = G.RNSContext(greedy(n))
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -230,6 +230,8 @@ def run_only(args):
             native.check(L.grns_max(ctx.handle, P(x), cnt, 0, P(val), P(idx), None, 0, sp))
         elif args.only == "eval32":
             native.check(L.grns_eval(ctx.handle, P(x), cnt, 0, P(out), None, sp))
+        elif args.only == "evtight32":
+            native.check(L.grns_eval_tight(ctx.handle, P(x), cnt, 0, P(out), None, sp))
         elif args.only == "mpint64":
             native.check(L.grns_mpint_mul(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
 
@@ -608,7 +610,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
-    ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "mpint64"], default=None,
+    ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "evtight32", "mpint64"], default=None,
                     help="profiling: run just this op --warmup + --steps times on --pairs numbers, no JSON line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.only is None else args.warmup

@@ -52,6 +52,50 @@ __global__ void __launch_bounds__(256) k_eval_tight(const __grid_constant__ Cons
     }
 }
 
+/* four consecutive numbers per thread with 16-byte loads of each modulus
+ * slice (SoA, leading dimension a multiple of 4, 16-byte aligned base) */
+template <int N>
+__global__ void __launch_bounds__(256, 2) k_eval_tight_soa4(const __grid_constant__ Consts<N> C, Operand<N> x,
+                                                            int64_t count, Er *__restrict__ out,
+                                                            uint8_t *__restrict__ flags) {
+    const int64_t quads = count / 4;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < quads; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = 4 * t;
+        Fx128 f[4];
+        uint32_t bad = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(x.base + (int64_t)i * x.ld + k));
+            const uint32_t m = C.m[i], c0 = C.c128w_0[i], c1 = C.c128w_1[i], c2 = C.c128w_2[i], c3 = C.c128w_3[i];
+            bad |= (uint32_t)(v.x >= m) | (uint32_t)(v.y >= m) | (uint32_t)(v.z >= m) | (uint32_t)(v.w >= m);
+            f[0].add(v.x, c0, c1, c2, c3);
+            f[1].add(v.y, c0, c1, c2, c3);
+            f[2].add(v.z, c0, c1, c2, c3);
+            f[3].add(v.w, c0, c1, c2, c3);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            Er lo, up;
+            uint32_t fl = 0;
+            const bool ok = !bad && eval_tight_finish(f[j].value(), C.E, lo, up);
+            if (!ok) eval_tight_fallback<N>(C, x, k + j, lo, up, fl);  // invalid residues are flagged there
+            out[2 * (k + j)] = lo;
+            out[2 * (k + j) + 1] = up;
+            if (flags) flags[k + j] = (uint8_t)fl;
+        }
+    }
+    const int64_t tail = 4 * quads + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tail < count) {
+        uint32_t fl = 0, bad = 0;
+        Er lo, up;
+        const bool ok = eval_tight<N>(C, [&](int i) { return x.load(tail, i); }, lo, up, bad);
+        if (bad || !ok) eval_tight_fallback<N>(C, x, tail, lo, up, fl);
+        out[2 * tail] = lo;
+        out[2 * tail + 1] = up;
+        if (flags) flags[tail] = (uint8_t)fl;
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(256) k_cmp(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> y,
                                              int64_t count, int32_t *__restrict__ out, uint8_t *__restrict__ flags) {
@@ -202,7 +246,12 @@ template <int N>
 static grns_status run_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                                   uint8_t *flags, cudaStream_t s) {
     const int B = 256;
-    k_eval_tight<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out, flags);
+    if (ld != 0 && ld % 4 == 0 && ((uintptr_t)x % 16) == 0)
+        k_eval_tight_soa4<N><<<grid_for(c, (count + 3) / 4, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld},
+                                                                             count, (Er *)out, flags);
+    else
+        k_eval_tight<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
+                                                           flags);
     return cuda_status(cudaGetLastError());
 }
 

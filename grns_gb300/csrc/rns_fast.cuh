@@ -274,8 +274,8 @@ GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &ba
 /* ---------------- one-ulp interval evaluation ----------------
  *
  * T = sum_i x_i ceil(2^128 w_i / m_i) mod 2^128 exceeds 2^128 frac(X/M) by
- * less than E = sum_i x_i (frac(x w / m) = s / m), so when T >= E,
- * X/M lies in ((T - E) / 2^128, T / 2^128] -- an interval of width < 2^-93.
+ * less than sum_i x_i <= E = sum_i (m_i - 1) (frac(x w / m) = s / m), so when
+ * T > E, X/M lies in ((T - E) / 2^128, T / 2^128] -- width < 2^-90.
  * Rounded outward to 53-bit er_float bounds it is at most one unit in the last
  * place wide whenever both ends round down to the same double.  X/M (M odd,
  * X != 0) is never a dyadic rational, so no double enclosure of it -- the
@@ -284,25 +284,23 @@ GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &ba
  * near 0 or M; the ends in different ulps) the caller falls back to the
  * bit-exact evaluation.
  */
-template <int N, class Get>
-GRNS_HD u128 fx128w(const Consts<N> &C, Get get, uint64_t &sumx, uint32_t &bad) {
+/* one residue's term of the 128-bit sum (S3 keeps bits 96..127) */
+struct Fx128 {
     uint64_t S0 = 0, S1 = 0, S2 = 0;
     uint32_t S3 = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        const uint32_t x = get(i);
-        bad |= (uint32_t)(x >= C.m[i]);
-        sumx += x;
-        const uint64_t p0 = (uint64_t)x * C.c128w_0[i];
-        const uint64_t p1 = (uint64_t)x * C.c128w_1[i];
-        const uint64_t p2 = (uint64_t)x * C.c128w_2[i];
+    GRNS_HD void add(uint32_t x, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
+        const uint64_t p0 = (uint64_t)x * c0;
+        const uint64_t p1 = (uint64_t)x * c1;
+        const uint64_t p2 = (uint64_t)x * c2;
         S0 += (uint32_t)p0;
         S1 += (p0 >> 32) + (uint32_t)p1;
         S2 += (p1 >> 32) + (uint32_t)p2;
-        S3 += (uint32_t)(p2 >> 32) + x * C.c128w_3[i];
+        S3 += (uint32_t)(p2 >> 32) + x * c3;
     }
-    return (u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64) + ((u128)S3 << 96);
-}
+    GRNS_HD u128 value() const {
+        return (u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64) + ((u128)S3 << 96);
+    }
+};
 
 /* er_float of v / 2^128 rounded to 53 bits (down, or up), for v > 0; also
  * the rounded-down mantissa and bit length (to compare two values' ulps) */
@@ -324,18 +322,28 @@ GRNS_HD Er er_fx128(u128 v, bool up, uint64_t &mant, int &L) {
     return Er{bitsd((m & ((((uint64_t)1) << 52) - 1)) | (((uint64_t)1023) << 52)), (int64_t)(L - 129)};
 }
 
-/* the one-ulp interval of X/M when certified (returns true), else false;
- * bad collects residues >= m_i */
-template <int N, class Get>
-GRNS_HD bool eval_tight(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
-    uint64_t sumx = 0;
-    const u128 T = fx128w<N>(C, get, sumx, bad);
-    if (T <= (u128)sumx) return false;  // X near 0 or M (or X = 0)
+/* the one-ulp interval of X/M from T = the 128-bit sum (true when certified) */
+GRNS_HD bool eval_tight_finish(u128 T, uint64_t E, Er &low, Er &upp) {
+    if (T <= (u128)E) return false;  // X near 0 or M (or X = 0)
     uint64_t ml, mu;
     int Ll, Lu;
-    low = er_fx128(T - sumx, false, ml, Ll);
+    low = er_fx128(T - E, false, ml, Ll);
     upp = er_fx128(T, true, mu, Lu);
     return Ll == Lu && ml == mu;
+}
+
+/* one number: the one-ulp interval when certified (returns true), else
+ * false; bad collects residues >= m_i */
+template <int N, class Get>
+GRNS_HD bool eval_tight(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
+    Fx128 f;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t x = get(i);
+        bad |= (uint32_t)(x >= C.m[i]);
+        f.add(x, C.c128w_0[i], C.c128w_1[i], C.c128w_2[i], C.c128w_3[i]);
+    }
+    return eval_tight_finish(f.value(), C.E, low, upp);
 }
 
 /* ---------------- mixed-radix conversion (exact) ---------------- */
