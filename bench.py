@@ -320,7 +320,14 @@ def bench_eval_cmp(ctx_for, L, dev, stream, sp, P, seed, steps, flush, peak):
     m = statistics.median(time_calls(f, max(3, steps), stream, flush))
     gbs = (4 * 32 + 32) * cnt / (m * 1e-3) / 1e9
     res["eval_n32_soa"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": gbs, "frac_hbm": gbs / peak, "ms": m,
-                           "count": cnt, "bytes_per_number": 160}
+                           "count": cnt, "bytes_per_number": 160, "kernel": "k_eval (bit-identical intervals)"}
+    f = lambda: native.check(L.grns_eval_tight(c32.handle, P(x), cnt, 0, P(iv), None, sp))  # noqa
+    time_calls(f, 3, stream)
+    m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+    gbs = (4 * 32 + 32) * cnt / (m * 1e-3) / 1e9
+    res["eval_tight_n32_soa"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": gbs, "frac_hbm": gbs / peak, "ms": m,
+                                 "count": cnt, "bytes_per_number": 160,
+                                 "kernel": "k_eval_tight_soa4 (one-ulp intervals, never wider than the reference's)"}
     return res
 
 
