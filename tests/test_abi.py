@@ -16,6 +16,8 @@ def declared_symbols():
     names = set()
     inc = os.path.join(ROOT, "include", "grns")
     for f in os.listdir(inc):
+        if not f.endswith(".h"):  # device.cuh is the header-only namespace-cuda drop-in, not C ABI
+            continue
         src = open(os.path.join(inc, f)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         src = re.sub(r"//[^\n]*", "", src)
