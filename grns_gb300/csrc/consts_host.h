@@ -37,7 +37,9 @@ struct HostTables {
     std::vector<uint64_t> evl_lo, evl_hi, evu_lo, evu_hi;  // recip_rd / recip_ru * 2^100
     uint64_t acc_lo = 0, acc_hi = 0;             // ceil(acc * 2^100)
     std::vector<uint32_t> c128w;                 // n x 4 words: ceil(2^128 w_i / m_i) mod 2^128
-    std::vector<uint32_t> pow2neg, pow2neg_sh;   // (kDivB+1) x n: 2^-j mod m_i
+    std::vector<uint32_t> pow2neg, pow2neg_sh;   // kPow2NegRows x n: 2^-j mod m_i
+    std::vector<uint64_t> mi64;                  // M_i mod 2^64
+    uint64_t m64 = 0;                            // M mod 2^64
     uint64_t E = 0;  // sum_i (m_i - 1)
 };
 
@@ -237,10 +239,10 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
             row[2] = (uint32_t)(c >> 64);
         }
     }
-    /* division: 2^kDivB mod m_i and 2^-j mod m_i for j = 0..kDivB */
+    /* division and scaling: 2^kDivB mod m_i and 2^-j mod m_i for j < kPow2NegRows */
     T.b48.resize(n);
     T.b48_sh.resize(n);
-    T.pow2neg.resize((size_t)(kDivB + 1) * n);
+    T.pow2neg.resize((size_t)kPow2NegRows * n);
     T.pow2neg_sh.resize(T.pow2neg.size());
     for (int i = 0; i < n; i++) {
         uint64_t v = 1;
@@ -249,11 +251,21 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
         T.b48_sh[i] = shoup((uint32_t)v, m[i]);
         const uint64_t half = (m[i] + 1) / 2;  // 2^-1 mod m_i (m_i odd)
         uint64_t u = 1;
-        for (int j = 0; j <= kDivB; j++) {
+        for (int j = 0; j < kPow2NegRows; j++) {
             T.pow2neg[(size_t)j * n + i] = (uint32_t)u;
             T.pow2neg_sh[(size_t)j * n + i] = shoup((uint32_t)u, m[i]);
             u = (u * half) % m[i];
         }
+    }
+    /* scaling: M_i mod 2^64 and M mod 2^64 */
+    T.mi64.assign(n, 0);
+    T.m64 = 1;
+    for (int i = 0; i < n; i++) T.m64 *= m[i];
+    for (int i = 0; i < n; i++) {
+        uint64_t v = 1;
+        for (int j = 0; j < n; j++)
+            if (j != i) v *= m[j];
+        T.mi64[i] = v;
     }
     /* MRC_MULT_INV as [j*n + i] = m_j^-1 mod m_i for j < i */
     T.mrc_inv.assign((size_t)n * n, 0);
@@ -316,6 +328,7 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
         C.c96w_2[i] = T.c96k[(size_t)i * 4 + 2];
         C.b48[i] = T.b48[i];
         C.b48_sh[i] = T.b48_sh[i];
+        C.mi64[i] = T.mi64[i];
         C.c128w_0[i] = T.c128w[(size_t)i * 4 + 0];
         C.c128w_1[i] = T.c128w[(size_t)i * 4 + 1];
         C.c128w_2[i] = T.c128w[(size_t)i * 4 + 2];
@@ -330,6 +343,7 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     }
     C.acc = T.acc;
     C.acc_lo = T.acc_lo;
+    C.m64 = T.m64;
     C.acc_hi = T.acc_hi;
     C.ref_factor = T.ref_factor;
     C.log2M = T.log2M;

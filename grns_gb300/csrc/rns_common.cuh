@@ -32,6 +32,8 @@ namespace grns {
 constexpr int kMaxModuli = 64;
 constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/params.h:22)
 constexpr int kDivB = 48;       // quotient bits per step of the integer division
+constexpr int kScaleB = 52;     // bits per step of the integer power-of-two scaling
+constexpr int kPow2NegRows = 64;  // rows j = 0..63 of the 2^-j mod m_i table
 
 /* levels of the pairwise summation tree over n leaves */
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c((n + 1) / 2); }
@@ -66,6 +68,9 @@ struct Consts {
      * (exact integers below 2^100) and ceil(RNS_EVAL_ACCURACY * 2^100) */
     uint64_t evl_lo[N], evl_hi[N], evu_lo[N], evu_hi[N];
     uint64_t acc_lo, acc_hi;
+    /* scaling: M_i mod 2^64, M mod 2^64 (binary low words of the CRT weights) */
+    uint64_t mi64[N];
+    uint64_t m64;
     /* one-ulp evaluation: ceil(2^128 w_i / m_i) mod 2^128, 32-bit words (w-folded) */
     uint32_t c128w_0[N], c128w_1[N], c128w_2[N], c128w_3[N];
     uint32_t t32[N], t32_sh[N];           // 2^32 mod m_i, Shoup companion
@@ -80,8 +85,8 @@ struct Consts {
     const uint32_t *m_pow2;     // [30]     M mod 2^(j+1)               (RNS_MODULI_PRODUCT_POW2_RESIDUES)
     const uint32_t *pow2_inv;   // [30 * N] (2^(j+1))^-1 mod m_i        (RNS_POW2_INVERSE)
     const uint32_t *pow2_inv_sh;// [30 * N]
-    const uint32_t *pow2neg;    // [(kDivB + 1) * N]  2^-j mod m_i
-    const uint32_t *pow2neg_sh; // [(kDivB + 1) * N]
+    const uint32_t *pow2neg;    // [kPow2NegRows * N]  2^-j mod m_i
+    const uint32_t *pow2neg_sh; // [kPow2NegRows * N]
 };
 
 /* ---------------- modular arithmetic ---------------- */

@@ -740,40 +740,43 @@ GRNS_HD uint32_t rank_fast(const Consts<N> &C, const uint32_t *x, const uint32_t
     return a[N - 1] == 0 ? kk : kk - 1;
 }
 
-/* one step of make_scaling_step (:181): y = (x - (X mod 2^j)) * (2^j)^-1 */
+/* One exact scaling step (the role of make_scaling_step, :181, with steps of
+ * up to kScaleB = 52 bits instead of RNS_P2_SCALING_THRESHOLD = 30):
+ * y = (x - (X mod 2^j)) 2^-j, with X mod 2^j = (sum_i c_i M_i - k M) mod 2^j
+ * computed in 64-bit wrap-around arithmetic (c_i = x_i w_i mod m_i, k the
+ * rank) and reduced once per modulus (X mod 2^j < 2^52). */
 template <int N>
-GRNS_HD void scaling_step_hd(const Consts<N> &C, uint32_t *y, uint32_t k, unsigned j, const uint32_t *x,
-                             const uint32_t *c) {
-    const uint32_t mask = (1u << j) - 1u;
-    const uint32_t *hrow = C.mi_pow2 + (int64_t)(j - 1) * N;
+GRNS_HD void scaling_step_big(const Consts<N> &C, uint32_t *y, uint32_t k, int j, const uint32_t *x,
+                              const uint32_t *c) {
     uint64_t acc = 0;
 #pragma unroll
-    for (int i = 0; i < N; i++) acc += (uint64_t)((ldg_u32(hrow + i) * c[i]) & mask);
-    uint32_t res = (uint32_t)((acc - (uint64_t)k * ldg_u32(C.m_pow2 + j - 1)) & mask);
-    const uint32_t *inv = C.pow2_inv + (int64_t)(j - 1) * N;
-    const uint32_t *inv_sh = C.pow2_inv_sh + (int64_t)(j - 1) * N;
+    for (int i = 0; i < N; i++) acc += (uint64_t)c[i] * C.mi64[i];
+    const uint64_t res = (acc - (uint64_t)k * C.m64) & ((((uint64_t)1) << j) - 1);
+    const uint32_t *inv = C.pow2neg + (int64_t)j * N, *inv_sh = C.pow2neg_sh + (int64_t)j * N;
 #pragma unroll
     for (int i = 0; i < N; i++) {
         const uint32_t m = C.m[i];
-        uint32_t rm = reduce32<N>(C, i, res);
-        y[i] = mulmod_shoup(submod(x[i], rm, m), ldg_u32(inv + i), ldg_u32(inv_sh + i), m);
+        y[i] = mulmod_shoup(submod(x[i], reduce53<N>(C, i, res), m), ldg_u32(inv + i), ldg_u32(inv_sh + i), m);
     }
 }
 
+/* floor(X / 2^D) (the result of rns_scale2pow, src/rnsscal.cuh:207): steps of
+ * kScaleB bits; the first step's rank is checked (X arbitrary), later ones
+ * act on X < M / 2 */
 template <int N>
 GRNS_HD void scale_fast(const Consts<N> &C, uint32_t *res, const uint32_t *x, unsigned D) {
     uint32_t cur[N], c[N];
 #pragma unroll
     for (int i = 0; i < N; i++) cur[i] = x[i];
-    unsigned t = D / kScaleStep, dr = D % kScaleStep;
     bool small = false;
 #pragma unroll 1
-    for (unsigned step = 0; step < t + (dr ? 1u : 0u); step++) {
-        const unsigned j = step < t ? (unsigned)kScaleStep : dr;
+    for (unsigned left = D; left > 0;) {
+        const int j = left < (unsigned)kScaleB ? (int)left : kScaleB;
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_shoup(cur[i], C.w[i], C.w_sh[i], C.m[i]);
-        uint32_t k = rank_fast<N>(C, cur, c, small);
-        scaling_step_hd<N>(C, cur, k, j, cur, c);
+        const uint32_t k = rank_fast<N>(C, cur, c, small);
+        scaling_step_big<N>(C, cur, k, j, cur, c);
+        left -= (unsigned)j;
         small = true;
     }
 #pragma unroll

@@ -257,3 +257,20 @@ def test_one_ulp_evaluation(fc, tag):
         rlo = er_fraction(ref[k]["low"]["frac"], ref[k]["low"]["exp"])
         rup = er_fraction(ref[k]["upp"]["frac"], ref[k]["upp"]["exp"])
         assert up - lo <= rup - rlo
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64"])
+def test_scaling_step_boundaries(fc, tag):
+    """exponents at and around multiples of the 52-bit step, the full range,
+    and dividends next to 0 and M (the first step's checked rank)"""
+    f = FC(fc, moduli_for(tag))
+    M = f.M
+    L = M.bit_length() - 1
+    rng = random.Random(11)
+    X, S = [], []
+    for D in sorted({1, 2, 51, 52, 53, 103, 104, 105, 156, 157, L - 1, L, L + 1}):
+        for x in [M - 1, M - 2, 0, 1, (1 << min(D, L)) - 1, 1 << min(D, L)] + [rng.randrange(M) for _ in range(6)]:
+            if 0 <= x < M:
+                X.append(x)
+                S.append(D)
+    assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
