@@ -392,16 +392,18 @@ __device__ __forceinline__ int dv_rec_steps(const uint2 &r) {
 constexpr int kDivBins = 64;  // > log2(M) / 48 + 1 for every supported moduli set
 
 /* order[begin + p] (p = 0..) = offsets of the range's numbers by decreasing
- * step count (a counting sort; hist: this warp's kDivBins shared counters),
- * so a warp's last divisions are its shortest and the drain is short */
-__device__ __forceinline__ void div_order(const uint2 *rec, int32_t *order, int64_t begin, int64_t end,
+ * step count steps_of(k) in [0, kDivBins) (a counting sort; hist: this warp's
+ * kDivBins shared counters), so a warp's last numbers are its cheapest and
+ * the drain at the end of the range is short */
+template <class StepsOf>
+__device__ __forceinline__ void lpt_order(StepsOf steps_of, int32_t *order, int64_t begin, int64_t end,
                                           uint32_t *hist) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     hist[lane] = 0;
     hist[lane + 32] = 0;
     __syncwarp();
-    for (int64_t e = begin + lane; e < end; e += 32) atomicAdd(&hist[dv_rec_steps(rec[e])], 1u);
+    for (int64_t e = begin + lane; e < end; e += 32) atomicAdd(&hist[steps_of(e)], 1u);
     __syncwarp();
     /* exclusive prefix over bins in decreasing order: lane l holds bins 63 - l and 31 - l */
     const uint32_t h0 = hist[63 - lane], h1 = hist[31 - lane];
@@ -420,10 +422,15 @@ __device__ __forceinline__ void div_order(const uint2 *rec, int32_t *order, int6
     hist[31 - lane] = s1 - h1;
     __syncwarp();
     for (int64_t e = begin + lane; e < end; e += 32) {
-        const uint32_t p = atomicAdd(&hist[dv_rec_steps(rec[e])], 1u);
+        const uint32_t p = atomicAdd(&hist[steps_of(e)], 1u);
         order[begin + p] = (int32_t)(e - begin);
     }
     __syncwarp();  // the order written by one lane is read by another
+}
+
+__device__ __forceinline__ void div_order(const uint2 *rec, int32_t *order, int64_t begin, int64_t end,
+                                          uint32_t *hist) {
+    lpt_order([&](int64_t e) { return dv_rec_steps(rec[e]); }, order, begin, end, hist);
 }
 
 /* both passes for one warp's range; rec / order hold one entry per number of

@@ -8,6 +8,7 @@
  *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
  */
 #include "div_warp.cuh"
+#include "scale_warp.cuh"
 #include "internal.h"
 #include "rns_device.cuh"
 #include "rns_fast.cuh"
@@ -68,6 +69,25 @@ __global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
     const int64_t e = b + per_warp < count ? b + per_warp : count;
     div_range<N>(K, C, x, d, rec, order, q, r, flags, b, e, cols + threadIdx.x, blockDim.x,
                  hist + (threadIdx.x / 32) * kDivBins);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kDivBlock, N > 32 ? 4 : 6)
+    k_scale_warp(const __grid_constant__ Consts<N> C, Operand<N> x, const uint32_t *__restrict__ D,
+                 uint32_t D_uniform, int32_t *__restrict__ order, int64_t count, int64_t per_warp, Output<N> out,
+                 uint8_t *__restrict__ flags) {
+    extern __shared__ uint4 scale_smem[];
+    ScK *K = reinterpret_cast<ScK *>(scale_smem);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(K + N);
+    uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
+    sck_fill<N>(C, K);
+    __syncthreads();
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t b = w * per_warp;
+    if (b >= count) return;  // whole warp
+    const int64_t e = b + per_warp < count ? b + per_warp : count;
+    scale_range<N>(K, C, x, D, D_uniform, out, flags, order, b, e, cols + threadIdx.x, blockDim.x,
+                   hist + (threadIdx.x / 32) * kDivBins);
 }
 
 template <int N, bool FAST>
@@ -142,13 +162,39 @@ template <int N>
 static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
                              int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s) {
     const int B = 128;
-    if (c->path == GRNS_PATH_REFERENCE)
+    if (c->path == GRNS_PATH_REFERENCE) {
         k_scale<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
                                                                  Output<N>{out, ld}, flags);
-    else
-        k_scale<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
-                                                                Output<N>{out, ld}, flags);
-    return cuda_status(cudaGetLastError());
+        return cuda_status(cudaGetLastError());
+    }
+    /* fast path: warps over contiguous ranges (scale_warp.cuh) */
+    const size_t smem = scale_smem_bytes<N>(kDivBlock);
+    static int per_sm[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident blocks per SM, per device
+    int &occ = per_sm[c->device & 7];
+    if (occ == 0) {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_scale_warp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scale_warp<N>, kDivBlock, smem) != cudaSuccess ||
+            nb < 1)
+            nb = 1;
+        occ = nb;
+    }
+    const int64_t warps_cap = (int64_t)c->sm_count * occ * (kDivBlock / 32);
+    int64_t warps = (count + 31) / 32;
+    if (warps > warps_cap) warps = warps_cap;
+    if (warps < 1) warps = 1;
+    const int64_t per_warp = (count + warps - 1) / warps;
+    const unsigned grid = (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
+    int32_t *order = nullptr;  // longest-first order scratch (per-number exponents only)
+    cudaError_t e = cudaSuccess;
+    if (D) e = cudaMallocAsync((void **)&order, (size_t)count * sizeof(int32_t), s);
+    if (e != cudaSuccess) return cuda_status(e);
+    k_scale_warp<N><<<grid, kDivBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, order, count,
+                                                  per_warp > 0 ? per_warp : 1, Output<N>{out, ld}, flags);
+    e = cudaGetLastError();
+    if (order) cudaFreeAsync(order, s);
+    return cuda_status(e);
 }
 
 grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,

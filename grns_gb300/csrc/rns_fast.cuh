@@ -769,6 +769,12 @@ GRNS_HD void scale_fast(const Consts<N> &C, uint32_t *res, const uint32_t *x, un
 #pragma unroll
     for (int i = 0; i < N; i++) cur[i] = x[i];
     bool small = false;
+    if (D > (unsigned)C.log2M) D = 0, small = true;  // X < M < 2^(log2M + 1): the result is 0
+    if (small) {
+#pragma unroll
+        for (int i = 0; i < N; i++) res[i] = 0;
+        return;
+    }
 #pragma unroll 1
     for (unsigned left = D; left > 0;) {
         const int j = left < (unsigned)kScaleB ? (int)left : kScaleB;
