@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "div_warp.cuh"
+#include "scale_warp.cuh"
 #include "internal.h"
 #include "rns_device.cuh"
 #include "rns_fast.cuh"
@@ -40,8 +41,8 @@ struct JobDev {
     void *out0, *out1;
     uint8_t *flags;
     const Er *eval_a, *eval_b;  // cmp: optional cached evaluations (2 Er per number)
-    uint2 *rec;                 // div: pass-A records (one per number)
-    int32_t *order;             // div: longest-first order (one per number)
+    uint2 *rec;                 // div: pass-A records (one per number; also reserved for scale jobs)
+    int32_t *order;             // div, scale with per-number exponents: longest-first order
     uint32_t D_uniform;
     int32_t coop;
     int64_t chunk_begin;   // first global chunk of this job
@@ -56,13 +57,15 @@ struct Part {  // max: best of one chunk
 };
 
 /* block shape per moduli count: 256 threads x 2 blocks per SM, or 128 x 2 at
- * n = 64; division jobs keep their residues in shared-memory columns
- * (div_warp.cuh), allocated only when the batch holds a division */
+ * n = 64; division and scaling jobs keep their residues in shared-memory
+ * columns (div_warp.cuh, scale_warp.cuh), allocated only when the batch holds
+ * one: [DivK table][ScK table][warps' counters][columns of 3n words] */
 template <int N>
 struct BatchCfg {
     static constexpr int kBlock = N > 32 ? 128 : 256;
     static constexpr int kMinBlocks = 2;
-    static constexpr size_t kDivSmem = div_smem_bytes<N>(kBlock);
+    static constexpr size_t kTables = (sizeof(DivK) + sizeof(ScK)) * N;
+    static constexpr size_t kHeavySmem = kTables + (size_t)(kBlock / 32) * kDivBins * 4 + (size_t)3 * N * 4 * kBlock;
 };
 
 __device__ __forceinline__ int find_job(const JobDev *jobs, int njobs, int64_t c) {
@@ -197,34 +200,21 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
             break;
         case GRNS_OP_DIV:
         {
-            uint32_t *hist = smem + sizeof(DivK) / 4 * N;
+            uint32_t *hist = smem + BatchCfg<N>::kTables / 4;
             uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
             div_range<N>(reinterpret_cast<const DivK *>(smem), C, x, y, J.rec, J.order,
                          Output<N>{(uint32_t *)J.out0, ld}, Output<N>{(uint32_t *)J.out1, ld}, J.flags, start, end,
                          cols + threadIdx.x, blockDim.x, hist + (threadIdx.x / 32) * kDivBins);
         }
             break;
-        case GRNS_OP_SCALE2POW:
-            for (int64_t k = start + lane; k < end; k += 32) {
-                uint32_t xa[N], r0[N], f = 0;
-#pragma unroll
-                for (int i = 0; i < N; i++) {
-                    xa[i] = x.load(k, i);
-                    f |= xa[i] >= C.m[i] ? kFlagInvalidInput : 0u;
-                }
-                const unsigned D = J.b ? __ldg(J.b + k) : J.D_uniform;
-                if (f) {
-#pragma unroll
-                    for (int i = 0; i < N; i++) r0[i] = 0;
-                } else {
-                    scale_fast<N>(C, r0, xa, D);
-                }
-                const Output<N> o{(uint32_t *)J.out0, ld};
-#pragma unroll
-                for (int i = 0; i < N; i++) o.store(k, i, r0[i]);
-                if (J.flags) J.flags[k] = (uint8_t)f;
-            }
+        case GRNS_OP_SCALE2POW: {
+            uint32_t *hist = smem + BatchCfg<N>::kTables / 4;
+            uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
+            scale_range<N>(reinterpret_cast<const ScK *>(smem + sizeof(DivK) / 4 * N), C, x, J.b, J.D_uniform,
+                           Output<N>{(uint32_t *)J.out0, ld}, J.flags, J.b ? J.order : nullptr, start, end,
+                           cols + threadIdx.x, blockDim.x, hist + (threadIdx.x / 32) * kDivBins);
             break;
+        }
         case GRNS_OP_MAX: {
             Part best{0, -1};
             if (J.coop) {
@@ -292,8 +282,9 @@ __global__ void __launch_bounds__(BatchCfg<N>::kBlock, BatchCfg<N>::kMinBlocks) 
                                                           unsigned *done, Part *partials, int has_div) {
     extern __shared__ uint4 batch_smem4[];
     uint32_t *batch_smem = reinterpret_cast<uint32_t *>(batch_smem4);
-    if (has_div) {  // the division constants (DivK table) for every block
+    if (has_div) {  // division and scaling constants for every block
         divk_fill<N>(C, reinterpret_cast<DivK *>(batch_smem));
+        sck_fill<N>(C, reinterpret_cast<ScK *>(batch_smem + sizeof(DivK) / 4 * N));
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;
@@ -386,8 +377,8 @@ grns_status enqueue(grns_batch *b, cudaStream_t s) {
 
 template <int N>
 int occupancy_blocks(size_t smem) {
-    if (BatchCfg<N>::kDivSmem > 48 * 1024)  // per device: set on every shape computation
-        cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BatchCfg<N>::kDivSmem);
+    if (BatchCfg<N>::kHeavySmem > 48 * 1024)  // per device: set on every shape computation
+        cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BatchCfg<N>::kHeavySmem);
     int nb = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, BatchCfg<N>::kBlock, smem);
     return nb > 0 ? nb : 1;
@@ -396,10 +387,11 @@ int occupancy_blocks(size_t smem) {
 /* launch shape of a batch: grid (SMs x resident blocks) and shared memory */
 void batch_shape(grns_batch *b) {
     bool has_div = false;
-    for (const JobDev &J : b->host_jobs) has_div |= J.op == GRNS_OP_DIV && J.count > 0;
+    for (const JobDev &J : b->host_jobs)
+        has_div |= (J.op == GRNS_OP_DIV || J.op == GRNS_OP_SCALE2POW) && J.count > 0;
     int per_sm = 1;
 #define C_(n)                                                  \
-    b->smem = has_div ? BatchCfg<n>::kDivSmem : 0;             \
+    b->smem = has_div ? BatchCfg<n>::kHeavySmem : 0;           \
     per_sm = occupancy_blocks<n>(b->smem);                     \
     break
     switch (b->ctx->n) {
@@ -436,7 +428,7 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
         J.D_uniform = u.D_uniform;
         J.rec = nullptr;
         J.order = nullptr;
-        if (u.op == GRNS_OP_DIV) {
+        if (u.op == GRNS_OP_DIV || (u.op == GRNS_OP_SCALE2POW && u.b)) {
             J.rec = b->d_rec ? b->d_rec + recs : nullptr;
             recs += u.count;
         }
@@ -459,7 +451,7 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
         int32_t *ord = (int32_t *)(b->d_rec + recs);
         for (int t = 0; t < b->njobs; t++) {
             JobDev &J = b->host_jobs[t];
-            if (J.op == GRNS_OP_DIV) J.order = ord + (J.rec - b->d_rec);
+            if (J.rec) J.order = ord + (J.rec - b->d_rec);
         }
     }
     b->empty_max_index.clear();

@@ -30,7 +30,7 @@ struct grns_ctx {
     grns::HostTables T;  // host copies of all tables
     void *d_tables = nullptr;  // one device allocation holding the table blob
     /* batched-kernel schedule per grns_op (eval, cmp, div, scale2pow, max, mp_int add/sub/mul) */
-    grns::Sched sched[8] = {{0, 256}, {0, 1024}, {0, 256}, {0, 64}, {0, 1024}, {0, 256}, {0, 256}, {0, 256}};
+    grns::Sched sched[8] = {{0, 256}, {0, 1024}, {0, 256}, {0, 256}, {0, 1024}, {0, 256}, {0, 256}, {0, 256}};
     /* kernel constant block for this n (a grns::Consts<n>) */
     alignas(16) unsigned char consts[sizeof(grns::Consts<grns::kMaxModuli>)];
 };

@@ -144,7 +144,7 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
         case GRNS_OP_EVAL: return sizeof(interval_t) * k;
         case GRNS_OP_CMP: return 4 * (size_t)k;
         case GRNS_OP_DIV: return (2 * 4 * (size_t)n + 12) * k;
-        case GRNS_OP_SCALE2POW: return (4 * (size_t)n + 4) * k;
+        case GRNS_OP_SCALE2POW: return (4 * (size_t)n + 12) * k;
         case GRNS_OP_MAX: return ((4 * (size_t)n + 7) / 8) * 8 + 8;
         default: return GRNS_MPINT_BYTES(n) * (size_t)k;
     }

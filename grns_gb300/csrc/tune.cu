@@ -79,10 +79,10 @@ grns_status grns_autotune(grns_ctx *c, int op, int64_t count, const char *cache_
     job.out1 = (op == GRNS_OP_DIV || op == GRNS_OP_MAX) ? o1.p : nullptr;
 
     std::vector<grns::Sched> cands;
-    /* division chunks are refilled lane by lane inside a warp, so longer
-     * chunks trade tail length against balance; scaling runs one number per
-     * lane; the memory-bound ops want long chunks */
-    const int chunks_cheap[] = {256, 1024, 4096}, chunks_div[] = {64, 256, 1024}, chunks_scale[] = {32, 64, 128};
+    /* division and scaling chunks are refilled lane by lane inside a warp,
+     * so longer chunks trade tail length against balance; the memory-bound
+     * ops want long chunks */
+    const int chunks_cheap[] = {256, 1024, 4096}, chunks_div[] = {64, 256, 1024}, chunks_scale[] = {64, 256, 1024};
     const int *chunks = op == GRNS_OP_DIV ? chunks_div : op == GRNS_OP_SCALE2POW ? chunks_scale : chunks_cheap;
     for (int coop = 0; coop <= ((op == GRNS_OP_CMP || op == GRNS_OP_MAX) ? 1 : 0); coop++)
         for (int t = 0; t < 3; t++) cands.push_back(grns::Sched{coop, chunks[t]});
