@@ -50,6 +50,7 @@ SERVE_BUDGET = 48 << 30     # server HBM budget for outputs
 SERVE_LOADS = (0.5, 0.9)    # offered load as a fraction of the all-at-once throughput
 DMAX = 900
 SEED = 20260101
+WARMUP_SECONDS = 0.25       # minimum warm-up time before the timed steps
 
 
 def load_peaks():
@@ -669,12 +670,16 @@ def main():
         native.check(L.grns_scale2pow(ctx.handle, P(xs), P(D), 0, PAIRS, 0, P(so), None, sp))
         if e2: e2.record(stream)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-
     step_ms, div_ms, scale_ms = [], [], []
     with Clocks(local) as clk:
+        # warm-up: at least W steps and at least WARMUP_SECONDS, so the timed steps start
+        # after the clock sampler has started and the GPU has settled
+        t0 = time.perf_counter()
+        done = 0
+        while done < args.warmup or time.perf_counter() - t0 < WARMUP_SECONDS:
+            step()
+            torch.cuda.synchronize()
+            done += 1
         for _ in range(args.steps):
             flush.zero_()
             t = (_ev(), _ev(), _ev())
@@ -737,7 +742,9 @@ def main():
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                      "note": "division is integer-pipe bound (48-bit digit steps); the HBM-bound kernels "
                              "(eval, cmp, max, mp_int) carry their own fractions in extra"},
-        "kernels_ms": {"k_div_warp": div_avg, "k_scale": statistics.mean(scale_ms)},
+        "kernels_ms": {"k_div_warp": div_avg, "k_scale": statistics.mean(scale_ms),
+                       "k_div_warp_steps": [round(v, 4) for v in div_ms],
+                       "k_scale_steps": [round(v, 4) for v in scale_ms]},
         "e2e": {"value": e2e, "unit": "Mnum/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 2 * args.steps,
         "extra": extra,
