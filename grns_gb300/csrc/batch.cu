@@ -469,7 +469,7 @@ namespace grns {
 /* One-shot batch for the server: everything stream-ordered on `s`.  The
  * device job table is staged through `staging` (pinned, at least
  * batch_staging_bytes(njobs) bytes, not reused until the launch completes),
- * allocated with cudaMallocAsync and freed with cudaFreeAsync after the
+ * allocated from the context's stream-ordered pool and freed after the
  * kernel, so nothing here synchronises with other streams. */
 size_t batch_staging_bytes(int njobs) { return sizeof(JobDev) * (size_t)(njobs > 0 ? njobs : 1); }
 
@@ -487,14 +487,14 @@ grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *
     b.counters_bytes = sizeof(unsigned long long) + sizeof(unsigned) * (size_t)(njobs > 0 ? njobs : 1);
     cudaError_t e = cudaSuccess;
     if (b.nrec) {
-        e = cudaMallocAsync((void **)&b.d_rec, kDivScratchPerNumber * b.nrec, s);
+        e = scratch_alloc(c, (void **)&b.d_rec, kDivScratchPerNumber * b.nrec, s);
         if (e != cudaSuccess) return cuda_status(e);
         fill_jobs(&b, jobs);
     }
     std::memcpy(staging, b.host_jobs.data(), sizeof(JobDev) * njobs);
-    e = cudaMallocAsync((void **)&b.d_counter, b.counters_bytes, s);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&b.d_jobs, sizeof(JobDev) * (njobs > 0 ? njobs : 1), s);
-    if (e == cudaSuccess && b.nparts) e = cudaMallocAsync((void **)&b.d_parts, sizeof(Part) * b.nparts, s);
+    e = scratch_alloc(c, (void **)&b.d_counter, b.counters_bytes, s);
+    if (e == cudaSuccess) e = scratch_alloc(c, (void **)&b.d_jobs, sizeof(JobDev) * (njobs > 0 ? njobs : 1), s);
+    if (e == cudaSuccess && b.nparts) e = scratch_alloc(c, (void **)&b.d_parts, sizeof(Part) * b.nparts, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b.d_jobs, staging, sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, s);
     grns_status st = cuda_status(e);
     if (st == GRNS_OK) {

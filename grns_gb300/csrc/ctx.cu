@@ -93,6 +93,19 @@ grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out) {
         delete c;
         return grns::cuda_status(e);
     }
+    {  // scratch pool; without one, calls use the device's default pool
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = c->device;
+        if (cudaMemPoolCreate(&c->pool, &props) == cudaSuccess) {
+            uint64_t keep = grns::kPoolKeepBytes;
+            cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        } else {
+            c->pool = nullptr;
+            cudaGetLastError();
+        }
+    }
     grns_status st = build(c, mods.data());
     if (st != GRNS_OK) {
         grns_ctx_destroy(c);
@@ -105,6 +118,7 @@ grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out) {
 grns_status grns_ctx_destroy(grns_ctx *c) {
     if (!c) return GRNS_ERR_INVALID_ARGUMENT;
     if (c->d_tables) cudaFree(c->d_tables);
+    if (c->pool) cudaMemPoolDestroy(c->pool);  // released once outstanding scratch is freed
     delete c;
     return GRNS_OK;
 }

@@ -29,6 +29,10 @@ struct grns_ctx {
     int path = 0;  // 0: integer fast path, 1: reference-faithful FP64 kernels (GRNS_PATH_*)
     grns::HostTables T;  // host copies of all tables
     void *d_tables = nullptr;  // one device allocation holding the table blob
+    /* stream-ordered pool for per-call scratch (division records, scaling and
+     * batch orders, max partials); keeps up to kPoolKeepBytes across
+     * synchronisations so repeated calls do not map fresh memory */
+    cudaMemPool_t pool = nullptr;
     /* batched-kernel schedule per grns_op (eval, cmp, div, scale2pow, max, mp_int add/sub/mul) */
     grns::Sched sched[8] = {{0, 256}, {0, 1024}, {0, 256}, {0, 256}, {0, 1024}, {0, 256}, {0, 256}, {0, 256}};
     /* kernel constant block for this n (a grns::Consts<n>) */
@@ -41,6 +45,14 @@ template <int N>
 inline const Consts<N> &consts_of(const grns_ctx *c) {
     return *reinterpret_cast<const Consts<N> *>(c->consts);
 }
+
+constexpr uint64_t kPoolKeepBytes = 256ull << 20;
+
+/* scratch from the context's pool (the device's default pool if it has none) */
+inline cudaError_t scratch_alloc(const grns_ctx *c, void **p, size_t bytes, cudaStream_t s) {
+    return c->pool ? cudaMallocFromPoolAsync(p, bytes, c->pool, s) : cudaMallocAsync(p, bytes, s);
+}
+inline cudaError_t scratch_free(void *p, cudaStream_t s) { return cudaFreeAsync(p, s); }
 
 inline grns_status cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return GRNS_OK;

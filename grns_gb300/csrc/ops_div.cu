@@ -146,7 +146,7 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
     const unsigned grid = (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
     /* pass-A records and the longest-first order (12 bytes per number), stream-ordered */
     void *scratch = nullptr;
-    cudaError_t e = cudaMallocAsync(&scratch, (size_t)count * kDivScratchPerNumber, s);
+    cudaError_t e = scratch_alloc(c, &scratch, (size_t)count * kDivScratchPerNumber, s);
     if (e != cudaSuccess) return cuda_status(e);
     uint2 *rec = (uint2 *)scratch;
     int32_t *order = (int32_t *)(rec + count);
@@ -154,7 +154,7 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
                                                 count, per_warp > 0 ? per_warp : 1, Output<N>{q, ld},
                                                 Output<N>{r, ld}, flags);
     e = cudaGetLastError();
-    cudaFreeAsync(scratch, s);
+    scratch_free(scratch, s);
     return cuda_status(e);
 }
 
@@ -188,12 +188,12 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
     const unsigned grid = (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
     int32_t *order = nullptr;  // longest-first order scratch (per-number exponents only)
     cudaError_t e = cudaSuccess;
-    if (D) e = cudaMallocAsync((void **)&order, (size_t)count * sizeof(int32_t), s);
+    if (D) e = scratch_alloc(c, (void **)&order, (size_t)count * sizeof(int32_t), s);
     if (e != cudaSuccess) return cuda_status(e);
     k_scale_warp<N><<<grid, kDivBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, order, count,
                                                   per_warp > 0 ? per_warp : 1, Output<N>{out, ld}, flags);
     e = cudaGetLastError();
-    if (order) cudaFreeAsync(order, s);
+    if (order) scratch_free(order, s);
     return cuda_status(e);
 }
 

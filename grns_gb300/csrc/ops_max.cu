@@ -250,7 +250,7 @@ grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count
     }
     bool owned = false;
     if (!scratch) {  /* stream-ordered allocation: safe for concurrent calls on different streams */
-        cudaError_t e = cudaMallocAsync(&scratch, max_scratch_bytes(c, count), s);
+        cudaError_t e = scratch_alloc(c, &scratch, max_scratch_bytes(c, count), s);
         if (e != cudaSuccess) return cuda_status(e);
         owned = true;
     }
@@ -267,7 +267,7 @@ grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count
     }
 #undef C_
     if (owned) {
-        cudaError_t e = cudaFreeAsync(scratch, s);
+        cudaError_t e = scratch_free(scratch, s);
         if (st == GRNS_OK && e != cudaSuccess) st = cuda_status(e);
     }
     return st;
