@@ -480,6 +480,27 @@ static int OFN(mpint_mul)(const or_ctx *c, OFN(or_mpint) *res, const OFN(or_mpin
     return or_overflow(c, &res->eval[0], &res->eval[1]);
 }
 
+/* mpint_div (Euclidean quotient): host src/mpint.cuh:286 (rns_div_fast + host
+ * evaluation), device :511 (cuda::rns_div + device evaluation).  A negative
+ * dividend with a nonzero remainder takes |q| + 1, so x = q*y + r, 0 <= r < |y|;
+ * the reference checks no overflow here. */
+static int OFN(mpint_div)(const or_ctx *c, OFN(or_mpint) *res, const OFN(or_mpint) *x, const OFN(or_mpint) *y, int dev) {
+    int q[ON], r[ON], rz = 1, qz = 1;
+    if (dev) OFN(div_d)(c, q, r, x->digits, y->digits, 0);
+    else OFN(div_h)(c, q, r, x->digits, y->digits, 1);
+    for (int i = 0; i < ON; i++) rz &= r[i] == 0;
+    if (x->sign == 1 && !rz)
+        for (int i = 0; i < ON; i++) q[i] = (q[i] + 1) % c->m[i];
+    or_iv ev;
+    if (dev) OFN(eval_d)(c, &ev, q);
+    else OFN(eval_h)(c, &ev, q);
+    for (int i = 0; i < ON; i++) { res->digits[i] = q[i]; qz &= q[i] == 0; }
+    res->eval[0] = ev.low;
+    res->eval[1] = ev.upp;
+    res->sign = qz ? 0 : (x->sign ^ y->sign);
+    return 0;
+}
+
 /* ---------------- batch drivers (AoS arrays, reference layout) ---------------- */
 static void OFN(batch_eval)(const or_ctx *c, const int *x, long N, or_iv *out, int path, int threads) {
     #pragma omp parallel for schedule(dynamic, 256) num_threads(threads) if (threads > 1)
@@ -511,15 +532,17 @@ static void OFN(batch_mrc)(const or_ctx *c, const int *x, long N, int *mr, int p
         else OFN(mrc_h)(c, mr + k * ON, x + k * ON);
     }
 }
-/* op: 0 add, 1 sub, 2 mul; flags (optional) receives the overflow status per element */
+/* op: 0 add, 1 sub, 2 mul, 3 div; flags (optional) receives the overflow status per element */
 static void OFN(batch_mpint)(const or_ctx *c, int op, const void *xs, const void *ys, long N, void *outs, int *flags, int path, int threads) {
     const OFN(or_mpint) *x = (const OFN(or_mpint) *)xs, *y = (const OFN(or_mpint) *)ys;
     OFN(or_mpint) *o = (OFN(or_mpint) *)outs;
-    #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
+    #pragma omp parallel for schedule(dynamic, 16) num_threads(threads) if (threads > 1)
     for (long k = 0; k < N; k++) {
         OFN(or_mpint) r;
         memset(&r, 0, sizeof(r));
-        int f = op == 2 ? OFN(mpint_mul)(c, &r, x + k, y + k, path) : OFN(mpint_addsub)(c, &r, x + k, y + k, op, path);
+        int f = op == 3   ? OFN(mpint_div)(c, &r, x + k, y + k, path)
+                : op == 2 ? OFN(mpint_mul)(c, &r, x + k, y + k, path)
+                          : OFN(mpint_addsub)(c, &r, x + k, y + k, op, path);
         o[k] = r;
         if (flags) flags[k] = f;
     }

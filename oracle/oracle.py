@@ -157,8 +157,8 @@ class Oracle:
         return out
 
     def mpint(self, op, x, y, path=PATH_DEVICE, threads=1):
-        """op: 'add' | 'sub' | 'mul'; x, y arrays of mpint_dtype(n). Returns (out, overflow_flags)."""
-        code = {"add": 0, "sub": 1, "mul": 2}[op]
+        """op: 'add' | 'sub' | 'mul' | 'div'; x, y arrays of mpint_dtype(n). Returns (out, overflow_flags)."""
+        code = {"add": 0, "sub": 1, "mul": 2, "div": 3}[op]
         x = np.ascontiguousarray(x)
         y = np.ascontiguousarray(y)
         out = np.zeros(x.shape[0], mpint_dtype(self.n))

@@ -8,7 +8,8 @@ exact directed-rounding emulation).  Special values follow the reference's
 own verification programs: consecutive numbers from 0 and from M-1
 (tests/test_verify_rnseval.cu:87-149, tests/test_verify_mrc.cu:128-152),
 powers of two 2^0..2^LOG2 (tests/test_perf_rnseval.cu:679-688), the mp_int
-known-answer pair x=-55, y=13 (tests/test_verify_mpint.cu:92-93) and the
+known-answer pair x=-55, y=13 (tests/test_verify_mpint.cu:92-93), signed
+mp_int division operands with the Euclidean sign cases, and the
 extended-range doubles of tests/test_verify_extrange.cu:115-117.
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -100,6 +101,24 @@ def main():
             for path, dev in (("dev", True), ("host", False)):
                 fx[f"mpint_{op}_{path}"] = ref.mpint(op, ma.view(dt), mb.view(dt), dev=dev).view(np.uint8)
         fx["mpint_kat"] = np.concatenate([ref.mpint_set_i(-55).view(np.uint8), ref.mpint_set_i(13).view(np.uint8)])
+        # mpint_div (src/mpint.cuh:286/:511): signed dividends over the whole range,
+        # nonzero divisors of random bit lengths, and the Euclidean sign cases
+        rd = random.Random(20261203 + n)
+        DA, DB = [], []
+        for _ in range(nrand + 16):
+            DA.append(rd.choice((-1, 1)) * rd.randrange(M))
+            b = rd.randrange(1, L + 1)
+            DB.append(rd.choice((-1, 1)) * rd.randrange(1 << (b - 1), 1 << b))
+        for a, b in ((-55, 13), (55, -13), (-55, -13), (0, 7), (0, -7), (-52, 13), (52, -13), (M - 1, 1),
+                     (-(M - 1), 1), (-(M - 2), M - 1), (M - 2, -(M - 1)), (-(M - 2), 2), (12345, 12345),
+                     (-12344, 12345), (12344, -12345), (-(M - 1), -(M // 2))):
+            DA.append(a)
+            DB.append(b)
+        da = np.concatenate([ref.mpint_from_str(v).view(np.uint8) for v in DA])
+        db = np.concatenate([ref.mpint_from_str(v).view(np.uint8) for v in DB])
+        fx["mpdiv_a"], fx["mpdiv_b"] = da, db
+        for path, dev in (("dev", True), ("host", False)):
+            fx[f"mpint_div_{path}"] = ref.mpint("div", da.view(dt), db.view(dt), dev=dev).view(np.uint8)
         # extended-range known answers (tests/test_verify_extrange.cu:115-117)
         if tag == "ref8":
             dvals = [0.00003687544343, 0.41352, 12345.1443575]

@@ -62,6 +62,31 @@ def test_mpint_matches_golden(case, path, code, op):
     assert out.view(np.uint8).tobytes() == g[f"mpint_{op}_{path}"].tobytes()
 
 
+@pytest.mark.parametrize("path,code", PATHS)
+def test_mpint_div_matches_golden(case, path, code):
+    """mpint_div, host src/mpint.cuh:286 and device :511"""
+    tag, orc, g = case
+    dt = mpint_dtype(orc.n)
+    out, _ = orc.mpint("div", g["mpdiv_a"].view(dt), g["mpdiv_b"].view(dt), path=code)
+    assert out.view(np.uint8).tobytes() == g[f"mpint_div_{path}"].tobytes()
+
+
+def test_mpint_div_euclidean(case):
+    """x = q*y + r with 0 <= r < |y| for every golden pair"""
+    tag, orc, g = case
+    dt = mpint_dtype(orc.n)
+    a, b = g["mpdiv_a"].view(dt), g["mpdiv_b"].view(dt)
+    out, _ = orc.mpint("div", a, b, path=O.PATH_DEVICE)
+    ex = orc.exact
+    signed = lambda m: [(-v if s else v) for v, s in zip(ex.from_rns(m["digits"]), m["sign"])]  # noqa: E731
+    X, Y, Q = signed(a), signed(b), signed(out)
+    for x, y, q in zip(X, Y, Q):
+        r = x - q * y
+        assert 0 <= r < abs(y), (x, y, q)
+    ivs = [{"low": e[0], "upp": e[1]} for e in out["eval"]]
+    assert ex.encloses(ivs, ex.from_rns(out["digits"])).all()
+
+
 def test_mpint_known_answer(case):
     """x = -55, y = 13 (reference tests/test_verify_mpint.cu:92-93)"""
     tag, orc, g = case
