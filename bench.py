@@ -196,7 +196,8 @@ def run_only(args):
     from grns_gb300 import native
     from grns_gb300.workload import S_X, S_Y
     L = native.lib(build_if_missing=True)
-    n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32, "mpint64": 64}[args.only]
+    n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32, "mpint64": 64,
+         "mpdiv32": 32}[args.only]
     ctx = G.RNSContext(greedy(n))
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -215,11 +216,13 @@ def run_only(args):
     val = torch.empty(n, dtype=torch.int32, device="cuda")
     idx = torch.empty(1, dtype=torch.int64, device="cuda")
     mb = G.mpint_bytes(n)
-    if args.only == "mpint64":
-        from grns_gb300.workload import mpint_values  # operands: residues of random ints below 2^950
+    if args.only in ("mpint64", "mpdiv32"):
         ma = torch.zeros(cnt * mb, dtype=torch.uint8, device="cuda")
         mc = torch.zeros_like(ma)
         mo = torch.zeros_like(ma)
+    if args.only == "mpdiv32":  # signed dividends below 2^900, divisors below 2^450
+        native.check(L.grns_gen_mpint(ctx.handle, SEED, cnt, 900, P(ma), sp))
+        native.check(L.grns_gen_mpint(ctx.handle, SEED + 1, cnt, 450, P(mc), sp))
     def call():
         if args.only == "div":
             native.check(L.grns_div(ctx.handle, P(x), P(y), cnt, 0, P(a), P(b), None, sp))
@@ -235,6 +238,8 @@ def run_only(args):
             native.check(L.grns_eval_tight(ctx.handle, P(x), cnt, 0, P(out), None, sp))
         elif args.only == "mpint64":
             native.check(L.grns_mpint_mul(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
+        elif args.only == "mpdiv32":
+            native.check(L.grns_mpint_div(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
 
     for _ in range(args.warmup):
         call()
@@ -618,7 +623,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
-    ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "evtight32", "mpint64"], default=None,
+    ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "evtight32", "mpint64",
+                                           "mpdiv32"], default=None,
                     help="profiling: run just this op --warmup + --steps times on --pairs numbers, no JSON line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.only is None else args.warmup

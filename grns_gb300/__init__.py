@@ -9,7 +9,8 @@ whole device arrays through the C ABI of libgrns_gb300.so.
     s   = ctx.rns_cmp(x, y)                   # cuda::rns_cmp           (src/rnscmp.cuh:55)
     q,r = ctx.rns_div(x, d)                   # cuda::rns_div           (src/rnsdiv.cuh:128)
     z   = ctx.rns_scale2pow(x, D)             # cuda::rns_scale2pow     (src/rnsscal.cuh:207)
-    z   = ctx.mpint_add(a, b) / mpint_sub / mpint_mul   (src/mpint.cuh:336/:407/:478)
+    z   = ctx.mpint_add(a, b) / mpint_sub / mpint_mul / mpint_div
+                                              (src/mpint.cuh:336/:407/:478/:511)
     v,i = ctx.rns_max(x)                      # cuda::rns_max           (src/dpp/rnsmax.cuh:129)
 
 RNS arrays are int32 CUDA tensors: layout "soa" is shape (n, count) (residue
@@ -208,6 +209,10 @@ class RNSContext:
 
     def mpint_mul(self, x, y, flags=None, stream=None):
         return self._mpint(native.lib().grns_mpint_mul, x, y, flags, stream)
+
+    def mpint_div(self, x, y, flags=None, stream=None):
+        """Euclidean quotient x / y (cuda::mpint_div, src/mpint.cuh:511)."""
+        return self._mpint(native.lib().grns_mpint_div, x, y, flags, stream)
 
     def rns_max(self, x, layout="soa", scratch=None, stream=None):
         """returns (value residues int32[n], index int64[1]) on the device"""

@@ -77,6 +77,10 @@ grns_status grns_mpint_mul(grns_ctx *c, const void *x, const void *y, int64_t co
                            void *stream) {
     return mpint_op(c, 2, x, y, count, out, flags, stream);
 }
+grns_status grns_mpint_div(grns_ctx *c, const void *x, const void *y, int64_t count, void *out, uint8_t *flags,
+                           void *stream) {
+    return mpint_op(c, 3, x, y, count, out, flags, stream);
+}
 
 grns_status grns_max_scratch_size(const grns_ctx *c, int64_t count, size_t *bytes) {
     if (!c || !bytes || count < 0) return GRNS_ERR_INVALID_ARGUMENT;

@@ -146,6 +146,16 @@ grns_status grns_mpint_sub(grns_ctx *ctx, const void *x, const void *y, int64_t 
                            uint8_t *flags, void *stream);
 grns_status grns_mpint_mul(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
                            uint8_t *flags, void *stream);
+/* result = x / y with the Euclidean quotient, as cuda::mpint_div (reference
+ * src/mpint.cuh:511; host mpint_div :286 returns the same digits): q = |x| div
+ * |y|, plus one when x < 0 and the remainder is nonzero, so that x = q*y + r
+ * with 0 <= r < |y|; sign x.sign ^ y.sign (0 for a zero quotient); the
+ * evaluation is rns_eval_compute's of the quotient, bit for bit.  y = 0 sets
+ * GRNS_FLAG_DIV_BY_ZERO and yields the zero record.  Runs the division of
+ * grns_div on residue-major scratch of 16 * n bytes per element from the
+ * context's pool; `out` must not overlap x or y. */
+grns_status grns_mpint_div(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
+                           uint8_t *flags, void *stream);
 
 /* ---- maximum of an RNS array ----
  * Replaces template cuda::rns_max<g1,b1,g2,b2>(out, in, N, buffer)

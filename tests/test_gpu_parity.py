@@ -197,6 +197,66 @@ def test_mpint(case, op):
     assert [(-v if s else v) for v, s in zip(mags, got["sign"])] == [exact(p, q) for p, q in zip(vals_a, vals_b)]
 
 
+def _signed(orc, m):
+    return [(-v if s else v) for v, s in zip(orc.exact.from_rns(m["digits"]), m["sign"])]
+
+
+def _mpint_div_check(ctx, orc, a, b, got, want):
+    """digits and sign as the oracle's cuda::mpint_div; the evaluation bit for
+    bit as the device evaluation of the quotient (device ceil(log2))"""
+    assert got["digits"].tobytes() == want["digits"].tobytes()
+    assert np.array_equal(got["sign"], want["sign"])
+    ev = oracle_eval_device(ctx, orc, got["digits"])
+    assert got["eval"].tobytes() == np.stack([ev["low"], ev["upp"]], axis=1).tobytes()
+    for x, y, q in zip(_signed(orc, a), _signed(orc, b), _signed(orc, got)):
+        assert 0 <= x - q * y < abs(y), (x, y, q)
+
+
+def test_mpint_div(case, path):
+    """Euclidean mp_int division, cuda::mpint_div (src/mpint.cuh:511)"""
+    tag, ctx, orc, g = case
+    dt = mpint_dtype(orc.n)
+    a, b = g["mpdiv_a"].view(dt), g["mpdiv_b"].view(dt)
+    flags = flags_buf(len(a))
+    out = ctx.mpint_div(torch.from_numpy(g["mpdiv_a"]).cuda(), torch.from_numpy(g["mpdiv_b"]).cuda(), flags=flags)
+    got = out.cpu().numpy().view(dt)
+    want = g["mpint_div_dev"].view(dt)
+    assert int(flags.sum()) == 0
+    _mpint_div_check(ctx, orc, a, b, got, want)
+    xs = orc.log2_inputs(got["digits"])
+    if len(xs) == 0 or np.array_equal(ctx.device_ceil_log2(xs), np.ceil(np.log2(xs)).astype(np.int32)):
+        assert got.tobytes() == want.tobytes()
+    # fresh operands: signed dividends over the whole range, nonzero divisors of
+    # random bit lengths, quotients from 0 to M - 1
+    rng = random.Random(31)
+    N = 1500 if orc.n <= 16 else 400
+    va = [rng.choice((-1, 1)) * rng.randrange(orc.M) for _ in range(N)]
+    vb = []
+    for _ in range(N):
+        bits = rng.randrange(1, orc.log2M + 1)
+        vb.append(rng.choice((-1, 1)) * rng.randrange(1 << (bits - 1), 1 << bits))
+    vb[:4] = [1, -1, 2, orc.M - 1]
+    ma, mb = orc.mpint_from_ints(va), orc.mpint_from_ints(vb)
+    out = ctx.mpint_div(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda())
+    got = out.cpu().numpy().view(dt)
+    want, _ = orc.mpint("div", ma, mb, path=O.PATH_DEVICE, threads=8)
+    _mpint_div_check(ctx, orc, ma, mb, got, want)
+
+
+def test_mpint_div_by_zero(case):
+    tag, ctx, orc, g = case
+    ma, mb = orc.mpint_from_ints([-77, 77, 5]), orc.mpint_from_ints([0, 0, 3])
+    flags = flags_buf(3)
+    out = ctx.mpint_div(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda(),
+                        flags=flags)
+    got = out.cpu().numpy().view(mpint_dtype(orc.n))
+    f = flags.cpu().numpy()
+    assert list(f) == [2, 2, 0]
+    assert not got["digits"][:2].any() and not got["sign"][:2].any()
+    assert not got["eval"]["frac"][:2].any()
+    assert _signed(orc, got[2:]) == [1]
+
+
 def test_mpint_overflow_flag(case):
     tag, ctx, orc, g = case
     big = orc.M // 2 + 12345
