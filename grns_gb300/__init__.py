@@ -5,6 +5,7 @@ Python mirror of the reference library's interface for this path
 whole device arrays through the C ABI of libgrns_gb300.so.
 
     ctx = RNSContext(moduli)                  # rns_const_init() + mpint_const_init()
+    ctx = RNSContext.from_params("params.h")  # a moduli set in the reference's params.h format
     ev  = ctx.rns_eval_compute(x)             # cuda::rns_eval_compute  (src/rnseval.cuh:182)
     s   = ctx.rns_cmp(x, y)                   # cuda::rns_cmp           (src/rnscmp.cuh:55)
     q,r = ctx.rns_div(x, d)                   # cuda::rns_div           (src/rnsdiv.cuh:128)
@@ -12,6 +13,10 @@ whole device arrays through the C ABI of libgrns_gb300.so.
     z   = ctx.mpint_add(a, b) / mpint_sub / mpint_mul / mpint_div
                                               (src/mpint.cuh:336/:407/:478/:511)
     v,i = ctx.rns_max(x)                      # cuda::rns_max           (src/dpp/rnsmax.cuh:129)
+    x   = ctx.rns_from_binary(limbs) / w = ctx.rns_to_binary(x)
+                                              # rns_from_binary / rns_to_binary (src/rnsbase.cuh:253/:277)
+    m   = ctx.mpint_set_binary(limbs, signs) / w,s = ctx.mpint_get_binary(m)
+                                              # mpint_set_mpz / mpint_get_mpz (src/mpint.cuh:74/:100)
 
 RNS arrays are int32 CUDA tensors: layout "soa" is shape (n, count) (residue
 i of every number contiguous, the native layout), "aos" is shape (count, n)
@@ -50,6 +55,25 @@ def mpint_dtype(n):
                      "offsets": [0, 4 * n, off], "itemsize": off + 32})
 
 
+def ints_to_limbs(values, limbs):
+    """(count, limbs) int32 array of little-endian 32-bit limbs of nonnegative Python ints"""
+    out = np.zeros((len(values), limbs), dtype=np.uint32)
+    for k, v in enumerate(values):
+        v = int(v)
+        if v < 0 or v.bit_length() > 32 * limbs:
+            raise ValueError("value out of range for the limb count")
+        for j in range(limbs):
+            out[k, j] = v & 0xFFFFFFFF
+            v >>= 32
+    return out.view(np.int32)
+
+
+def limbs_to_ints(words):
+    """Python ints from a (count, limbs) array of little-endian 32-bit limbs"""
+    w = np.ascontiguousarray(words).view(np.uint32)
+    return [int.from_bytes(row.astype("<u4").tobytes(), "little") for row in w]
+
+
 def intervals_to_numpy(t):
     """device uint8 tensor of interval_t -> numpy structured array"""
     return t.cpu().numpy().view(IV_DTYPE)
@@ -63,6 +87,17 @@ def _stream(stream):
     import torch
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def parse_params(text):
+    """(moduli, stated RNS_MODULI_PRODUCT_LOG2 or None) of a moduli set in the
+    reference's params.h format (src/params.h); raises GrnsError on bad text"""
+    t = text.encode() if isinstance(text, str) else bytes(text)
+    n, lg = ctypes.c_int(0), ctypes.c_int(-1)
+    check(native.lib().grns_params_parse(t, None, 0, ctypes.byref(n), ctypes.byref(lg)), "grns_params_parse")
+    arr = (ctypes.c_int32 * max(1, n.value))()
+    check(native.lib().grns_params_parse(t, arr, n.value, ctypes.byref(n), ctypes.byref(lg)), "grns_params_parse")
+    return [int(v) for v in arr[:n.value]], (lg.value if lg.value >= 0 else None)
 
 
 class RNSContext:
@@ -82,6 +117,19 @@ class RNSContext:
         self.M = 1
         for m in self.moduli:
             self.M *= m
+
+    @classmethod
+    def from_params(cls, source):
+        """context for a params.h file (path) or its text: the reference's way of
+        choosing a moduli set (src/params.h, the src/params/ catalogue)"""
+        import os
+        text = open(source).read() if os.path.exists(str(source)) else source
+        moduli, lg = parse_params(text)
+        ctx = cls(moduli)
+        if lg is not None and lg != ctx.log2M:
+            ctx.close()
+            raise native.GrnsError(1, "RNS_MODULI_PRODUCT_LOG2 differs from floor(log2 M)")
+        return ctx
 
     @property
     def handle(self):
@@ -213,6 +261,65 @@ class RNSContext:
     def mpint_div(self, x, y, flags=None, stream=None):
         """Euclidean quotient x / y (cuda::mpint_div, src/mpint.cuh:511)."""
         return self._mpint(native.lib().grns_mpint_div, x, y, flags, stream)
+
+    # ---- binary <-> RNS conversion ----
+    @property
+    def binary_limbs(self):
+        """32-bit limbs of an integer below M"""
+        return native.lib().grns_ctx_binary_limbs(self._h)
+
+    @staticmethod
+    def _words(words):
+        if words.dtype.itemsize != 4 or not words.is_cuda or not words.is_contiguous() or words.dim() != 2:
+            raise ValueError("binary integers must be a contiguous (count, limbs) 32-bit CUDA tensor")
+        return words.shape[0], words.shape[1]
+
+    def rns_from_binary(self, words, layout="soa", stream=None):
+        """residues of nonnegative integers given as (count, limbs) little-endian
+        32-bit limbs (rns_from_binary, src/rnsbase.cuh:253)"""
+        import torch
+        count, limbs = self._words(words)
+        shape = (self.n, count) if layout == "soa" else (count, self.n)
+        out = torch.empty(shape, dtype=torch.int32, device=words.device)
+        check(native.lib().grns_from_binary(self._h, _ptr(words), limbs, count, LAYOUTS[layout], _ptr(out),
+                                            _stream(stream)), "grns_from_binary")
+        return out
+
+    def rns_to_binary(self, x, layout="soa", limbs=None, flags=None, stream=None):
+        """X in [0, M) as (count, limbs) little-endian 32-bit limbs (rns_to_binary, src/rnsbase.cuh:277)"""
+        import torch
+        count = self._count(x, layout)
+        limbs = self.binary_limbs if limbs is None else limbs
+        out = torch.empty((count, limbs), dtype=torch.int32, device=x.device)
+        check(native.lib().grns_to_binary(self._h, _ptr(x), count, LAYOUTS[layout], _ptr(out), limbs, _ptr(flags),
+                                          _stream(stream)), "grns_to_binary")
+        return out
+
+    def mpint_set_binary(self, words, signs=None, stream=None):
+        """mp_int_t records of sign-magnitude integers (mpint_set_mpz, src/mpint.cuh:74):
+        magnitudes as (count, limbs) limbs, signs an int32 CUDA tensor (nonzero: negative) or None"""
+        import torch
+        count, limbs = self._words(words)
+        if signs is not None and (signs.numel() != count or signs.dtype.itemsize != 4 or not signs.is_cuda):
+            raise ValueError("signs must hold one int32 per integer")
+        out = torch.empty(count * mpint_bytes(self.n), dtype=torch.uint8, device=words.device)
+        check(native.lib().grns_mpint_from_binary(self._h, _ptr(words), limbs, _ptr(signs), count, _ptr(out),
+                                                  _stream(stream)), "grns_mpint_from_binary")
+        return out
+
+    def mpint_get_binary(self, x, limbs=None, flags=None, stream=None):
+        """(magnitudes as (count, limbs) limbs, signs) of mp_int_t records (mpint_get_mpz, src/mpint.cuh:100)"""
+        import torch
+        nb = mpint_bytes(self.n)
+        if x.numel() % nb:
+            raise ValueError("mp_int arrays must be count * mpint_bytes(n) bytes")
+        count = x.numel() // nb
+        limbs = self.binary_limbs if limbs is None else limbs
+        words = torch.empty((count, limbs), dtype=torch.int32, device=x.device)
+        signs = torch.empty(count, dtype=torch.int32, device=x.device)
+        check(native.lib().grns_mpint_to_binary(self._h, _ptr(x), count, _ptr(words), limbs, _ptr(signs),
+                                                _ptr(flags), _stream(stream)), "grns_mpint_to_binary")
+        return words, signs
 
     def rns_max(self, x, layout="soa", scratch=None, stream=None):
         """returns (value residues int32[n], index int64[1]) on the device"""

@@ -41,6 +41,10 @@ struct HostTables {
     std::vector<uint64_t> mi64;                  // M_i mod 2^64
     uint64_t m64 = 0;                            // M mod 2^64
     uint64_t E = 0;  // sum_i (m_i - 1)
+    std::vector<uint32_t> bin_p26;               // kBinMaxChunks x n: 2^(26 c) mod m_i
+    std::vector<uint32_t> bin_mi26;              // bin_chunks x n: 26-bit chunks of M_i
+    std::vector<uint32_t> bin_m26;               // bin_chunks, padded to a multiple of 4: chunks of M
+    int bin_chunks = 0, bin_limbs = 0;
 };
 
 namespace hostdetail {
@@ -276,6 +280,41 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
             T.mrc_inv[(size_t)j * n + i] = v;
             T.mrc_inv_sh[(size_t)j * n + i] = shoup(v, m[i]);
         }
+    /* binary conversion: 26-bit chunks of M and of M_i = M / m_i, 2^(26 c) mod m_i */
+    {
+        auto chunks26 = [](const std::vector<uint32_t> &v, int count, uint32_t *dst, size_t stride) {
+            for (int c = 0; c < count; c++) {
+                const int bit = kBinChunk * c, j = bit / 32, off = bit % 32;
+                uint64_t w = j < (int)v.size() ? v[j] : 0;
+                if (j + 1 < (int)v.size()) w |= (uint64_t)v[j + 1] << 32;
+                dst[(size_t)c * stride] = (uint32_t)(w >> off) & ((1u << kBinChunk) - 1);
+            }
+        };
+        T.bin_limbs = (int)M.size();
+        T.bin_chunks = (bitlen + kBinChunk - 1) / kBinChunk;
+        T.bin_m26.assign((size_t)((T.bin_chunks + 3) / 4) * 4, 0);
+        chunks26(M, T.bin_chunks, T.bin_m26.data(), 1);
+        T.bin_mi26.assign((size_t)T.bin_chunks * n, 0);
+        for (int i = 0; i < n; i++) {
+            std::vector<uint32_t> q(M.size(), 0);  // M / m_i by long division
+            uint64_t r = 0;
+            for (int j = (int)M.size() - 1; j >= 0; j--) {
+                const uint64_t v = (r << 32) | M[j];
+                q[j] = (uint32_t)(v / m[i]);
+                r = v % m[i];
+            }
+            chunks26(q, T.bin_chunks, &T.bin_mi26[i], (size_t)n);
+        }
+        T.bin_p26.assign((size_t)kBinMaxChunks * n, 0);
+        for (int i = 0; i < n; i++) {
+            const uint64_t step = (((uint64_t)1) << kBinChunk) % m[i];
+            uint64_t v = 1 % m[i];
+            for (int c = 0; c < kBinMaxChunks; c++) {
+                T.bin_p26[(size_t)c * n + i] = (uint32_t)v;
+                v = (v * step) % m[i];
+            }
+        }
+    }
     /* scaling tables (src/rnsbase.cuh:364-387) */
     T.mi_pow2.resize((size_t)30 * n);
     T.m_pow2.resize(30);
@@ -300,8 +339,9 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
 
 /* The device-table blob (one allocation) and the pointer layout inside it. */
 inline std::vector<uint32_t> table_blob(const HostTables &T) {
-    std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows */
-    for (const auto *v : {&T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
+    std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows (every size below the
+                                            conversion tables is a multiple of 4 words) */
+    for (const auto *v : {&T.bin_p26, &T.bin_mi26, &T.bin_m26, &T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
                           &T.pow2_inv_sh, &T.pow2neg, &T.pow2neg_sh})
         blob.insert(blob.end(), v->begin(), v->end());
     return blob;
@@ -355,6 +395,11 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     C.E = T.E;
     C.c96k = reinterpret_cast<const uint4 *>(blob);
     size_t off = T.c96k.size();
+    C.bin_p26 = blob + off;     off += T.bin_p26.size();
+    C.bin_mi26 = blob + off;    off += T.bin_mi26.size();
+    C.bin_m26 = blob + off;     off += T.bin_m26.size();
+    C.bin_chunks = T.bin_chunks;
+    C.bin_limbs = T.bin_limbs;
     C.pow2 = blob + off;        off += T.pow2.size();
     C.pow2_sh = blob + off;     off += T.pow2_sh.size();
     C.mrc_inv = blob + off;     off += T.mrc_inv.size();

@@ -10,9 +10,12 @@
  * computes 1/M and 1-1/M.  Everything else is a product, power or inverse
  * modulo a 31-bit modulus or a power of two.
  */
+#include <cctype>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
+#include <string>
 
 #include "internal.h"
 
@@ -46,6 +49,65 @@ grns_status build(grns_ctx *c, const uint32_t *moduli) {
         default: return GRNS_ERR_UNSUPPORTED;
     }
     return GRNS_OK;
+}
+
+/* ---- the reference's params.h format (src/params.h:11-39, src/params/...) ---- */
+
+/* text with comments removed and backslash-newline continuations joined */
+std::string params_clean(const char *text) {
+    std::string out;
+    for (const char *p = text; *p;) {
+        if (p[0] == '/' && p[1] == '*') {
+            const char *e = strstr(p + 2, "*/");
+            p = e ? e + 2 : p + strlen(p);
+            out += ' ';
+        } else if (p[0] == '/' && p[1] == '/') {
+            while (*p && *p != '\n') p++;
+        } else if (p[0] == '\\' && p[1] == '\n') {
+            p += 2;
+            out += ' ';
+        } else {
+            out += *p++;
+        }
+    }
+    return out;
+}
+
+/* the text after "#define NAME" up to the end of its line, or "" */
+std::string params_define(const std::string &t, const char *name) {
+    size_t pos = 0;
+    const size_t nl = strlen(name);
+    while ((pos = t.find("#define", pos)) != std::string::npos) {
+        size_t q = pos + 7;
+        while (q < t.size() && (t[q] == ' ' || t[q] == '\t')) q++;
+        if (t.compare(q, nl, name) == 0 && q + nl < t.size() && !(isalnum((unsigned char)t[q + nl]) || t[q + nl] == '_')) {
+            const size_t e = t.find('\n', q + nl);
+            return t.substr(q + nl, e == std::string::npos ? std::string::npos : e - q - nl);
+        }
+        pos = q;
+    }
+    return "";
+}
+
+/* integers of a definition, ignoring parentheses, braces and commas; false on other text */
+bool params_numbers(const std::string &v, std::vector<long long> &out, bool allow_fraction = false) {
+    out.clear();
+    for (size_t i = 0; i < v.size();) {
+        const char ch = v[i];
+        if (ch == ' ' || ch == '\t' || ch == '\r' || ch == '(' || ch == ')' || ch == '{' || ch == '}' || ch == ',') {
+            i++;
+        } else if (isdigit((unsigned char)ch) || (allow_fraction && ch == '.')) {
+            size_t j = i;
+            while (j < v.size() && (isdigit((unsigned char)v[j]) || (allow_fraction && (v[j] == '.' || v[j] == 'e' ||
+                                                                                       v[j] == 'E' || v[j] == '-'))))
+                j++;
+            out.push_back(allow_fraction ? 0 : atoll(v.substr(i, j - i).c_str()));
+            i = j;
+        } else {
+            return false;
+        }
+    }
+    return true;
 }
 
 __global__ void k_ceil_log2(const double *x, int32_t *out, int64_t count) {
@@ -113,6 +175,52 @@ grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out) {
     }
     *out = c;
     return GRNS_OK;
+}
+
+grns_status grns_params_parse(const char *text, int32_t *moduli, int capacity, int *n_out, int *log2_out) {
+    if (!text || !n_out) return GRNS_ERR_INVALID_ARGUMENT;
+    const std::string t = params_clean(text);
+    std::vector<long long> size, vals, lg, thr;
+    if (!params_numbers(params_define(t, "RNS_MODULI_SIZE"), size) || size.size() != 1 ||
+        !params_numbers(params_define(t, "RNS_MODULI_VALUES"), vals) || (long long)vals.size() != size[0])
+        return GRNS_ERR_INVALID_ARGUMENT;
+    const std::string l2 = params_define(t, "RNS_MODULI_PRODUCT_LOG2");
+    if (!l2.empty() && (!params_numbers(l2, lg) || lg.size() != 1)) return GRNS_ERR_INVALID_ARGUMENT;
+    /* the scaling threshold and the evaluation error bound are fixed at the
+     * values every shipped set uses */
+    const std::string th = params_define(t, "RNS_P2_SCALING_THRESHOLD");
+    if (!th.empty() && (!params_numbers(th, thr) || thr.size() != 1 || thr[0] != grns::kScaleStep))
+        return GRNS_ERR_UNSUPPORTED;
+    const std::string re = params_define(t, "RNS_EVAL_RELATIVE_ERROR");
+    if (!re.empty() && std::fabs(strtod(re.c_str() + re.find_first_not_of(" \t("), nullptr) - 0.0000001) > 1e-15)
+        return GRNS_ERR_UNSUPPORTED;
+    for (long long v : vals)
+        if (v < 1 || v > 0x7fffffffLL) return GRNS_ERR_INVALID_ARGUMENT;
+    *n_out = (int)size[0];
+    if (log2_out) *log2_out = lg.empty() ? -1 : (int)lg[0];
+    if (moduli) {
+        if (capacity < (int)vals.size()) return GRNS_ERR_INVALID_ARGUMENT;
+        for (size_t i = 0; i < vals.size(); i++) moduli[i] = (int32_t)vals[i];
+    }
+    return GRNS_OK;
+}
+
+grns_status grns_ctx_create_from_params(const char *text, grns_ctx **out) {
+    if (!out) return GRNS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0, lg = -1;
+    grns_status st = grns_params_parse(text, nullptr, 0, &n, &lg);
+    if (st != GRNS_OK) return st;
+    std::vector<int32_t> mods(n > 0 ? n : 1);
+    st = grns_params_parse(text, mods.data(), n, &n, &lg);
+    if (st != GRNS_OK) return st;
+    st = grns_ctx_create(mods.data(), n, out);
+    if (st == GRNS_OK && lg >= 0 && lg != (*out)->log2M) {  // RNS_MODULI_PRODUCT_LOG2 must be floor(log2 M)
+        grns_ctx_destroy(*out);
+        *out = nullptr;
+        return GRNS_ERR_INVALID_ARGUMENT;
+    }
+    return st;
 }
 
 grns_status grns_ctx_destroy(grns_ctx *c) {

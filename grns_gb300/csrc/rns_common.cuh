@@ -34,6 +34,12 @@ constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/param
 constexpr int kDivB = 48;       // quotient bits per step of the integer division
 constexpr int kScaleB = 52;     // bits per step of the integer power-of-two scaling
 constexpr int kPow2NegRows = 64;  // rows j = 0..63 of the 2^-j mod m_i table
+/* binary <-> RNS conversion: integers as 32-bit little-endian limbs, worked
+ * on in 26-bit chunks (26 + 30.42 bits per product: up to 158 products, or
+ * 64 moduli, sum below 2^64) */
+constexpr int kBinChunk = 26;
+constexpr int kBinMaxLimbs = 128;                                   // 4096-bit inputs
+constexpr int kBinMaxChunks = (32 * kBinMaxLimbs + kBinChunk - 1) / kBinChunk;  // 158
 
 /* levels of the pairwise summation tree over n leaves */
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c((n + 1) / 2); }
@@ -87,6 +93,12 @@ struct Consts {
     const uint32_t *pow2_inv_sh;// [30 * N]
     const uint32_t *pow2neg;    // [kPow2NegRows * N]  2^-j mod m_i
     const uint32_t *pow2neg_sh; // [kPow2NegRows * N]
+    /* binary conversion (16-byte aligned rows) */
+    const uint32_t *bin_p26;    // [kBinMaxChunks * N]  2^(26 c) mod m_i
+    const uint32_t *bin_mi26;   // [bin_chunks * N]     26-bit chunk c of M_i = M / m_i
+    const uint32_t *bin_m26;    // [bin_chunks]         26-bit chunk c of M
+    int bin_chunks;             // ceil(bits(M) / 26)
+    int bin_limbs;              // ceil(bits(M) / 32): 32-bit limbs of an integer below M
 };
 
 /* ---------------- modular arithmetic ---------------- */

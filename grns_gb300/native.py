@@ -19,6 +19,8 @@ SIGNATURES = {
     "grns_version": (ctypes.c_char_p, []),
     "grns_ctx_create": (c_int, [c_void_p, c_int, ctypes.POINTER(c_void_p)]),
     "grns_ctx_destroy": (c_int, [c_void_p]),
+    "grns_params_parse": (c_int, [ctypes.c_char_p, c_void_p, c_int, c_void_p, c_void_p]),
+    "grns_ctx_create_from_params": (c_int, [ctypes.c_char_p, ctypes.POINTER(c_void_p)]),
     "grns_ctx_n": (c_int, [c_void_p]),
     "grns_ctx_log2": (c_int, [c_void_p]),
     "grns_ctx_get_table": (c_int, [c_void_p, c_int, c_void_p, c_size_t]),
@@ -33,6 +35,11 @@ SIGNATURES = {
     "grns_mpint_sub": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "grns_mpint_mul": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "grns_mpint_div": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "grns_ctx_binary_limbs": (c_int, [c_void_p]),
+    "grns_from_binary": (c_int, [c_void_p, c_void_p, c_int, c_int64, c_int, c_void_p, c_void_p]),
+    "grns_to_binary": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "grns_mpint_from_binary": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int64, c_void_p, c_void_p]),
+    "grns_mpint_to_binary": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_max_scratch_size": (c_int, [c_void_p, c_int64, ctypes.POINTER(c_size_t)]),
     "grns_max": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "grns_max_noalloc": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),

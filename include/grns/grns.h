@@ -70,6 +70,18 @@ const char *grns_version(void);
  * moduli odd, pairwise coprime, 3 <= m_i <= 1431655765. */
 grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out);
 grns_status grns_ctx_destroy(grns_ctx *ctx);
+
+/* Moduli sets in the reference's params.h format (src/params.h:11-39 and the
+ * catalogue src/params/moduli-<range>/params.<n>m.<bits>b.h): the text of such a file, with
+ * RNS_MODULI_SIZE and RNS_MODULI_VALUES; RNS_MODULI_PRODUCT_LOG2, when given,
+ * must equal floor(log2 M), RNS_P2_SCALING_THRESHOLD 30 and
+ * RNS_EVAL_RELATIVE_ERROR 1e-7 (the values of every shipped set; others return
+ * GRNS_ERR_UNSUPPORTED).  grns_params_parse writes n (and the moduli when
+ * `moduli` is not NULL and capacity >= n; log2_out gets the stated
+ * RNS_MODULI_PRODUCT_LOG2 or -1); grns_ctx_create_from_params parses and
+ * creates the context (grns_ctx_create's rules on n and the moduli apply). */
+grns_status grns_params_parse(const char *text, int32_t *moduli, int capacity, int *n_out, int *log2_out);
+grns_status grns_ctx_create_from_params(const char *text, grns_ctx **out);
 int grns_ctx_n(const grns_ctx *ctx);
 /* floor(log2 M): the reference's RNS_MODULI_PRODUCT_LOG2 (src/params.h:16) */
 int grns_ctx_log2(const grns_ctx *ctx);
@@ -156,6 +168,37 @@ grns_status grns_mpint_mul(grns_ctx *ctx, const void *x, const void *y, int64_t 
  * context's pool; `out` must not overlap x or y. */
 grns_status grns_mpint_div(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
                            uint8_t *flags, void *stream);
+
+/* ---- binary <-> RNS conversion ----
+ * Binary integers are number-major rows of `limbs` little-endian 32-bit
+ * words (word l of number k at words[k * limbs + l]; GMP's
+ * mpz_export(w, NULL, -1, 4, 0, 0, z) writes this form), limbs <= 128.
+ *   grns_from_binary      : out = residues of each nonnegative integer, as
+ *                           rns_from_binary (reference src/rnsbase.cuh:253);
+ *                           integers of M or more give their residues mod M.
+ *   grns_to_binary        : X in [0, M) of each RNS number, as rns_to_binary
+ *                           (src/rnsbase.cuh:277); limbs >= grns_ctx_binary_limbs,
+ *                           words above the value are zero.  A residue >= its
+ *                           modulus sets GRNS_FLAG_INVALID_INPUT and gives 0.
+ *   grns_mpint_from_binary: mp_int_t records of sign-magnitude integers, as
+ *                           mpint_set_mpz (src/mpint.cuh:74): magnitudes in
+ *                           `words`, signs[k] != 0 for a negative integer
+ *                           (signs may be NULL: all nonnegative; zero gets
+ *                           sign 0); the evaluation is cuda::rns_eval_compute's
+ *                           of the digits (the host mpint_set_mpz uses the
+ *                           host evaluation).
+ *   grns_mpint_to_binary  : magnitudes and signs of mp_int_t records, as
+ *                           mpint_get_mpz (src/mpint.cuh:100); signs may be
+ *                           NULL; the sign of zero is 0. */
+int grns_ctx_binary_limbs(const grns_ctx *ctx);  /* ceil(bits(M) / 32) */
+grns_status grns_from_binary(grns_ctx *ctx, const uint32_t *words, int limbs, int64_t count, int layout,
+                             int32_t *out, void *stream);
+grns_status grns_to_binary(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, uint32_t *words, int limbs,
+                           uint8_t *flags, void *stream);
+grns_status grns_mpint_from_binary(grns_ctx *ctx, const uint32_t *words, int limbs, const int32_t *signs,
+                                   int64_t count, void *out, void *stream);
+grns_status grns_mpint_to_binary(grns_ctx *ctx, const void *x, int64_t count, uint32_t *words, int limbs,
+                                 int32_t *signs, uint8_t *flags, void *stream);
 
 /* ---- maximum of an RNS array ----
  * Replaces template cuda::rns_max<g1,b1,g2,b2>(out, in, N, buffer)

@@ -156,6 +156,34 @@ void ref_mpint_from_str(const char *dec, mp_int_t *out) {
 }
 void ref_mpint_set_i(int v, mp_int_t *out) { mpint_set_i(out, v); }
 
+/* rns_from_binary (src/rnsbase.cuh:253) of the integer in a decimal string */
+void ref_rns_from_str(const char *dec, int *out) {
+    mpz_t v;
+    mpz_init(v);
+    mpz_set_str(v, dec, 10);
+    rns_from_binary(out, v);
+    mpz_clear(v);
+}
+/* rns_to_binary (src/rnsbase.cuh:277) as a decimal string; buf holds 2048 chars */
+void ref_rns_to_str(const int *x, char *buf) {
+    mpz_t v;
+    mpz_init(v);
+    int t[N_];
+    memcpy(t, x, sizeof(t));
+    rns_to_binary(v, t);
+    mpz_get_str(buf, 10, v);
+    mpz_clear(v);
+}
+/* mpint_get_mpz (src/mpint.cuh:100) as a decimal string; buf holds 2048 chars */
+void ref_mpint_to_str(const mp_int_t *x, char *buf) {
+    mpz_t v;
+    mpz_init(v);
+    mp_int_t t = *x;
+    mpint_get_mpz(v, &t);
+    mpz_get_str(buf, 10, v);
+    mpz_clear(v);
+}
+
 /* extended-range ops for the reference's er_* known-answer checks.
  * op: 0 add, 1 add_rd, 2 add_ru, 3 sub, 4 sub_rd, 5 sub_ru, 6 mul, 7 mul_rd,
  *     8 mul_ru, 9 div, 10 div_rd, 11 div_ru, 12 md_rd(x,y,z), 13 md_ru(x,y,z),

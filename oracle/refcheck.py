@@ -104,6 +104,33 @@ class Ref:
         self.L.ref_mpint_from_str(str(s).encode(), _p(out))
         return out
 
+    def from_int(self, values):
+        """rns_from_binary of each nonnegative Python int (AoS int32 residues)"""
+        out = np.zeros((len(values), self.n), np.int32)
+        for k, v in enumerate(values):
+            self.L.ref_rns_from_str(str(int(v)).encode(), _p(out[k]))
+        return out
+
+    def to_int(self, x):
+        """rns_to_binary of each row of AoS residues, as Python ints"""
+        x = np.ascontiguousarray(x, np.int32)
+        buf = ctypes.create_string_buffer(2048)
+        res = []
+        for k in range(x.shape[0]):
+            self.L.ref_rns_to_str(_p(x[k]), buf)
+            res.append(int(buf.value.decode()))
+        return res
+
+    def mpint_to_int(self, m):
+        """mpint_get_mpz of each mp_int_t record, as Python ints"""
+        m = np.ascontiguousarray(m)
+        buf = ctypes.create_string_buffer(2048)
+        res = []
+        for k in range(m.shape[0]):
+            self.L.ref_mpint_to_str(_p(m[k:k + 1]), buf)
+            res.append(int(buf.value.decode()))
+        return res
+
     def er(self, op, dev, x, y=(0.0, 0), z=(0.0, 0)):
         a = np.array([x], ER_DTYPE)
         b = np.array([y], ER_DTYPE)

@@ -9,7 +9,8 @@ own verification programs: consecutive numbers from 0 and from M-1
 (tests/test_verify_rnseval.cu:87-149, tests/test_verify_mrc.cu:128-152),
 powers of two 2^0..2^LOG2 (tests/test_perf_rnseval.cu:679-688), the mp_int
 known-answer pair x=-55, y=13 (tests/test_verify_mpint.cu:92-93), signed
-mp_int division operands with the Euclidean sign cases, and the
+mp_int division operands with the Euclidean sign cases, binary <-> RNS
+conversions through the reference's GMP routines, and the
 extended-range doubles of tests/test_verify_extrange.cu:115-117.
 
 Run from the repository root:  python tests/golden/make_golden.py
@@ -38,6 +39,15 @@ def special_values(M, log2M):
     v += list(range(4, 10)) + [M - k for k in range(4, 10)]
     v += [1 << j for j in range(0, log2M + 1, max(1, log2M // 16))] + [1 << log2M, (1 << log2M) - 1]
     return v
+
+
+def limbs_of(values, limbs):
+    """(count, limbs) uint32 little-endian limbs of nonnegative ints"""
+    out = np.zeros((len(values), limbs), np.uint32)
+    for k, v in enumerate(values):
+        for j in range(limbs):
+            out[k, j] = (int(v) >> (32 * j)) & 0xFFFFFFFF
+    return out
 
 
 def main():
@@ -119,6 +129,18 @@ def main():
         fx["mpdiv_a"], fx["mpdiv_b"] = da, db
         for path, dev in (("dev", True), ("host", False)):
             fx[f"mpint_div_{path}"] = ref.mpint("div", da.view(dt), db.view(dt), dev=dev).view(np.uint8)
+        # binary <-> RNS (rns_to_binary / rns_from_binary, src/rnsbase.cuh:277/:253;
+        # mpint_get_mpz, src/mpint.cuh:100) as 32-bit little-endian limbs
+        LM = (M.bit_length() + 31) // 32
+        fx["tobin_words"] = limbs_of(ref.to_int(x), LM)
+        rb = random.Random(20261204 + n)
+        FB = [rb.randrange(1 << (32 * (LM + 2))) for _ in range(nrand)] + [0, 1, M - 1, M, M + 1, 2 * M + 5]
+        FB += [rb.randrange(1 << b) for b in range(1, 32 * (LM + 2), max(1, 32 * (LM + 2) // 24))]
+        fx["frombin_words"] = limbs_of(FB, LM + 2)
+        fx["frombin_rns"] = ref.from_int(FB)
+        mv = ref.mpint_to_int(da.view(dt))
+        fx["mpint_tobin_words"] = limbs_of([abs(v) for v in mv], LM)
+        fx["mpint_tobin_signs"] = np.array([1 if v < 0 else 0 for v in mv], np.int32)
         # extended-range known answers (tests/test_verify_extrange.cu:115-117)
         if tag == "ref8":
             dvals = [0.00003687544343, 0.41352, 12345.1443575]

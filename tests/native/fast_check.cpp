@@ -7,6 +7,7 @@
 
 #include "../../grns_gb300/csrc/consts_host.h"
 #include "../../grns_gb300/csrc/rns_fast.cuh"
+#include "../../grns_gb300/csrc/rns_convert.cuh"
 
 using namespace grns;
 
@@ -97,6 +98,30 @@ int fc_eval_tight(void *p, const uint32_t *x, long cnt, int32_t *ok, Er *iv) {
 #undef C_
     return 0;
 }
+
+/* binary -> RNS: words[k * limbs ..] little-endian 32-bit limbs */
+int fc_from_binary(void *p, const uint32_t *words, int limbs, long cnt, uint32_t *out) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) from_binary<N>(K<N>(b), words + k * limbs, limbs, out + k * N)
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
+/* RNS -> binary: out[k * bin_limbs ..]; ok[k] = 0 for an invalid residue */
+int fc_to_binary(void *p, const uint32_t *x, long cnt, uint32_t *out, int32_t *ok) {
+    Box *b = (Box *)p;
+    std::vector<uint32_t> d(b->T.bin_chunks);
+    const int L = b->T.bin_limbs;
+#define C_(N) for (long k = 0; k < cnt; k++) { \
+        ok[k] = to_binary<N>(K<N>(b), [&](int i) { return x[k * N + i]; }, d.data(), 1) ? 1 : 0; \
+        for (int l = 0; l < L; l++) out[k * L + l] = d[l]; }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
+int fc_binary_limbs(void *p) { return ((Box *)p)->T.bin_limbs; }
 
 uint64_t fc_E(void *p) { return ((Box *)p)->T.E; }
 

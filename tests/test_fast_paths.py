@@ -29,7 +29,8 @@ def fc(tmp_path_factory):
     L.fc_destroy.argtypes = [ctypes.c_void_p]
     L.fc_E.restype = ctypes.c_uint64
     L.fc_E.argtypes = [ctypes.c_void_p]
-    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight"):
+    L.fc_binary_limbs.argtypes = [ctypes.c_void_p]
+    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary"):
         getattr(L, f).argtypes = None
     return L
 
@@ -72,6 +73,23 @@ class FC:
         out = np.zeros_like(x)
         self.L.fc_scale(self.h, self.P(x), self.P(s), ctypes.c_long(len(X)), self.P(out))
         return self.ints(out)
+
+    def from_binary(self, vals, limbs):
+        w = np.zeros((len(vals), limbs), np.uint32)
+        for k, v in enumerate(vals):
+            for j in range(limbs):
+                w[k, j] = (v >> (32 * j)) & 0xFFFFFFFF
+        out = np.zeros((len(vals), self.n), np.uint32)
+        self.L.fc_from_binary(self.h, self.P(w), ctypes.c_int(limbs), ctypes.c_long(len(vals)), self.P(out))
+        return out
+
+    def to_binary(self, x):
+        x = np.ascontiguousarray(x, np.uint32)
+        L = self.L.fc_binary_limbs(self.h)
+        out = np.zeros((len(x), L), np.uint32)
+        ok = np.zeros(len(x), np.int32)
+        self.L.fc_to_binary(self.h, self.P(x), ctypes.c_long(len(x)), self.P(out), self.P(ok))
+        return [int.from_bytes(r.astype("<u4").tobytes(), "little") for r in out], ok
 
     def fx(self, X):
         x = self.res(X)
@@ -274,3 +292,37 @@ def test_scaling_step_boundaries(fc, tag):
                 X.append(x)
                 S.append(D)
     assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
+
+
+@pytest.mark.parametrize("moduli", SMALL_SETS[:2])
+def test_binary_conversion_exhaustive_small(fc, moduli):
+    """every X in [0, M) (or a dense sample) through RNS -> binary -> RNS"""
+    f = FC(fc, moduli)
+    vals = list(range(f.M)) if f.M <= 200000 else sorted(set(random.Random(3).randrange(f.M) for _ in range(200000)))
+    x = f.res(vals)
+    back, ok = f.to_binary(x)
+    assert back == vals and ok.all()
+    limbs = max(1, (f.M.bit_length() + 31) // 32)
+    assert np.array_equal(f.from_binary(vals, limbs), x)
+
+
+@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+def test_binary_conversion(fc, tag):
+    """rns_from_binary / rns_to_binary arithmetic against exact integers: uniform
+    values, values of every bit length, near 0 and M (the rank estimate is one
+    too high there), inputs of M and more, up to 128 limbs"""
+    f = FC(fc, moduli_for(tag))
+    rng = random.Random(11)
+    vals = [rng.randrange(f.M) for _ in range(400)]
+    vals += [rng.randrange(1 << b) for b in range(1, f.M.bit_length())]
+    vals += list(range(0, 40)) + [f.M - k for k in range(1, 40)] + [f.M // 2 + d for d in (-1, 0, 1)]
+    back, ok = f.to_binary(f.res(vals))
+    assert back == vals and ok.all()
+    for limbs in (1, 3, (f.M.bit_length() + 31) // 32, 128):
+        wide = [rng.randrange(1 << (32 * limbs)) for _ in range(60)] + [(1 << (32 * limbs)) - 1]
+        assert np.array_equal(f.from_binary(wide, limbs), f.res([v % f.M for v in wide]))
+    # a residue >= its modulus is refused
+    bad = f.res([5])
+    bad[0, 0] = f.moduli[0]
+    back, ok = f.to_binary(bad)
+    assert ok[0] == 0 and back[0] == 0

@@ -87,6 +87,25 @@ def test_mpint_div_euclidean(case):
     assert ex.encloses(ivs, ex.from_rns(out["digits"])).all()
 
 
+def _ints(words):
+    return [int.from_bytes(r.astype("<u4").tobytes(), "little") for r in np.asarray(words)]
+
+
+def test_binary_conversion_matches_golden(case):
+    """rns_to_binary / rns_from_binary (src/rnsbase.cuh:277/:253) and
+    mpint_get_mpz (src/mpint.cuh:100) through GMP in the reference"""
+    tag, orc, g = case
+    ex = orc.exact
+    assert ex.from_rns(g["x"]) == _ints(g["tobin_words"])
+    vals = _ints(g["frombin_words"])
+    assert np.array_equal(ex.to_rns([v % ex.M for v in vals]), g["frombin_rns"])
+    dt = mpint_dtype(orc.n)
+    m = g["mpdiv_a"].view(dt)
+    mags = ex.from_rns(m["digits"])
+    assert mags == _ints(g["mpint_tobin_words"])
+    assert [int(s == 1 and v != 0) for s, v in zip(m["sign"], mags)] == list(g["mpint_tobin_signs"])
+
+
 def test_mpint_known_answer(case):
     """x = -55, y = 13 (reference tests/test_verify_mpint.cu:92-93)"""
     tag, orc, g = case
