@@ -239,6 +239,44 @@ class RNSContext:
                                           _ptr(flags), _stream(stream)), "grns_scale2pow")
         return out
 
+    # ---- host-buffer forms (copies pipelined with the kernels) ----
+    @staticmethod
+    def _host(t, name):
+        if t.is_cuda or not t.is_contiguous() or t.dtype.itemsize != 4:
+            raise ValueError(f"{name} must be a contiguous 32-bit CPU tensor (page-locked for overlap)")
+
+    def _host_count(self, x, layout):
+        self._host(x, "x")
+        if x.dim() != 2 or x.shape[0 if layout == "soa" else 1] != self.n:
+            raise ValueError("RNS host array has the wrong shape for the layout")
+        return x.shape[1] if layout == "soa" else x.shape[0]
+
+    def rns_div_host(self, x, d, layout="soa", flags=None, chunks=0, stream=None):
+        """rns_div over host arrays: (q, r) host tensors (page-locked like x)"""
+        import torch
+        count = self._host_count(x, layout)
+        self._host(d, "d")
+        pin = x.is_pinned()
+        q = torch.empty(x.shape, dtype=x.dtype, pin_memory=pin)
+        r = torch.empty(x.shape, dtype=x.dtype, pin_memory=pin)
+        check(native.lib().grns_div_host(self._h, _ptr(x), _ptr(d), count, LAYOUTS[layout], _ptr(q), _ptr(r),
+                                         _ptr(flags), chunks, _stream(stream)), "grns_div_host")
+        return q, r
+
+    def rns_scale2pow_host(self, x, D, layout="soa", flags=None, chunks=0, stream=None):
+        """rns_scale2pow over host arrays; D an int or a host tensor of per-element exponents"""
+        import torch
+        count = self._host_count(x, layout)
+        out = torch.empty(x.shape, dtype=x.dtype, pin_memory=x.is_pinned())
+        if isinstance(D, int):
+            dptr, du = ctypes.c_void_p(0), D
+        else:
+            self._host(D, "D")
+            dptr, du = _ptr(D), 0
+        check(native.lib().grns_scale2pow_host(self._h, _ptr(x), dptr, du, count, LAYOUTS[layout], _ptr(out),
+                                               _ptr(flags), chunks, _stream(stream)), "grns_scale2pow_host")
+        return out
+
     def _mpint(self, fn, x, y, flags, stream):
         import torch
         nb = mpint_bytes(self.n)

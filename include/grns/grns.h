@@ -147,6 +147,20 @@ grns_status grns_div(grns_ctx *ctx, const int32_t *x, const int32_t *d, int64_t 
 grns_status grns_scale2pow(grns_ctx *ctx, const int32_t *x, const uint32_t *D, uint32_t D_uniform,
                            int64_t count, int layout, int32_t *out, uint8_t *flags, void *stream);
 
+/* ---- host-buffer forms ----
+ * grns_div / grns_scale2pow over arrays in HOST memory (same layouts, same
+ * results): the arrays are split into `chunks` ranges (0: automatic) and the
+ * host->device copies of one range, the kernels of the previous one and the
+ * device->host copies of the one before run at the same time on internal
+ * streams; the call is ordered on `stream` like the device-pointer forms (the
+ * host outputs are complete when the stream reaches that point).  Copies
+ * overlap for page-locked host memory.  Device scratch: two chunks' worth of
+ * inputs and outputs from the context's pool. */
+grns_status grns_div_host(grns_ctx *ctx, const int32_t *x, const int32_t *d, int64_t count, int layout, int32_t *q,
+                          int32_t *r, uint8_t *flags, int chunks, void *stream);
+grns_status grns_scale2pow_host(grns_ctx *ctx, const int32_t *x, const uint32_t *D, uint32_t D_uniform,
+                                int64_t count, int layout, int32_t *out, uint8_t *flags, int chunks, void *stream);
+
 /* ---- multiple-precision integers (mp_int_t arrays, reference layout) ----
  * result = x + y / x - y / x * y elementwise with the interval evaluation
  * derived as cuda::mpint_add / mpint_sub / mpint_mul (reference

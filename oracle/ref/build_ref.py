@@ -46,14 +46,26 @@ def floor_log2_product(moduli):
     return M.bit_length() - 1
 
 
-# tag -> moduli (None = the reference's shipped src/params.h)
+# tag -> moduli (None = the reference's shipped src/params.h; a string = a
+# params file of the reference's catalogue, pre-included as it is)
 SETS = {
     "ref8": None,
     "g8": greedy_moduli(8),
     "g12": greedy_moduli(12),
     "g32": greedy_moduli(32),
     "g64": greedy_moduli(64),
+    "p16": "src/params/moduli-10-69-bit/params.16m.69b.h",    # moduli 3..59
+    "p32": "src/params/moduli-64-4096-bit/params.32m.512b.h",  # 17-bit moduli
+    "p64": "src/params/moduli-100-6400-bit/params.64m.1600b.h",  # 26-bit moduli
 }
+
+
+def catalogue_moduli(relpath):
+    """RNS_MODULI_VALUES of a params file of the reference's catalogue"""
+    import re
+    text = open(os.path.join(REF, relpath)).read().replace("\\\n", " ")
+    vals = re.search(r"#define\s+RNS_MODULI_VALUES\s*\{([^}]*)\}", text).group(1)
+    return [int(v) for v in vals.split(",")]
 
 
 def params_header(moduli):
@@ -87,7 +99,9 @@ def build_one(tag, gmp, mpfr):
     drv = os.path.join(HERE, "ref_driver.cpp")
     cmd = ["g++", "-std=c++14", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-frounding-math",
            "-w", "-include", os.path.join(HERE, "shim", "cuda_host_shim.h")]
-    if SETS[tag] is not None:
+    if isinstance(SETS[tag], str):
+        cmd += ["-include", os.path.join(REF, SETS[tag])]
+    elif SETS[tag] is not None:
         hdr = os.path.join(OUT, f"params_{tag}.h")
         with open(hdr, "w") as f:
             f.write(params_header(SETS[tag]))

@@ -31,7 +31,7 @@ from oracle.oracle import REFERENCE_DEFAULT_MODULI  # noqa: E402
 from oracle.ref import build_ref  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-TAGS = ["ref8", "g8", "g12", "g32", "g64"]
+TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"]
 
 
 def special_values(M, log2M):
@@ -57,6 +57,8 @@ def main():
     for tag in TAGS:
         ref = refcheck.get(tag)
         moduli = build_ref.SETS[tag] or REFERENCE_DEFAULT_MODULI
+        if isinstance(moduli, str):  # a params file of the reference's catalogue
+            moduli = build_ref.catalogue_moduli(moduli)
         n = len(moduli)
         M = 1
         for m in moduli:

@@ -6,7 +6,9 @@ import numpy as np
 from oracle.oracle import REFERENCE_DEFAULT_MODULI, greedy_moduli
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-TAGS = ["ref8", "g8", "g12", "g32", "g64"]
+# moduli sets: the reference's shipped default (ref8), greedy 30-bit sets (gN) and
+# three sets of the reference's params catalogue (pN: moduli 3..59, 17-bit, 26-bit)
+TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"]
 
 ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
 IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
@@ -15,6 +17,8 @@ IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
 def moduli_for(tag):
     if tag == "ref8":
         return list(REFERENCE_DEFAULT_MODULI)
+    if tag.startswith("p"):  # recorded in the fixture by tests/golden/make_golden.py
+        return [int(m) for m in np.load(os.path.join(GOLDEN, f"golden_{tag}.npz"))["moduli"]]
     return greedy_moduli(int(tag[1:]))
 
 

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from grns_gb300 import workload as W
-from tests.helpers import IV_DTYPE as IV, moduli_for
+from tests.helpers import IV_DTYPE as IV, TAGS, moduli_for
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SMALL_SETS = [[3, 5, 7, 11], [3, 5, 7, 11, 13, 17, 19, 23], [3, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43]]
@@ -135,7 +135,7 @@ def test_fixed_point_enclosure(fc):
                 assert U - E <= Fraction(v, f.M) * 2 ** 96 <= U
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+@pytest.mark.parametrize("tag", TAGS)
 def test_random_and_special(fc, tag):
     f = FC(fc, moduli_for(tag))
     M = f.M
@@ -161,7 +161,7 @@ def test_random_and_special(fc, tag):
     assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64"])
+@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64", "p16", "p32", "p64"])
 def test_division_quotient_boundaries(fc, tag):
     """dividends just below, at and above multiples of the divisor, divisors
     near M and near powers of two: the certified quotient estimate must never
@@ -191,7 +191,7 @@ def test_division_quotient_boundaries(fc, tag):
     assert not fl.any()
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g8", "g32", "g64"])
+@pytest.mark.parametrize("tag", ["ref8", "g8", "g32", "g64", "p16", "p32", "p64"])
 def test_division_short_and_extreme_dividends(fc, tag):
     """dividends of every length (the leading zero digits are skipped), and
     dividends within a hair of M or of 0 (where a fixed-point evaluation
@@ -217,7 +217,7 @@ def test_division_short_and_extreme_dividends(fc, tag):
     assert not fl.any()
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+@pytest.mark.parametrize("tag", TAGS)
 def test_integer_eval_is_bit_exact(fc, tag):
     """the integer-pipe evaluation returns, on its common path, the same two
     doubles as the reference's FP64 directed-rounding evaluation (device path
@@ -247,7 +247,7 @@ def er_fraction(frac, exp):
     return Fraction(float(frac)) * Fraction(2) ** int(exp)
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+@pytest.mark.parametrize("tag", TAGS)
 def test_one_ulp_evaluation(fc, tag):
     """where the 128-bit evaluation certifies it, the interval encloses X/M
     exactly, is at most one ulp wide, and is never wider than the reference's
@@ -277,7 +277,7 @@ def test_one_ulp_evaluation(fc, tag):
         assert up - lo <= rup - rlo
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64"])
+@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64", "p16", "p32", "p64"])
 def test_scaling_step_boundaries(fc, tag):
     """exponents at and around multiples of the 52-bit step, the full range,
     and dividends next to 0 and M (the first step's checked rank)"""
@@ -306,7 +306,7 @@ def test_binary_conversion_exhaustive_small(fc, moduli):
     assert np.array_equal(f.from_binary(vals, limbs), x)
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g8", "g12", "g32", "g64"])
+@pytest.mark.parametrize("tag", TAGS)
 def test_binary_conversion(fc, tag):
     """rns_from_binary / rns_to_binary arithmetic against exact integers: uniform
     values, values of every bit length, near 0 and M (the rank estimate is one

@@ -73,6 +73,19 @@ def test_constants_match_oracle(case):
         assert ctx.table(which).tobytes() == c[k].tobytes(), k
 
 
+def test_context_from_params(case):
+    """a context from the params.h text of the same set has the same tables"""
+    import grns_gb300 as G
+    from tests.test_params import params_text
+    tag, ctx, orc, g = case
+    other = G.RNSContext.from_params(params_text(orc.moduli))
+    for which in range(12):
+        assert other.table(which).tobytes() == ctx.table(which).tobytes(), which
+    other.close()
+    with pytest.raises(G.GrnsError):
+        G.RNSContext.from_params(params_text(orc.moduli, log2=orc.log2M + 1))
+
+
 @pytest.mark.parametrize("layout", ["soa", "aos"])
 def test_eval_golden(case, layout):
     tag, ctx, orc, g = case

@@ -1,0 +1,76 @@
+"""CPU: moduli sets in the reference's params.h format (src/params.h:11-39 and
+the src/params/ catalogue) through grns_params_parse."""
+import pytest
+
+import grns_gb300 as G
+from grns_gb300 import build
+from tests.helpers import TAGS, moduli_for
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    build.build()
+
+
+def params_text(moduli, log2=None, threshold=30, error="0.0000001", per_line=8):
+    """a params file in the reference's layout: guard, defines, continuation lines"""
+    M = 1
+    for m in moduli:
+        M *= m
+    rows = [",".join(str(m) for m in moduli[k:k + per_line]) for k in range(0, len(moduli), per_line)]
+    vals = ", \\\n                          ".join(rows)
+    return f"""/*
+ *  The set of RNS moduli and other parameters
+ */
+#ifndef GRNS_PARAMS_H
+#define GRNS_PARAMS_H
+
+#define RNS_MODULI_SIZE ({len(moduli)})
+
+#define RNS_MODULI_PRODUCT_LOG2 ({M.bit_length() - 1 if log2 is None else log2})  // floor(log2 M)
+
+#define RNS_P2_SCALING_THRESHOLD ({threshold})
+
+#define RNS_EVAL_RELATIVE_ERROR ({error})
+
+#define RNS_MODULI_VALUES {{{vals}}}
+
+constexpr int RNS_MODULI[RNS_MODULI_SIZE] = RNS_MODULI_VALUES;
+
+#define EMPLOY_STD_FMA false
+
+#endif  //GRNS_PARAMS_H
+"""
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_parse_round_trip(tag):
+    mods = moduli_for(tag)
+    M = 1
+    for m in mods:
+        M *= m
+    got, lg = G.parse_params(params_text(mods))
+    assert got == mods and lg == M.bit_length() - 1
+
+
+def test_parse_without_optional_defines():
+    text = "#define RNS_MODULI_SIZE 4\n#define RNS_MODULI_VALUES { 3, 5, 7, 11 }\n"
+    assert G.parse_params(text) == ([3, 5, 7, 11], None)
+
+
+@pytest.mark.parametrize("bad,status", [
+    ("#define RNS_MODULI_SIZE (4)\n#define RNS_MODULI_VALUES {3,5,7}\n", 1),        # count differs
+    ("#define RNS_MODULI_VALUES {3,5,7,11}\n", 1),                                     # no size
+    ("#define RNS_MODULI_SIZE (4)\n#define RNS_MODULI_VALUES {3,5,x,11}\n", 1),        # not a number
+    (params_text([3, 5, 7, 11], threshold=31), 2),                                     # other scaling step
+    (params_text([3, 5, 7, 11], error="0.000001"), 2),                                 # other error bound
+])
+def test_parse_rejects(bad, status):
+    with pytest.raises(G.GrnsError) as e:
+        G.parse_params(bad)
+    assert e.value.status == status
+
+
+def test_commented_out_definitions_are_ignored():
+    text = params_text([3, 5, 7, 11]) + "/* #define RNS_MODULI_SIZE (8) */\n// #define RNS_MODULI_VALUES {1}\n"
+    assert G.parse_params(text)[0] == [3, 5, 7, 11]
