@@ -13,6 +13,7 @@ whole device arrays through the C ABI of libgrns_gb300.so.
     z   = ctx.mpint_add(a, b) / mpint_sub / mpint_mul / mpint_div
                                               (src/mpint.cuh:336/:407/:478/:511)
     v,i = ctx.rns_max(x)                      # cuda::rns_max           (src/dpp/rnsmax.cuh:129)
+    a   = ctx.mrc(x)                          # cuda::mrc               (src/mrc.cuh:101)
     x   = ctx.rns_from_binary(limbs) / w = ctx.rns_to_binary(x)
                                               # rns_from_binary / rns_to_binary (src/rnsbase.cuh:253/:277)
     m   = ctx.mpint_set_binary(limbs, signs) / w,s = ctx.mpint_get_binary(m)
@@ -299,6 +300,15 @@ class RNSContext:
     def mpint_div(self, x, y, flags=None, stream=None):
         """Euclidean quotient x / y (cuda::mpint_div, src/mpint.cuh:511)."""
         return self._mpint(native.lib().grns_mpint_div, x, y, flags, stream)
+
+    def mrc(self, x, layout="soa", flags=None, stream=None):
+        """mixed-radix digits of each number, in the layout of x (cuda::mrc, src/mrc.cuh:101)"""
+        import torch
+        count = self._count(x, layout)
+        out = torch.empty_like(x)
+        check(native.lib().grns_mrc(self._h, _ptr(x), count, LAYOUTS[layout], _ptr(out), _ptr(flags),
+                                    _stream(stream)), "grns_mrc")
+        return out
 
     # ---- binary <-> RNS conversion ----
     @property

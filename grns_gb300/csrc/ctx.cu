@@ -225,6 +225,10 @@ grns_status grns_ctx_create_from_params(const char *text, grns_ctx **out) {
 
 grns_status grns_ctx_destroy(grns_ctx *c) {
     if (!c) return GRNS_ERR_INVALID_ARGUMENT;
+    for (auto &p : c->pipe_idle) {
+        for (cudaStream_t s : p.s) cudaStreamDestroy(s);
+        cudaEventDestroy(p.done);
+    }
     if (c->d_tables) cudaFree(c->d_tables);
     if (c->pool) cudaMemPoolDestroy(c->pool);  // released once outstanding scratch is freed
     delete c;

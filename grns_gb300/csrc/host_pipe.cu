@@ -3,9 +3,12 @@
  * memory, split into chunks so that the host->device copies of chunk j+1 and
  * the device->host copies of chunk j-1 overlap the kernels of chunk j.
  *
- * Three internal streams per call (copy in, compute, copy out; the two copy
- * directions run at the same time on the link), two device buffer slots used
- * in turn, events between them; the caller's stream waits for the last copy.
+ * Internal streams per call: copy in, copy out (the two directions run at the
+ * same time on the link) and one compute stream per device buffer slot (two
+ * slots used in turn), with events between them; the caller's stream waits
+ * for all of them.  Each chunk's kernel is launched with at least 64 numbers
+ * per warp, which keeps the warps balanced on short chunks and leaves SMs to
+ * the other slot's kernel.  The context keeps idle stream sets for later calls.
  * The call is stream-ordered like the device-pointer entry points: results are
  * in host memory once the caller's stream reaches that point.  Copies overlap
  * only for page-locked host buffers (cudaHostAlloc / cudaHostRegister); with
@@ -73,9 +76,25 @@ grns_status pipeline(const grns_ctx *c, int64_t count, int chunks, const std::ve
     cudaError_t err = scratch_alloc(c, (void **)&buf, slot_bytes * slots, user);
     if (err != cudaSuccess) return cuda_status(err);
 
-    cudaStream_t st[3] = {nullptr, nullptr, nullptr};  // copy in, compute, copy out
-    for (auto &s : st)
-        if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    /* a triple whose earlier calls have all ended (so concurrent calls on other
+     * streams do not queue behind each other), else new streams */
+    grns_ctx *cm = const_cast<grns_ctx *>(c);
+    grns_ctx::PipeStreams ps = {{nullptr, nullptr, nullptr, nullptr}, nullptr};
+    if (cudaPeekAtLastError() == cudaSuccess) {  // never hide an error the caller has not read
+        std::lock_guard<std::mutex> lock(cm->pipe_mu);
+        for (size_t k = 0; k < cm->pipe_idle.size(); k++) {
+            if (cudaEventQuery(cm->pipe_idle[k].done) == cudaSuccess) {
+                ps = cm->pipe_idle[k];
+                cm->pipe_idle.erase(cm->pipe_idle.begin() + k);
+                break;
+            }
+        }
+        cudaGetLastError();  // a cudaErrorNotReady of the queries is not an error
+    }
+    cudaStream_t *st = ps.s;  // copy in, copy out, compute of slot 0, compute of slot 1
+    for (int k = 0; k < 4; k++)
+        if (!st[k] && err == cudaSuccess) err = cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking);
+    if (!ps.done && err == cudaSuccess) err = cudaEventCreateWithFlags(&ps.done, cudaEventDisableTiming);
     std::vector<cudaEvent_t> ev(3 * chunks + 1, nullptr);
     for (auto &e : ev)
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
@@ -83,8 +102,8 @@ grns_status pipeline(const grns_ctx *c, int64_t count, int chunks, const std::ve
     grns_status status = GRNS_OK;
     if (err == cudaSuccess) {
         err = cudaEventRecord(start, user);  // orders the scratch allocation before the copies
-        for (auto &s : st)
-            if (err == cudaSuccess) err = cudaStreamWaitEvent(s, start, 0);
+        for (int k = 0; k < 4; k++)
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(st[k], start, 0);
     }
     for (int j = 0; j < chunks && err == cudaSuccess && status == GRNS_OK; j++) {
         const int64_t k0 = (int64_t)j * per, len = count - k0 < per ? count - k0 : per;
@@ -92,31 +111,52 @@ grns_status pipeline(const grns_ctx *c, int64_t count, int chunks, const std::ve
         cudaEvent_t e_in = ev[3 * j], e_comp = ev[3 * j + 1], e_out = ev[3 * j + 2];
         if (j >= slots) err = cudaStreamWaitEvent(st[0], ev[3 * (j - slots) + 1], 0);  // inputs consumed
         for (size_t a = 0; a < in.size(); a++) copy_chunk(in[a], slot + off_in[a], count, k0, len, true, st[0], err);
+        cudaStream_t comp = st[2 + j % slots];  // chunks of the two slots may compute at the same time
         if (err == cudaSuccess) err = cudaEventRecord(e_in, st[0]);
-        if (err == cudaSuccess) err = cudaStreamWaitEvent(st[1], e_in, 0);
-        if (err == cudaSuccess && j >= slots) err = cudaStreamWaitEvent(st[1], ev[3 * (j - slots) + 2], 0);  // outputs read
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(comp, e_in, 0);
+        if (err == cudaSuccess && j >= slots) err = cudaStreamWaitEvent(comp, ev[3 * (j - slots) + 2], 0);  // outputs read
         if (err != cudaSuccess) break;
         std::vector<void *> din(in.size()), dout(out.size());
         for (size_t a = 0; a < in.size(); a++) din[a] = slot + off_in[a];
         for (size_t a = 0; a < out.size(); a++) dout[a] = slot + off_out[a];
-        status = launch(din, dout, len, st[1]);
+        status = launch(din, dout, len, comp);
         if (status != GRNS_OK) break;
-        err = cudaEventRecord(e_comp, st[1]);
-        if (err == cudaSuccess) err = cudaStreamWaitEvent(st[2], e_comp, 0);
+        err = cudaEventRecord(e_comp, comp);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(st[1], e_comp, 0);
         for (size_t a = 0; a < out.size(); a++)
-            copy_chunk(out[a], slot + off_out[a], count, k0, len, false, st[2], err);
-        if (err == cudaSuccess) err = cudaEventRecord(e_out, st[2]);
+            copy_chunk(out[a], slot + off_out[a], count, k0, len, false, st[1], err);
+        if (err == cudaSuccess) err = cudaEventRecord(e_out, st[1]);
     }
-    /* join: the caller's stream waits for every internal stream, then frees the slots */
-    for (auto &s : st) {
-        if (!s) continue;
+    /* join: the caller's stream waits for every internal stream, then frees the
+     * slots; the streams go back to the context (work queued on them later
+     * runs after this call's, which keeps the order without waiting here) */
+    bool joined = ps.done != nullptr;
+    for (int k = 0; k < 4; k++) {
+        if (!st[k]) {
+            joined = false;
+            continue;
+        }
         cudaEvent_t done = nullptr;
         if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess) {
-            cudaEventRecord(done, s);
-            cudaStreamWaitEvent(user, done, 0);
+            joined &= cudaEventRecord(done, st[k]) == cudaSuccess && cudaStreamWaitEvent(user, done, 0) == cudaSuccess;
             cudaEventDestroy(done);
+        } else {
+            joined = false;
         }
-        cudaStreamDestroy(s);  // released once its work completes
+    }
+    if (joined) joined = cudaEventRecord(ps.done, user) == cudaSuccess;
+    bool kept = false;
+    if (joined) {
+        std::lock_guard<std::mutex> lock(cm->pipe_mu);
+        if (cm->pipe_idle.size() < 8) {
+            cm->pipe_idle.push_back(ps);
+            kept = true;
+        }
+    }
+    if (!kept) {
+        for (int k = 0; k < 4; k++)
+            if (st[k]) cudaStreamDestroy(st[k]);  // released once its work completes
+        if (ps.done) cudaEventDestroy(ps.done);
     }
     for (auto &e : ev)
         if (e) cudaEventDestroy(e);
@@ -126,6 +166,8 @@ grns_status pipeline(const grns_ctx *c, int64_t count, int chunks, const std::ve
 }
 
 bool layout_ok(int layout) { return layout == GRNS_LAYOUT_SOA || layout == GRNS_LAYOUT_AOS; }
+
+constexpr int kChunkPerWarp = 64;
 
 }  // namespace
 }  // namespace grns
@@ -148,7 +190,7 @@ grns_status grns_div_host(grns_ctx *c, const int32_t *x, const int32_t *d, int64
                     [&](const std::vector<void *> &di, const std::vector<void *> &dout, int64_t len, cudaStream_t s) {
                         return launch_div(c, (const uint32_t *)di[0], (const uint32_t *)di[1], soa ? len : 0, len,
                                           (uint32_t *)dout[0], (uint32_t *)dout[1],
-                                          has_flags ? (uint8_t *)dout[2] : nullptr, s);
+                                          has_flags ? (uint8_t *)dout[2] : nullptr, s, kChunkPerWarp);
                     });
 }
 
@@ -165,11 +207,11 @@ grns_status grns_scale2pow_host(grns_ctx *c, const int32_t *x, const uint32_t *D
     std::vector<HostArr> outs = {{(void *)out, soa, c->n, rec}};
     if (flags) outs.push_back({(void *)flags, false, 1, 1});
     const bool has_D = D != nullptr, has_flags = flags != nullptr;
-    return pipeline(c, count, chunks ? chunks : auto_chunks(count, 1 << 16), in, outs, (cudaStream_t)stream,
+    return pipeline(c, count, chunks ? chunks : auto_chunks(count, 1 << 17), in, outs, (cudaStream_t)stream,
                     [&](const std::vector<void *> &di, const std::vector<void *> &dout, int64_t len, cudaStream_t s) {
                         return launch_scale2pow(c, (const uint32_t *)di[0], has_D ? (const uint32_t *)di[1] : nullptr,
                                                 D_uniform, soa ? len : 0, len, (uint32_t *)dout[0],
-                                                has_flags ? (uint8_t *)dout[1] : nullptr, s);
+                                                has_flags ? (uint8_t *)dout[1] : nullptr, s, kChunkPerWarp);
                     });
 }
 

@@ -35,6 +35,15 @@ struct grns_ctx {
     cudaMemPool_t pool = nullptr;
     /* batched-kernel schedule per grns_op (eval, cmp, div, scale2pow, max, mp_int add/sub/mul) */
     grns::Sched sched[8] = {{0, 256}, {0, 1024}, {0, 256}, {0, 256}, {0, 1024}, {0, 256}, {0, 256}, {0, 256}};
+    /* idle stream sets of the host-buffer forms (copy in, copy out, one compute
+     * stream per buffer slot), each with an event that completes once the
+     * set's last call has ended */
+    struct PipeStreams {
+        cudaStream_t s[4];
+        cudaEvent_t done;
+    };
+    std::mutex pipe_mu;
+    std::vector<PipeStreams> pipe_idle;
     /* kernel constant block for this n (a grns::Consts<n>) */
     alignas(16) unsigned char consts[sizeof(grns::Consts<grns::kMaxModuli>)];
 };
@@ -76,10 +85,14 @@ grns_status launch_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_
                         uint8_t *flags, cudaStream_t s);
 grns_status launch_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, int64_t ld, int64_t count,
                        int32_t *out, uint8_t *flags, cudaStream_t s);
+/* min_per_warp > 0 launches fewer warps when that gives each warp at least
+ * min_per_warp numbers (better balance inside a warp's range; the kernel then
+ * leaves SMs free for a concurrent launch) */
 grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
-                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s);
+                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp = 0);
 grns_status launch_scale2pow(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t D_uniform,
-                             int64_t ld, int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s);
+                             int64_t ld, int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s,
+                             int min_per_warp = 0);
 grns_status launch_mpint(const grns_ctx *c, int op, const void *x, const void *y, int64_t count, void *out,
                          uint8_t *flags, cudaStream_t s);
 grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out_value,

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N>
 
 template <int N>
 static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
-                           uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s) {
+                           uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
         k_div<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
@@ -140,6 +140,8 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
     }
     const int64_t warps_cap = (int64_t)c->sm_count * occ * (kDivBlock / 32);
     int64_t warps = (count + 31) / 32;
+    if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)
+        warps = (count + min_per_warp - 1) / min_per_warp;
     if (warps > warps_cap) warps = warps_cap;
     if (warps < 1) warps = 1;
     const int64_t per_warp = (count + warps - 1) / warps;
@@ -160,7 +162,7 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
 
 template <int N>
 static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
-                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s) {
+                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
         k_scale<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
@@ -182,6 +184,8 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
     }
     const int64_t warps_cap = (int64_t)c->sm_count * occ * (kDivBlock / 32);
     int64_t warps = (count + 31) / 32;
+    if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)
+        warps = (count + min_per_warp - 1) / min_per_warp;
     if (warps > warps_cap) warps = warps_cap;
     if (warps < 1) warps = 1;
     const int64_t per_warp = (count + warps - 1) / warps;
@@ -198,15 +202,15 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
 }
 
 grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
-                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s) {
-#define C_(n) return run_div<n>(c, x, d, ld, count, q, r, flags, s)
+                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp) {
+#define C_(n) return run_div<n>(c, x, d, ld, count, q, r, flags, s, min_per_warp)
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }
 
 grns_status launch_scale2pow(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
-                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s) {
-#define C_(n) return run_scale<n>(c, x, D, Du, ld, count, out, flags, s)
+                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp) {
+#define C_(n) return run_scale<n>(c, x, D, Du, ld, count, out, flags, s, min_per_warp)
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }

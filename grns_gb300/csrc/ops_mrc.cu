@@ -1,0 +1,80 @@
+/*
+ * grns_gb300 -- mixed-radix conversion over arrays (cuda::mrc, reference
+ * src/mrc.cuh:101; Szabo-Tanaka digits: X = a_0 + a_1 m_0 + a_2 m_0 m_1 + ...).
+ *
+ * One thread per number.  The digit loops are uniform across a warp (the
+ * modulus i and the earlier digit j are the same on every lane), so the
+ * constants m_j^-1 mod m_i with their Shoup companions sit in a per-block
+ * shared table read as broadcasts, and each thread keeps its digits in a
+ * shared-memory column; the loops stay rolled (n^2 / 2 steps would not fit
+ * the instruction cache unrolled).  Digits are canonical (the reference's
+ * mod_psub can return a negative digit for descending moduli, a case of
+ * probability ~1e-13 on such sets).
+ */
+#include "internal.h"
+#include "rns_device.cuh"
+
+namespace grns {
+
+constexpr int kMrcBlock = 128;
+
+template <int N>
+__global__ void __launch_bounds__(kMrcBlock) k_mrc(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+                                                   Output<N> out, uint8_t *__restrict__ flags) {
+    extern __shared__ uint2 mrc_smem[];
+    uint2 *inv = mrc_smem;  // [j * N + i] = (m_j^-1 mod m_i, Shoup companion), j < i
+    uint32_t *col = reinterpret_cast<uint32_t *>(inv + N * N) + threadIdx.x;
+    for (int w = threadIdx.x; w < N * N; w += blockDim.x) inv[w] = make_uint2(C.mrc_inv[w], C.mrc_inv_sh[w]);
+    __syncthreads();
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t bad = 0;
+#pragma unroll 1
+        for (int i = 0; i < N; i++) {
+            const uint32_t m = C.m[i], b = C.b[i], mu = C.mu[i];
+            uint32_t v = x.load(k, i);
+            bad |= (uint32_t)(v >= m);
+#pragma unroll 4
+            for (int j = 0; j < i; j++) {
+                uint32_t t = col[j * kMrcBlock];
+                if (C.m[j] > m) t = b >= 16 ? mulmod_barrett(t, 1u, m, mu, b) : t % m;  // digit j below m_j
+                const uint2 c = inv[j * N + i];
+                v = mulmod_shoup(submod(v, t, m), c.x, c.y, m);
+            }
+            col[i * kMrcBlock] = v;
+        }
+#pragma unroll 4
+        for (int i = 0; i < N; i++) out.store(k, i, bad ? 0u : col[i * kMrcBlock]);
+        if (flags) flags[k] = bad ? (uint8_t)kFlagInvalidInput : (uint8_t)0;
+    }
+}
+
+template <int N>
+static grns_status run_mrc(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out,
+                           uint8_t *flags, cudaStream_t s) {
+    const size_t smem = (size_t)N * N * sizeof(uint2) + (size_t)N * kMrcBlock * 4;
+    static int per_sm[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident blocks per SM, per device
+    int &occ = per_sm[c->device & 7];
+    if (occ == 0) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_mrc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_mrc<N>, kMrcBlock, smem) != cudaSuccess || nb < 1)
+            nb = 1;
+        occ = nb;
+    }
+    k_mrc<N><<<grid_for(c, count, kMrcBlock, occ), kMrcBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
+                                                                          Output<N>{out, ld}, flags);
+    return cuda_status(cudaGetLastError());
+}
+
+}  // namespace grns
+
+extern "C" grns_status grns_mrc(grns_ctx *c, const int32_t *x, int64_t count, int layout, int32_t *out,
+                                uint8_t *flags, void *stream) {
+    if (!c || count < 0 || (layout != GRNS_LAYOUT_SOA && layout != GRNS_LAYOUT_AOS)) return GRNS_ERR_INVALID_ARGUMENT;
+    if (count == 0) return GRNS_OK;
+    if (!x || !out) return GRNS_ERR_INVALID_ARGUMENT;
+    const int64_t ld = layout == GRNS_LAYOUT_SOA ? count : 0;
+#define C_(n) return grns::run_mrc<n>(c, (const uint32_t *)x, ld, count, (uint32_t *)out, flags, (cudaStream_t)stream)
+    GRNS_DISPATCH_N(c->n, C_)
+#undef C_
+}

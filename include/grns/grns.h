@@ -183,6 +183,14 @@ grns_status grns_mpint_mul(grns_ctx *ctx, const void *x, const void *y, int64_t 
 grns_status grns_mpint_div(grns_ctx *ctx, const void *x, const void *y, int64_t count, void *out,
                            uint8_t *flags, void *stream);
 
+/* ---- mixed-radix conversion ----
+ * out = the Szabo-Tanaka mixed-radix digits of each number (X = a_0 + a_1 m_0
+ * + a_2 m_0 m_1 + ...), as cuda::mrc (reference src/mrc.cuh:101), in the
+ * layout of x; digits canonical in [0, m_i).  A residue >= its modulus sets
+ * GRNS_FLAG_INVALID_INPUT and gives zero digits. */
+grns_status grns_mrc(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, int32_t *out, uint8_t *flags,
+                     void *stream);
+
 /* ---- binary <-> RNS conversion ----
  * Binary integers are number-major rows of `limbs` little-endian 32-bit
  * words (word l of number k at words[k * limbs + l]; GMP's

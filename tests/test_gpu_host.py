@@ -34,7 +34,7 @@ def test_div_host(case, layout, pinned, chunks):
     ctx, orc = case
     N = 20001
     x = W.uniform_residues(orc.moduli, N, seed=3, stream=W.S_X, layout="aos")
-    d = W.divisors(orc.moduli, orc.log2M, N, seed=3, layout="aos")
+    d, _ = W.divisors(orc.moduli, orc.log2M, N, seed=3, layout="aos")
     d[5] = 0  # a zero divisor: flagged, q = 0, r = x
     hx, hd = host(x, layout, pinned), host(d, layout, pinned)
     flags = torch.zeros(N, dtype=torch.uint8, pin_memory=pinned)

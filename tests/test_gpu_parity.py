@@ -270,6 +270,32 @@ def test_mpint_div_by_zero(case):
     assert _signed(orc, got[2:]) == [1]
 
 
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_mrc(case, layout):
+    """mixed-radix digits, cuda::mrc (src/mrc.cuh:101)"""
+    tag, ctx, orc, g = case
+    got = from_dev(ctx.mrc(to_dev(g["x"], layout), layout=layout), layout)
+    assert np.array_equal(got, g["mrc_dev"])
+    N = 5000 if orc.n <= 16 else 1500
+    x = W.uniform_residues(orc.moduli, N, seed=41, stream=W.S_X, layout="aos")
+    x[:3] = orc.exact.to_rns([0, 1, orc.M - 1])
+    x[3, 1] = orc.moduli[1]  # invalid residue
+    flags = flags_buf(N)
+    got = from_dev(ctx.mrc(to_dev(x, layout), layout=layout, flags=flags), layout)
+    f = flags.cpu().numpy()
+    assert f[3] == 1 and not got[3].any() and int(f.sum()) == 1
+    ok = np.arange(N) != 3
+    assert np.array_equal(got[ok], orc.mrc(x[ok], path=O.PATH_DEVICE))
+    # digits recompose X
+    X = orc.exact.from_rns(x[ok][:200])
+    for row, v in zip(got[ok][:200], X):
+        acc, w = 0, 1
+        for a, m in zip(row, orc.moduli):
+            acc += int(a) * w
+            w *= m
+        assert acc == v
+
+
 def test_mpint_overflow_flag(case):
     tag, ctx, orc, g = case
     big = orc.M // 2 + 12345
