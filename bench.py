@@ -122,13 +122,22 @@ def dist_setup(ngpus):
 
 
 def barrier_max(value, world):
+    """the maximum of `value` over the ranks (NCCL on GPUs; gloo on the CPU)"""
     import torch
     if world == 1:
         return value
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate(per_rank_ms, count_per_rank, world):
+    """(ms per step, whole-job Mnum/s): every rank processed count_per_rank
+    numbers per step (weak scaling); the job takes the slowest rank's time"""
+    ms = barrier_max(per_rank_ms, world)
+    return ms, world * count_per_rank / (ms * 1e-3) / 1e6
 
 
 def cpu_baseline(threads=None, sample=4096):
@@ -726,10 +735,8 @@ def main():
             if i >= args.warmup:
                 e2e_ms.append(a.elapsed_time(b))
         e2e_ok = torch.equal(hq, q.cpu()) and torch.equal(hr, r.cpu()) and torch.equal(hso, so.cpu())
-    total_ms = barrier_max(sum(step_ms), world)
-    ms = total_ms / args.steps
-    value = world * 2 * PAIRS / (ms * 1e-3) / 1e6
-    e2e = world * 2 * PAIRS / (barrier_max(sum(e2e_ms), world) / args.steps * 1e-3) / 1e6
+    ms, value = aggregate(sum(step_ms) / args.steps, 2 * PAIRS, world)
+    _, e2e = aggregate(sum(e2e_ms) / args.steps, 2 * PAIRS, world)
     h2d = 4 * (x.numel() * 3 + D.numel())
     d2h = 4 * x.numel() * 3
     del hx, hd, hxs, hD, hq, hr, hso

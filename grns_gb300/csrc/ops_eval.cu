@@ -24,6 +24,47 @@ __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> 
     }
 }
 
+/* the same, with the next number's residues loaded into registers while the
+ * current one is evaluated (the common path is latency-bound on its loads
+ * otherwise); the rare branch re-reads its residues from memory */
+template <int N>
+__global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Consts<N> C, Operand<N> x,
+                                                      int64_t count, Er *__restrict__ out,
+                                                      uint8_t *__restrict__ flags) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t cur[N];
+    if (k < count) {
+#pragma unroll
+        for (int i = 0; i < N; i++) cur[i] = x.load(k, i);
+    }
+    for (; k < count; k += stride) {
+        uint32_t nxt[N];
+        const int64_t kn = k + stride;
+        if (kn < count) {
+#pragma unroll
+            for (int i = 0; i < N; i++) nxt[i] = x.load(kn, i);
+        }
+        uint32_t f = 0, bad = 0;
+        Er lo, up;
+        const int st = eval_int<N>(C, [&](int i) { return cur[i]; }, lo, up, bad);
+        if (bad) {
+            f = kFlagInvalidInput;
+            lo = up = Er{0.0, 0};
+        } else if (st == kEvalZero) {
+            lo = up = Er{0.0, 0};
+        } else if (st == kEvalRare) {
+            const int64_t kk = k;
+            eval_full<N>(C, [&](int i) { return x.load(kk, i); }, lo, up, f);
+        }
+        out[2 * k] = lo;
+        out[2 * k + 1] = up;
+        if (flags) flags[k] = (uint8_t)f;
+#pragma unroll
+        for (int i = 0; i < N; i++) cur[i] = nxt[i];
+    }
+}
+
 /* one-ulp enclosure where certified (rns_fast.cuh eval_tight), the
  * bit-exact evaluation otherwise (noinline: rare for uniform X) */
 template <int N>
@@ -222,7 +263,11 @@ template <int N>
 static grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                             uint8_t *flags, cudaStream_t s) {
     const int B = 256;
-    k_eval<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out, flags);
+    if (N <= 32)
+        k_eval_pipe<N><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
+                                                             flags);
+    else
+        k_eval<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out, flags);
     return cuda_status(cudaGetLastError());
 }
 
