@@ -130,6 +130,7 @@ const char *grns_status_string(grns_status s) {
         case GRNS_ERR_REJECTED: return "rejected by admission control";
         case GRNS_ERR_BUSY: return "busy";
         case GRNS_ERR_TOO_LARGE: return "request exceeds a fixed capacity";
+        case GRNS_ERR_CANCELLED: return "cancelled";
     }
     return "unknown status";
 }

@@ -31,7 +31,14 @@
 
 namespace grns {
 
-constexpr int kDivRefill = 8;
+#ifndef GRNS_DIV_REFILL
+#define GRNS_DIV_REFILL 8
+#endif
+#ifndef GRNS_DIV_GROUP
+#define GRNS_DIV_GROUP 4
+#endif
+constexpr int kDivRefill = GRNS_DIV_REFILL;
+constexpr int kDivGroup = GRNS_DIV_GROUP;  // residues per load / arithmetic / store group of a digit step
 constexpr int kDivPrefetch = 64;  // pass A prefetches the operands this many numbers ahead
 
 /* per-modulus constants of the division loops (shared memory, one per modulus) */
@@ -101,21 +108,22 @@ struct Fx96 {
 
 constexpr int kDivUnroll = 4;
 
-/* pass A over [begin, end): rec[k] = record of number k.  Column rows: the
- * working value in rows [0, N), the dividend in rows [2N, 3N). */
-template <int N>
+/* pass A over the numbers claim() hands out below end: rec[k] = record of
+ * number k.  Column rows: the working value in rows [0, N), the dividend in
+ * rows [N, 2N). */
+template <int N, class Claim>
 __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
-                                              const Operand<N> &d, uint2 *rec, int64_t begin, int64_t end,
-                                              uint32_t *col, int stride) {
+                                              const Operand<N> &d, uint2 *rec, int64_t end, Claim claim,
+                                              int64_t prefetch, uint32_t *col, int stride) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     enum { Idle, ChainD, ChainX, Done, Dead };
     uint32_t *__restrict__ W = col;
-    uint32_t *__restrict__ X = col + 2 * N * stride;
+    uint32_t *__restrict__ X = col + N * stride;
     int ph = Idle, k = 0, guard = 0, s = 0;
     bool xz = false;
-    int64_t idx = 0, next = begin;
+    int64_t idx = 0;
     uint2 out = make_uint2(0, 0);
     for (;;) {
         const unsigned lv = __ballot_sync(FULL, ph == ChainD || ph == ChainX);
@@ -126,12 +134,11 @@ __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C,
                 ph = Idle;
             }
             const unsigned need = __ballot_sync(FULL, ph == Idle);
-            const int64_t my = next + __popc(need & lt);
-            next += __popc(need);
+            const int64_t my = claim(__popc(need)) + __popc(need & lt);
             if (ph == Idle) {
-                if (my + kDivPrefetch < end) {  // the numbers this lane will take next, into L2
-                    d.prefetch_l2(my + kDivPrefetch);
-                    x.prefetch_l2(my + kDivPrefetch);
+                if (my + prefetch < end) {  // numbers taken a little later, into L2
+                    d.prefetch_l2(my + prefetch);
+                    x.prefetch_l2(my + prefetch);
                 }
                 if (my < end) {
                     idx = my;
@@ -219,11 +226,12 @@ __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C,
 /* pass B over [begin, end) with the records of pass A, numbers taken in the
  * order of div_order.  Column rows: R in [0, N), the scaled divisor D in
  * [N, 2N), the quotient Q in [2N, 3N). */
-template <int N>
+template <int N, class Claim>
 __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
                                               const Operand<N> &d, const uint2 *rec, const int32_t *order,
                                               const Output<N> &qo, const Output<N> &ro, uint8_t *flags,
-                                              int64_t begin, int64_t end, uint32_t *col, int stride) {
+                                              int64_t begin, int64_t end, Claim claim, uint32_t *col,
+                                              int stride) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -238,7 +246,7 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
     st.b = kDivB;
     u128 U = 0;
     int ph = Idle;
-    int64_t idx = 0, next = begin;
+    int64_t idx = 0;
 
     for (;;) {
         const unsigned lv = __ballot_sync(FULL, ph == Iter);
@@ -274,8 +282,7 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
                 ph = Idle;
             }
             const unsigned need = __ballot_sync(FULL, ph == Idle);
-            const int64_t my = next + __popc(need & lt);
-            next += __popc(need);
+            const int64_t my = claim(__popc(need)) + __popc(need & lt);
             if (ph == Idle) {
                 if (my < end) {
                     idx = begin + order[my];
@@ -348,17 +355,18 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
         const bool live = ph == Iter;
         const uint64_t qd = live ? dv_digit(st, U, C.E, st.f) : 0;
         Fx96 fx;
+        constexpr int G = N % kDivGroup == 0 ? kDivGroup : 4;  // every supported N is a multiple of 4
 #pragma unroll 1
-        for (int i0 = 0; i0 < N; i0 += 4) {  // groups of 4: loads, arithmetic, stores
-            uint32_t rv[4], dv[4], qv[4];
+        for (int i0 = 0; i0 < N; i0 += G) {  // groups: loads, arithmetic, stores
+            uint32_t rv[G], dv[G], qv[G];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < G; j++) {
                 rv[j] = Rc[(i0 + j) * stride];
                 dv[j] = Dc[(i0 + j) * stride];
                 qv[j] = Qc[(i0 + j) * stride];
             }
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < G; j++) {
                 const DivK k = K[i0 + j];
                 const uint32_t m = k.a.x;
                 const uint32_t qi = kred53(qd, k);
@@ -368,7 +376,7 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
                 fx.add(rv[j], k);
             }
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < G; j++) {
                 Rc[(i0 + j) * stride] = rv[j];
                 if (live) Qc[(i0 + j) * stride] = qv[j];
             }
@@ -442,17 +450,46 @@ __device__ __forceinline__ void div_range(const DivK *K, const Consts<N> &C, con
                                           const Operand<N> &d, uint2 *rec, int32_t *order, const Output<N> &qo,
                                           const Output<N> &ro, uint8_t *flags, int64_t begin, int64_t end,
                                           uint32_t *col, int stride, uint32_t *hist) {
-    divnorm_range<N>(K, C, x, d, rec, begin, end, col, stride);
+    int64_t next = begin;
+    divnorm_range<N>(K, C, x, d, rec, end, [&](int c) { const int64_t b = next; next += c; return b; }, kDivPrefetch,
+                     col, stride);
     __syncwarp();  // records written by one lane are read by another
     div_order(rec, order, begin, end, hist);
-    divloop_range<N>(K, C, x, d, rec, order, qo, ro, flags, begin, end, col, stride);
+    int64_t pos = 0;  // order holds offsets from begin at positions begin..end-1
+    divloop_range<N>(K, C, x, d, rec, order + begin, qo, ro, flags, begin, end - begin,
+                     [&](int c) { const int64_t b = pos; pos += c; return b; }, col, stride);
 }
+
+/* a warp's claim of c consecutive positions from a grid-wide counter (all
+ * lanes call it with the same c; lane 0 does the atomic) */
+__device__ __forceinline__ int64_t warp_claim(unsigned long long *ctr, int c) {
+    unsigned long long b = 0;
+    if ((threadIdx.x & 31) == 0 && c > 0) b = atomicAdd(ctr, (unsigned long long)c);
+    return (int64_t)__shfl_sync(0xffffffffu, b, 0);
+}
+
+/* grid-wide form, in three launches (div_global_* below): pass A over numbers
+ * claimed from a counter, a counting sort of all numbers by decreasing step
+ * count, pass B over the sorted order claimed from a second counter -- the
+ * whole grid then works longest-first with no per-warp ranges to drain */
+struct DivGlobal {
+    unsigned long long ctr_a, ctr_b;
+    uint32_t hist[kDivBins];   // numbers per step count
+    uint32_t fill[kDivBins];   // positions taken per step count by the scatter
+};
 
 /* shared memory of a block of `threads` threads running div_range: the DivK
  * table, the warps' counters, then the columns */
 template <int N>
 constexpr size_t div_smem_bytes(int threads) {
     return sizeof(DivK) * N + (size_t)(threads / 32) * kDivBins * 4 + (size_t)3 * N * 4 * threads;
+}
+
+/* shared memory of a block of `threads` threads running pass A alone (two
+ * column rows per residue) */
+template <int N>
+constexpr size_t divnorm_smem_bytes(int threads) {
+    return sizeof(DivK) * N + (size_t)(threads / 32) * kDivBins * 4 + (size_t)2 * N * 4 * threads;
 }
 
 /* scratch bytes per number of the global pass-A records and the order */

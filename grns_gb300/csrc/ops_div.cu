@@ -2,9 +2,10 @@
  * grns_gb300 -- division and power-of-two scaling kernels.
  *   k_div      : q = floor(X/D), r = X - qD (reference src/rnsdiv.cuh:128),
  *                reference-faithful FP64 form, one thread per number
- *   k_div_warp : the same results on the integer fast path; each warp runs a
- *                contiguous range of numbers through the division state
- *                machine (div_warp.cuh)
+ *   k_div_a, k_div_hist, k_div_scatter, k_div_b : the same results on the
+ *                integer fast path (div_warp.cuh): pass A over the whole
+ *                grid, a counting sort of the numbers by step count, pass B
+ *                longest-first, numbers claimed from grid-wide counters
  *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
  */
 #include "div_warp.cuh"
@@ -47,28 +48,96 @@ constexpr int kDivBlock = 128;
 
 /* resident 128-thread blocks per SM the register budget must allow: shared
  * memory (3N words per thread) allows 4 at n <= 32 and 2 at n = 64 */
+#ifndef GRNS_DIV_MIN_BLOCKS
+#define GRNS_DIV_MIN_BLOCKS 4
+#endif
 template <int N>
 constexpr int div_min_blocks() {
-    return N > 32 ? 2 : 4;
+    return N > 32 ? 2 : GRNS_DIV_MIN_BLOCKS;
 }
 
+/* pass A of the grid-wide division: numbers claimed from G->ctr_a, records
+ * into rec */
 template <int N>
-__global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
-    k_div_warp(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
-               int32_t *__restrict__ order, int64_t count, int64_t per_warp, Output<N> q, Output<N> r,
-               uint8_t *__restrict__ flags) {
+__global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
+    k_div_a(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
+            DivGlobal *__restrict__ G, int64_t count) {
     extern __shared__ uint4 div_smem[];
     DivK *K = reinterpret_cast<DivK *>(div_smem);
-    uint32_t *hist = reinterpret_cast<uint32_t *>(K + N);
-    uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
+    uint32_t *cols = reinterpret_cast<uint32_t *>(K + N) + (blockDim.x / 32) * kDivBins;  // layout of div_smem_bytes
     divk_fill<N>(C, K);
     __syncthreads();
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t b = w * per_warp;
-    if (b >= count) return;  // whole warp
-    const int64_t e = b + per_warp < count ? b + per_warp : count;
-    div_range<N>(K, C, x, d, rec, order, q, r, flags, b, e, cols + threadIdx.x, blockDim.x,
-                 hist + (threadIdx.x / 32) * kDivBins);
+    /* prefetch distance: one number per lane of the grid ahead, about what the
+     * grid claims while a number is normalised */
+    const int64_t lanes = (int64_t)gridDim.x * blockDim.x;
+    divnorm_range<N>(K, C, x, d, rec, count, [&](int c) { return warp_claim(&G->ctr_a, c); }, lanes,
+                     cols + threadIdx.x, blockDim.x);
+}
+
+/* the histogram of step counts over all records (G->hist) */
+__global__ void __launch_bounds__(256) k_div_hist(const uint2 *__restrict__ rec, DivGlobal *__restrict__ G,
+                                                  int64_t count) {
+    __shared__ uint32_t h[kDivBins];
+    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&h[dv_rec_steps(rec[k])], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&G->hist[i], h[i]);
+}
+
+/* order[p] = the numbers by decreasing step count (counting sort): each
+ * block takes a contiguous share, claims room in every bin with one atomic
+ * per bin, and places its numbers with shared-memory atomics */
+__global__ void __launch_bounds__(256) k_div_scatter(const uint2 *__restrict__ rec, DivGlobal *__restrict__ G,
+                                                     int32_t *__restrict__ order, int64_t count) {
+    __shared__ uint32_t base[kDivBins], local[kDivBins], slot[kDivBins];
+    const int64_t per = (count + gridDim.x - 1) / gridDim.x;
+    const int64_t b0 = (int64_t)blockIdx.x * per, b1 = b0 + per < count ? b0 + per : count;
+    if (threadIdx.x < 32) {  /* exclusive prefix over bins in decreasing order (lane l: bins 63 - l, 31 - l) */
+        const int lane = threadIdx.x;
+        const uint32_t h0 = G->hist[63 - lane], h1 = G->hist[31 - lane];
+        uint32_t s0 = h0, s1 = h1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t a0 = __shfl_up_sync(0xffffffffu, s0, o), a1 = __shfl_up_sync(0xffffffffu, s1, o);
+            if (lane >= o) {
+                s0 += a0;
+                s1 += a1;
+            }
+        }
+        s1 += __shfl_sync(0xffffffffu, s0, 31);
+        base[63 - lane] = s0 - h0;
+        base[31 - lane] = s1 - h1;
+    }
+    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x) local[i] = 0;
+    __syncthreads();
+    for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) atomicAdd(&local[dv_rec_steps(rec[k])], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x)
+        slot[i] = base[i] + (local[i] ? atomicAdd(&G->fill[i], local[i]) : 0u);
+    __syncthreads();
+    for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+        const uint32_t p = atomicAdd(&slot[dv_rec_steps(rec[k])], 1u);
+        order[p] = (int32_t)k;
+    }
+}
+
+/* pass B of the grid-wide division: positions of the sorted order claimed
+ * from G->ctr_b, longest divisions first */
+template <int N>
+__global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
+    k_div_b(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, const uint2 *__restrict__ rec,
+            const int32_t *__restrict__ order, DivGlobal *__restrict__ G, int64_t count, Output<N> q, Output<N> r,
+            uint8_t *__restrict__ flags) {
+    extern __shared__ uint4 div_smem[];
+    DivK *K = reinterpret_cast<DivK *>(div_smem);
+    uint32_t *cols = reinterpret_cast<uint32_t *>(K + N) + (blockDim.x / 32) * kDivBins;
+    divk_fill<N>(C, K);
+    __syncthreads();
+    divloop_range<N>(K, C, x, d, rec, order, q, r, flags, 0, count,
+                     [&](int c) { return warp_claim(&G->ctr_b, c); }, cols + threadIdx.x, blockDim.x);
 }
 
 template <int N>
@@ -125,37 +194,61 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
                                                                count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
         return cuda_status(cudaGetLastError());
     }
-    /* fast path: warps over contiguous ranges, as many warps as fit at once */
-    const size_t smem = div_smem_bytes<N>(kDivBlock);
-    static int per_sm[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident blocks per SM, per device
-    int &occ = per_sm[c->device & 7];
-    if (occ == 0) {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_div_warp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_div_warp<N>, kDivBlock, smem) != cudaSuccess ||
-            nb < 1)
+    /* fast path: pass A, a counting sort by step count, pass B (div_warp.cuh),
+     * each over the whole grid with numbers claimed from counters */
+    const size_t smem = div_smem_bytes<N>(kDivBlock), smem_a = divnorm_smem_bytes<N>(kDivBlock);
+    static int per_sm[8][2] = {};  // resident blocks per SM of k_div_a / k_div_b, per device
+    int *occ = per_sm[c->device & 7];
+    if (occ[0] == 0) {
+        if (smem_a > 48 * 1024) cudaFuncSetAttribute(k_div_a<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_div_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int na = 0, nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&na, k_div_a<N>, kDivBlock, smem_a) != cudaSuccess || na < 1)
+            na = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_div_b<N>, kDivBlock, smem) != cudaSuccess || nb < 1)
             nb = 1;
-        occ = nb;
+        occ[0] = na;
+        occ[1] = nb;
     }
-    const int64_t warps_cap = (int64_t)c->sm_count * occ * (kDivBlock / 32);
-    int64_t warps = (count + 31) / 32;
-    if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)
-        warps = (count + min_per_warp - 1) / min_per_warp;
-    if (warps > warps_cap) warps = warps_cap;
-    if (warps < 1) warps = 1;
-    const int64_t per_warp = (count + warps - 1) / warps;
-    const unsigned grid = (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
-    /* pass-A records and the longest-first order (12 bytes per number), stream-ordered */
+    /* warps: every resident one, fewer when a warp would get under min_per_warp
+     * numbers (or one per lane's worth) */
+    auto grid_of = [&](int o) {
+        int64_t warps = (count + 31) / 32;
+        if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)
+            warps = (count + min_per_warp - 1) / min_per_warp;
+        const int64_t cap = (int64_t)c->sm_count * o * (kDivBlock / 32);
+        if (warps > cap) warps = cap;
+        if (warps < 1) warps = 1;
+        return (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
+    };
+    /* scratch: records, order, the grid-wide counters */
     void *scratch = nullptr;
-    cudaError_t e = scratch_alloc(c, &scratch, (size_t)count * kDivScratchPerNumber, s);
+    const size_t rec_bytes = (size_t)count * sizeof(uint2), ord_bytes = ((size_t)count * 4 + 15) & ~(size_t)15;
+    cudaError_t e = scratch_alloc(c, &scratch, rec_bytes + ord_bytes + sizeof(DivGlobal), s);
     if (e != cudaSuccess) return cuda_status(e);
     uint2 *rec = (uint2 *)scratch;
-    int32_t *order = (int32_t *)(rec + count);
-    k_div_warp<N><<<grid, kDivBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld}, rec, order,
-                                                count, per_warp > 0 ? per_warp : 1, Output<N>{q, ld},
-                                                Output<N>{r, ld}, flags);
-    e = cudaGetLastError();
+    int32_t *order = (int32_t *)((char *)scratch + rec_bytes);
+    DivGlobal *G = (DivGlobal *)((char *)scratch + rec_bytes + ord_bytes);
+    e = cudaMemsetAsync(G, 0, sizeof(DivGlobal), s);
+    const Operand<N> X{x, ld}, Dv{d, ld};
+    if (e == cudaSuccess) {
+        k_div_a<N><<<grid_of(occ[0]), kDivBlock, smem_a, s>>>(consts_of<N>(c), X, Dv, rec, G, count);
+        e = cudaGetLastError();
+    }
+    const unsigned sgrid = grid_for(c, (count + 1023) / 1024, 1, 4);
+    if (e == cudaSuccess) {
+        k_div_hist<<<grid_for(c, count, 256, 4), 256, 0, s>>>(rec, G, count);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_div_scatter<<<sgrid, 256, 0, s>>>(rec, G, order, count);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_div_b<N><<<grid_of(occ[1]), kDivBlock, smem, s>>>(consts_of<N>(c), X, Dv, rec, order, G, count,
+                                                             Output<N>{q, ld}, Output<N>{r, ld}, flags);
+        e = cudaGetLastError();
+    }
     scratch_free(scratch, s);
     return cuda_status(e);
 }

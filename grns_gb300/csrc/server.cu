@@ -95,6 +95,7 @@ struct grns_server {
     std::vector<Slot *> slots;
     uint64_t next_handle = 1, next_req = 1;
     size_t in_use = 0;
+    size_t allocated = 0;  // bytes of live arrays (alloc_cap_bytes applies to it)
     cudaMemPool_t pool = nullptr;
     cudaStream_t copy = nullptr;
     int device = 0;
@@ -102,7 +103,7 @@ struct grns_server {
     std::thread worker;
     // stats
     std::vector<double> lat;
-    uint64_t completed = 0, rejected = 0, launches = 0, jobs_launched = 0;
+    uint64_t completed = 0, rejected = 0, cancelled = 0, launches = 0, jobs_launched = 0;
     double numbers = 0, t_first = 0, t_last = 0;
 };
 
@@ -124,8 +125,10 @@ grns_status alloc_array(grns_server *sv, cudaStream_t s, int ctx, int kind, int6
     const grns_ctx *c = sv->ctxs[ctx];
     size_t bytes = elem_bytes(kind, c->n) * (size_t)count;
     if (kind == GRNS_ARRAY_MAXOUT) bytes = ((4 * (size_t)c->n + 7) / 8) * 8 + 8;
+    if (sv->opt.alloc_cap_bytes && sv->allocated + bytes > sv->opt.alloc_cap_bytes) return GRNS_ERR_OUT_OF_MEMORY;
     cudaError_t e = cudaMallocFromPoolAsync(&a.p, bytes ? bytes : 16, sv->pool, s);
     if (e != cudaSuccess) return grns::cuda_status(e);
+    sv->allocated += bytes;
     a.ctx = ctx;
     a.kind = kind;
     a.count = count;
@@ -216,7 +219,10 @@ void schedule_locked(grns_server *sv) {
             }
             sv->pending.pop_front();
             if (st != GRNS_OK) {
-                if (o0.p) cudaFreeAsync(o0.p, sl->s);
+                if (o0.p) {
+                    cudaFreeAsync(o0.p, sl->s);
+                    sv->allocated -= std::min(sv->allocated, o0.bytes);
+                }
                 q.state = 2;
                 q.status = st;
                 q.t_done = now_us();
@@ -395,6 +401,7 @@ grns_status grns_server_put(grns_server *sv, int ctx, int kind, const void *src,
     if (e != cudaSuccess) {
         cudaFreeAsync(a.p, sv->copy);
         sv->in_use -= bytes;
+        sv->allocated -= std::min(sv->allocated, a.bytes);
         return grns::cuda_status(e);
     }
     *handle = sv->next_handle++;
@@ -438,6 +445,7 @@ grns_status grns_server_free(grns_server *sv, uint64_t h) {
     if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
     cudaFreeAsync(it->second.p, sv->copy);
     sv->in_use -= std::min(sv->in_use, it->second.bytes);
+    sv->allocated -= std::min(sv->allocated, it->second.bytes);
     for (auto &kv : sv->arrays)
         if (kv.second.eval == h) kv.second.eval = 0;
     sv->arrays.erase(it);
@@ -508,6 +516,24 @@ grns_status grns_server_wait(grns_server *sv, uint64_t id, int64_t timeout_us, i
     if (status) *status = q.status;
     if (out0) *out0 = q.out0;
     if (out1) *out1 = q.out1;
+    return GRNS_OK;
+}
+
+grns_status grns_server_cancel(grns_server *sv, uint64_t id) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return GRNS_ERR_INVALID_ARGUMENT;
+    Req &q = it->second;
+    if (q.state == 1) return GRNS_ERR_BUSY;
+    if (q.state == 2) return GRNS_OK;
+    auto pos = std::find(sv->pending.begin(), sv->pending.end(), id);
+    if (pos != sv->pending.end()) sv->pending.erase(pos);
+    q.state = 2;
+    q.status = GRNS_ERR_CANCELLED;
+    q.t_done = now_us();
+    sv->cancelled++;
+    sv->cv.notify_all();
     return GRNS_OK;
 }
 

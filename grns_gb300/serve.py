@@ -11,9 +11,9 @@ OPS = {"eval": 0, "cmp": 1, "div": 2, "scale2pow": 3, "max": 4, "mpint_add": 5, 
 
 
 class Server:
-    def __init__(self, budget_bytes=0, slots=4, max_jobs=256, admission_timeout_ms=0):
+    def __init__(self, budget_bytes=0, slots=4, max_jobs=256, admission_timeout_ms=0, alloc_cap_bytes=0):
         self.L = native.lib()
-        opt = native.ServerOptions(budget_bytes, slots, max_jobs, admission_timeout_ms, 0)
+        opt = native.ServerOptions(budget_bytes, slots, max_jobs, admission_timeout_ms, 0, alloc_cap_bytes)
         h = ctypes.c_void_p()
         check(self.L.grns_server_create(ctypes.byref(opt), ctypes.byref(h)), "grns_server_create")
         self.h = h
@@ -67,6 +67,10 @@ class Server:
         rid = ctypes.c_uint64()
         check(self.L.grns_server_submit(self.h, ctypes.byref(r), ctypes.byref(rid)), "grns_server_submit")
         return rid.value
+
+    def cancel(self, rid):
+        """cancel a request still waiting for admission (GrnsError BUSY once launched)"""
+        check(self.L.grns_server_cancel(self.h, rid), "grns_server_cancel")
 
     def wait(self, rid, timeout_us=120_000_000):
         st, o0, o1 = ctypes.c_int32(), ctypes.c_uint64(), ctypes.c_uint64()

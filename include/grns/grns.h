@@ -44,7 +44,8 @@ typedef enum {
     GRNS_ERR_TIMEOUT = 5,       /* a bounded wait ran out */
     GRNS_ERR_REJECTED = 6,      /* admission refused (serving) */
     GRNS_ERR_BUSY = 7,
-    GRNS_ERR_TOO_LARGE = 8      /* the request needs more than a fixed capacity */
+    GRNS_ERR_TOO_LARGE = 8,     /* the request needs more than a fixed capacity */
+    GRNS_ERR_CANCELLED = 9      /* serving: the request was cancelled before it ran */
 } grns_status;
 
 typedef enum { GRNS_LAYOUT_SOA = 0, GRNS_LAYOUT_AOS = 1 } grns_layout;
@@ -343,6 +344,9 @@ typedef struct {
     int32_t admission_timeout_ms;/* a request not admitted within this time completes with
                                     GRNS_ERR_REJECTED (0: 10000) */
     int32_t reserved;
+    size_t alloc_cap_bytes;      /* hard cap on the device memory the server holds (0: none): a put
+                                    beyond it returns, and an admitted request beyond it completes
+                                    with, GRNS_ERR_OUT_OF_MEMORY; the server goes on */
 } grns_server_options;
 
 typedef struct {
@@ -378,6 +382,10 @@ grns_status grns_server_poll(grns_server *srv, uint64_t request_id, int *done, i
                              uint64_t *out1);
 grns_status grns_server_wait(grns_server *srv, uint64_t request_id, int64_t timeout_us, int32_t *status,
                              uint64_t *out0, uint64_t *out1);
+/* a request still waiting for admission completes with GRNS_ERR_CANCELLED;
+ * one already launched runs to the end (GRNS_ERR_BUSY); a finished one is
+ * left as it is (GRNS_OK) */
+grns_status grns_server_cancel(grns_server *srv, uint64_t request_id);
 grns_status grns_server_stats_get(grns_server *srv, grns_server_stats *stats);
 grns_status grns_server_reset_stats(grns_server *srv);
 

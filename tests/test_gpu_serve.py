@@ -164,3 +164,63 @@ def test_cached_evaluations_and_admission(env):
         assert st == 0
     finally:
         small.close()
+
+
+def test_failures_are_reported_not_fatal(env):
+    """host-side fault injection: a request cancelled while it waits for memory,
+    allocations beyond a hard cap, a bounded wait that runs out, and a
+    corrupted request descriptor -- each reported with its status while the
+    server goes on serving"""
+    G, native, ctxs = env
+    from grns_gb300.serve import Server
+    ctx = ctxs[32]
+    cnt = 40000
+    x = gen(native, ctx, cnt, 1, 11)
+    y = gen(native, ctx, cnt, 2, 11)
+    operands = 2 * 4 * 32 * cnt
+    # budget fits the operands and a comparison's output, not a division's: the division waits
+    srv = Server(budget_bytes=operands + 8 * cnt + (1 << 20), slots=1, admission_timeout_ms=20000)
+    try:
+        ci = srv.add_context(ctx)
+        hx, hy = srv.put(ci, x), srv.put(ci, y)
+        rid = srv.submit("div", ci, hx, hy)
+        srv.cancel(rid)
+        st, _, _ = srv.wait(rid, timeout_us=5_000_000)
+        assert st == 9  # GRNS_ERR_CANCELLED
+        srv.cancel(rid)  # already finished: no-op
+        st, o0, _ = srv.wait(srv.submit("cmp", ci, hx, hy), timeout_us=30_000_000)
+        assert st == 0
+        # a corrupted descriptor (unknown operand handle) is refused at submission
+        with pytest.raises(G.GrnsError):
+            srv.submit("cmp", ci, hx, 987654321)
+    finally:
+        srv.close()
+    # a hard allocation cap: the operands fit, a division's outputs do not
+    capped = Server(alloc_cap_bytes=operands + 8 * cnt + (1 << 20), slots=2)
+    try:
+        ci = capped.add_context(ctx)
+        hx, hy = capped.put(ci, x), capped.put(ci, y)
+        st, _, _ = capped.wait(capped.submit("div", ci, hx, hy), timeout_us=30_000_000)
+        assert st == 4  # GRNS_ERR_OUT_OF_MEMORY
+        with pytest.raises(G.GrnsError) as e:
+            capped.put(ci, x)
+        assert e.value.status == 4
+        st, _, _ = capped.wait(capped.submit("cmp", ci, hx, hy), timeout_us=30_000_000)
+        assert st == 0
+    finally:
+        capped.close()
+    # a bounded wait that runs out reports GRNS_ERR_TIMEOUT; the request still completes
+    srv = Server(slots=1)
+    try:
+        ci = srv.add_context(ctx)
+        big = gen(native, ctx, 1 << 18, 3, 12)
+        d = gen(native, ctx, 1 << 18, 4, 12, divisors=True)
+        hb, hd = srv.put(ci, big), srv.put(ci, d)
+        rid = srv.submit("div", ci, hb, hd)
+        with pytest.raises(G.GrnsError) as e:
+            srv.wait(rid, timeout_us=1)
+        assert e.value.status == 5
+        st, _, _ = srv.wait(rid, timeout_us=60_000_000)
+        assert st == 0
+    finally:
+        srv.close()
