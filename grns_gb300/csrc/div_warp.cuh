@@ -468,14 +468,11 @@ __device__ __forceinline__ int64_t warp_claim(unsigned long long *ctr, int c) {
     return (int64_t)__shfl_sync(0xffffffffu, b, 0);
 }
 
-/* grid-wide form, in three launches (div_global_* below): pass A over numbers
- * claimed from a counter, a counting sort of all numbers by decreasing step
- * count, pass B over the sorted order claimed from a second counter -- the
- * whole grid then works longest-first with no per-warp ranges to drain */
+/* grid-wide form (three launches, ops_div.cu): pass A over numbers claimed
+ * from one counter, a counting sort by step count, pass B over the sorted
+ * order claimed from a second counter -- no per-warp ranges to drain */
 struct DivGlobal {
     unsigned long long ctr_a, ctr_b;
-    uint32_t hist[kDivBins];   // numbers per step count
-    uint32_t fill[kDivBins];   // positions taken per step count by the scatter
 };
 
 /* shared memory of a block of `threads` threads running div_range: the DivK

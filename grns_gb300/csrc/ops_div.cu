@@ -2,10 +2,11 @@
  * grns_gb300 -- division and power-of-two scaling kernels.
  *   k_div      : q = floor(X/D), r = X - qD (reference src/rnsdiv.cuh:128),
  *                reference-faithful FP64 form, one thread per number
- *   k_div_a, k_div_hist, k_div_scatter, k_div_b : the same results on the
- *                integer fast path (div_warp.cuh): pass A over the whole
- *                grid, a counting sort of the numbers by step count, pass B
- *                longest-first, numbers claimed from grid-wide counters
+ *   k_div_a, k_div_sort, k_div_b : the same results on the integer fast
+ *                path (div_warp.cuh): pass A over the whole grid, a counting
+ *                sort by step count inside segments of consecutive numbers,
+ *                pass B segment by segment, longest first, numbers claimed
+ *                from grid-wide counters
  *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
  */
 #include "div_warp.cuh"
@@ -74,53 +75,44 @@ __global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
                      cols + threadIdx.x, blockDim.x);
 }
 
-/* the histogram of step counts over all records (G->hist) */
-__global__ void __launch_bounds__(256) k_div_hist(const uint2 *__restrict__ rec, DivGlobal *__restrict__ G,
+constexpr int kDivSegment = 4096;  // numbers sorted together: contiguous, so pass B's loads stay L2-local
+
+/* order: within each segment of kDivSegment consecutive numbers, the numbers
+ * by decreasing step count (one block per segment, a counting sort in shared
+ * memory).  Pass B claims positions in order, so the grid works through the
+ * segments one after another, longest divisions first inside each, and the
+ * operands it touches at any time span a few segments (L2-resident). */
+__global__ void __launch_bounds__(256) k_div_sort(const uint2 *__restrict__ rec, int32_t *__restrict__ order,
                                                   int64_t count) {
     __shared__ uint32_t h[kDivBins];
-    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
-        atomicAdd(&h[dv_rec_steps(rec[k])], 1u);
-    __syncthreads();
-    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x)
-        if (h[i]) atomicAdd(&G->hist[i], h[i]);
-}
-
-/* order[p] = the numbers by decreasing step count (counting sort): each
- * block takes a contiguous share, claims room in every bin with one atomic
- * per bin, and places its numbers with shared-memory atomics */
-__global__ void __launch_bounds__(256) k_div_scatter(const uint2 *__restrict__ rec, DivGlobal *__restrict__ G,
-                                                     int32_t *__restrict__ order, int64_t count) {
-    __shared__ uint32_t base[kDivBins], local[kDivBins], slot[kDivBins];
-    const int64_t per = (count + gridDim.x - 1) / gridDim.x;
-    const int64_t b0 = (int64_t)blockIdx.x * per, b1 = b0 + per < count ? b0 + per : count;
-    if (threadIdx.x < 32) {  /* exclusive prefix over bins in decreasing order (lane l: bins 63 - l, 31 - l) */
-        const int lane = threadIdx.x;
-        const uint32_t h0 = G->hist[63 - lane], h1 = G->hist[31 - lane];
-        uint32_t s0 = h0, s1 = h1;
+    for (int64_t b0 = (int64_t)blockIdx.x * kDivSegment; b0 < count; b0 += (int64_t)gridDim.x * kDivSegment) {
+        const int64_t b1 = b0 + kDivSegment < count ? b0 + kDivSegment : count;
+        for (int i = threadIdx.x; i < kDivBins; i += blockDim.x) h[i] = 0;
+        __syncthreads();
+        for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) atomicAdd(&h[dv_rec_steps(rec[k])], 1u);
+        __syncthreads();
+        if (threadIdx.x < 32) {  /* exclusive prefix over bins in decreasing order (lane l: bins 63 - l, 31 - l) */
+            const int lane = threadIdx.x;
+            const uint32_t h0 = h[63 - lane], h1 = h[31 - lane];
+            uint32_t s0 = h0, s1 = h1;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t a0 = __shfl_up_sync(0xffffffffu, s0, o), a1 = __shfl_up_sync(0xffffffffu, s1, o);
-            if (lane >= o) {
-                s0 += a0;
-                s1 += a1;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t a0 = __shfl_up_sync(0xffffffffu, s0, o), a1 = __shfl_up_sync(0xffffffffu, s1, o);
+                if (lane >= o) {
+                    s0 += a0;
+                    s1 += a1;
+                }
             }
+            s1 += __shfl_sync(0xffffffffu, s0, 31);
+            h[63 - lane] = s0 - h0;
+            h[31 - lane] = s1 - h1;
         }
-        s1 += __shfl_sync(0xffffffffu, s0, 31);
-        base[63 - lane] = s0 - h0;
-        base[31 - lane] = s1 - h1;
-    }
-    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x) local[i] = 0;
-    __syncthreads();
-    for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) atomicAdd(&local[dv_rec_steps(rec[k])], 1u);
-    __syncthreads();
-    for (int i = threadIdx.x; i < kDivBins; i += blockDim.x)
-        slot[i] = base[i] + (local[i] ? atomicAdd(&G->fill[i], local[i]) : 0u);
-    __syncthreads();
-    for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
-        const uint32_t p = atomicAdd(&slot[dv_rec_steps(rec[k])], 1u);
-        order[p] = (int32_t)k;
+        __syncthreads();
+        for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+            const uint32_t p = atomicAdd(&h[dv_rec_steps(rec[k])], 1u);
+            order[b0 + p] = (int32_t)k;
+        }
+        __syncthreads();
     }
 }
 
@@ -235,13 +227,8 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
         k_div_a<N><<<grid_of(occ[0]), kDivBlock, smem_a, s>>>(consts_of<N>(c), X, Dv, rec, G, count);
         e = cudaGetLastError();
     }
-    const unsigned sgrid = grid_for(c, (count + 1023) / 1024, 1, 4);
     if (e == cudaSuccess) {
-        k_div_hist<<<grid_for(c, count, 256, 4), 256, 0, s>>>(rec, G, count);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-        k_div_scatter<<<sgrid, 256, 0, s>>>(rec, G, order, count);
+        k_div_sort<<<grid_for(c, (count + kDivSegment - 1) / kDivSegment, 1, 8), 256, 0, s>>>(rec, order, count);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
