@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 N32 = 32
 PAIRS = 1 << 18
+DIV_TRAFFIC_BYTES = 328.2e6  # DRAM bytes of one 2^18-pair division call (ncu, three launches)
 CMP_PAIRS = 1 << 20
 EVAL_COUNT = 1 << 22
 MP_PAIRS = 1 << 22          # mp_int pairs at n = 64
@@ -766,17 +767,21 @@ def main():
         "config": {"workload": "div 2^18 pairs (divisor bits uniform in [1,959]) + scale2pow 2^18 numbers "
                                "(D uniform in [1,900]), n=32 greedy moduli from 2^30-1, SoA",
                    "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "k_div_warp<32>", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+        "roofline": {"bound": "hbm", "kernel": "k_div_a<32> + k_div_sort + k_div_b<32> (one division call)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": DIV_TRAFFIC_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three launches of "
+                                       "one call, profiles/k_div_n32_262144pairs.md",
                      "note": "division is integer-pipe bound (48-bit digit steps); the HBM-bound kernels "
                              "(eval, cmp, max, mp_int) carry their own fractions in extra"},
-        "kernels_ms": {"k_div_warp": div_avg, "k_scale": statistics.mean(scale_ms),
-                       "k_div_warp_steps": [round(v, 4) for v in div_ms],
-                       "k_scale_steps": [round(v, 4) for v in scale_ms]},
+        "kernels_ms": {"division": div_avg, "k_scale_warp": statistics.mean(scale_ms),
+                       "division_steps": [round(v, 4) for v in div_ms],
+                       "k_scale_warp_steps": [round(v, 4) for v in scale_ms]},
         "e2e": {"value": e2e, "unit": "Mnum/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "grns_div_host + grns_scale2pow_host (pinned host arrays, chunked copy/compute "
                        "overlap), the two on two streams", "matches_device_results": e2e_ok},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 4 * args.steps,  # per step: k_div_a, k_div_sort, k_div_b, k_scale_warp
         "extra": extra,
         "workloads": workloads,
     }
