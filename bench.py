@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 N32 = 32
 PAIRS = 1 << 18
 DIV_TRAFFIC_BYTES = 328.2e6  # DRAM bytes of one 2^18-pair division call (ncu, three launches)
+CONV_COUNT = 1 << 22  # numbers per binary <-> RNS conversion call
 CMP_PAIRS = 1 << 20
 EVAL_COUNT = 1 << 22
 MP_PAIRS = 1 << 22          # mp_int pairs at n = 64
@@ -396,6 +397,57 @@ def bench_mpint_max(ctx_for, L, dev, stream, sp, P, seed, steps, flush, peak):
     return res
 
 
+def bench_next_ops(ctx_for, L, dev, stream, sp, P, seed, steps, flush, peak):
+    """the operations next to the path: mp_int division (n = 32, 2^18 pairs,
+    900-bit dividends, 450-bit divisors), binary <-> RNS conversion (n = 32
+    and 64, 2^22 numbers below M) and mixed-radix conversion (n = 32, 2^22)"""
+    import torch
+    import grns_gb300 as G
+    from grns_gb300 import native
+    from grns_gb300.workload import S_X
+    res = {}
+    c32 = ctx_for(32)
+    mb = G.mpint_bytes(32)
+    cnt = PAIRS
+    ma = torch.empty(cnt * mb, dtype=torch.uint8, device=dev)
+    mc, mo = torch.empty_like(ma), torch.empty_like(ma)
+    native.check(L.grns_gen_mpint(c32.handle, seed, cnt, 900, P(ma), sp))
+    native.check(L.grns_gen_mpint(c32.handle, seed + 1, cnt, 450, P(mc), sp))
+    f = lambda: native.check(L.grns_mpint_div(c32.handle, P(ma), P(mc), cnt, P(mo), None, sp))  # noqa
+    time_calls(f, 3, stream)
+    m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+    res["mpint_div_n32"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "ms": m, "pairs": cnt,
+                            "operands": "900-bit dividends, 450-bit divisors, random signs"}
+    del ma, mc, mo
+    for n in (32, 64):
+        c = ctx_for(n)
+        cnt = CONV_COUNT
+        LM = L.grns_ctx_binary_limbs(c.handle)
+        x = torch.empty((n, cnt), dtype=torch.int32, device=dev)
+        y = torch.empty_like(x)
+        w = torch.empty((cnt, LM), dtype=torch.int32, device=dev)
+        native.check(L.grns_gen_uniform(c.handle, seed, S_X, cnt, 0, P(x), sp))
+        f = lambda: native.check(L.grns_to_binary(c.handle, P(x), cnt, 0, P(w), LM, None, sp))  # noqa
+        time_calls(f, 3, stream)
+        m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+        b = (4 * n + 4 * LM) * cnt
+        res[f"to_binary_n{n}"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": b / (m * 1e-3) / 1e9,
+                                  "frac_hbm": b / (m * 1e-3) / 1e9 / peak, "ms": m, "count": cnt, "limbs": LM}
+        f = lambda: native.check(L.grns_from_binary(c.handle, P(w), LM, cnt, 0, P(y), sp))  # noqa
+        time_calls(f, 3, stream)
+        m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+        res[f"from_binary_n{n}"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "GBps": b / (m * 1e-3) / 1e9,
+                                    "frac_hbm": b / (m * 1e-3) / 1e9 / peak, "ms": m, "count": cnt, "limbs": LM}
+        if n == 32:
+            f = lambda: native.check(L.grns_mrc(c.handle, P(x), cnt, 0, P(y), None, sp))  # noqa
+            time_calls(f, 3, stream)
+            m = statistics.median(time_calls(f, max(3, steps), stream, flush))
+            res["mrc_n32"] = {"Mnum_s": cnt / (m * 1e-3) / 1e6, "ms": m, "count": cnt,
+                              "note": "n (n - 1) / 2 = 496 subtract-and-multiply steps per number"}
+        del x, y, w
+    return res
+
+
 # ---------------------------------------------------------------------------
 # batched uneven workload (n = 32): one persistent launch (CUDA graph) vs one plain call per job
 
@@ -749,6 +801,8 @@ def main():
             extra.update(bench_eval_cmp(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush, peak))
             torch.cuda.empty_cache()
             extra.update(bench_mpint_max(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush, peak))
+            torch.cuda.empty_cache()
+            extra.update(bench_next_ops(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush, peak))
             torch.cuda.empty_cache()
             workloads["batched_uneven_n32"] = bench_batched(ctx_for, L, dev, stream, sp, P, seed, args.steps, flush)
             torch.cuda.empty_cache()

@@ -207,7 +207,7 @@ grns_status grns_scale2pow_host(grns_ctx *c, const int32_t *x, const uint32_t *D
     std::vector<HostArr> outs = {{(void *)out, soa, c->n, rec}};
     if (flags) outs.push_back({(void *)flags, false, 1, 1});
     const bool has_D = D != nullptr, has_flags = flags != nullptr;
-    return pipeline(c, count, chunks ? chunks : auto_chunks(count, 1 << 17), in, outs, (cudaStream_t)stream,
+    return pipeline(c, count, chunks ? chunks : auto_chunks(count, 1 << 16), in, outs, (cudaStream_t)stream,
                     [&](const std::vector<void *> &di, const std::vector<void *> &dout, int64_t len, cudaStream_t s) {
                         return launch_scale2pow(c, (const uint32_t *)di[0], has_D ? (const uint32_t *)di[1] : nullptr,
                                                 D_uniform, soa ? len : 0, len, (uint32_t *)dout[0],
