@@ -44,6 +44,31 @@ OR_DEFINE_TREE(OFN(tree_h_ru), h_add_ru)
 OR_DEFINE_TREE(OFN(tree_d_rd), d_add_rd)
 OR_DEFINE_TREE(OFN(tree_d_ru), d_add_ru)
 
+/* The n-threaded schedule's sums (cuda::block_reduce_sum_rd/ru,
+ * src/pairwise.cuh:969/:984, over warp_reduce_sum_rd/ru :932/:939): inside a
+ * warp, lane l adds lane l + 16, then l + 8, 4, 2, 1 (shuffles down), so lane 0
+ * holds ((v0 + v16) + (v8 + v24)) + ...; with n = 64 the two warp sums are
+ * then reduced the same way with zeros in the other lanes, which is s0 + s1.
+ * For n < 32 the reference's shuffles read lanes that do not exist
+ * (undefined); here, as in the device header, absent lanes are skipped. */
+static double OFN(warp_tree)(const double *v, int lanes, int up) {
+    double a[32], b[32];
+    for (int l = 0; l < 32; l++) a[l] = l < lanes ? v[l] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int l = 0; l < 32; l++)
+            b[l] = (l + off < lanes) ? (up ? d_add_ru(a[l], a[l + off]) : d_add_rd(a[l], a[l + off])) : a[l];
+        for (int l = 0; l < 32; l++) a[l] = b[l];
+    }
+    return a[0];
+}
+static double OFN(ptree_d)(const double *v, int up) {
+    if (ON <= 32) return OFN(warp_tree)(v, ON, up);
+    double w[32];
+    const int warps = ON / 32;
+    for (int j = 0; j < warps; j++) w[j] = OFN(warp_tree)(v + 32 * j, 32, up);
+    return OFN(warp_tree)(w, warps, up);
+}
+
 /* ---------------- mixed-radix conversion, src/mrc.cuh:31 (host) / :101 (device) ---------------- */
 static inline void OFN(mrc_h)(const or_ctx *c, int *mr, const int *x) {
     for (int i = 0; i < ON; i++) {
@@ -186,6 +211,47 @@ static void OFN(eval_d)(const or_ctx *c, or_iv *out, const int *x) {
     }
     for (int i = 0; i < ON; i++) fl[i] = d_mul_rd((double)s[i], c->recip_rd[i]);
     suml = OFN(tree_d_rd)(fl);
+    suml = d_sub_rd(suml, (double)(unsigned)suml);
+    or_er_set_d(&out->low, suml);
+    or_er_set_d(&out->upp, sumu);
+    out->low.exp -= K;
+    out->upp.exp -= K;
+}
+
+/* device cuda::rns_eval_compute_parallel, src/rnseval.cuh:332-418: the
+ * serial algorithm with the n-threaded schedule's sums (ptree_d) */
+static void OFN(eval_dpar)(const or_ctx *c, or_iv *out, const int *x) {
+    int s[ON], mrd[ON], mr = -1;
+    double fl[ON], fu[ON];
+    for (int i = 0; i < ON; i++) s[i] = or_modmul(x[i], c->w[i], c->m[i]);
+    for (int i = 0; i < ON; i++) {
+        fl[i] = d_mul_rd((double)s[i], c->recip_rd[i]);
+        fu[i] = d_mul_ru((double)s[i], c->recip_ru[i]);
+    }
+    double suml = OFN(ptree_d)(fl, 0), sumu = OFN(ptree_d)(fu, 1);
+    if (suml == 0 && sumu == 0) { out->low.frac = out->upp.frac = 0; out->low.exp = out->upp.exp = 0; return; }
+    unsigned whl = (unsigned)suml, whu = (unsigned)sumu;
+    suml = d_sub_rd(suml, (double)whl);
+    sumu = d_sub_ru(sumu, (double)whu);
+    or_er_set_d(&out->low, suml);
+    or_er_set_d(&out->upp, sumu);
+    if (whl != whu) { OFN(mrc_d)(c, mrd, x); mr = mrd[ON - 1]; }
+    if (mr > 0) { out->upp = c->inv_unit.upp; return; }
+    if (mr == 0) out->low = c->unit.low;
+    if (sumu >= c->acc) return;
+    int K = 0;
+    while (sumu < c->acc) {
+        double a = -(or_ceil_log2_dev(sumu) + 1);
+        int k = (int)(a > c->ref_factor ? a : (double)c->ref_factor);
+        const int *p2 = c->pow2 + (long)k * ON;
+        for (int i = 0; i < ON; i++) s[i] = or_modmul(s[i], p2[i], c->m[i]);
+        for (int i = 0; i < ON; i++) fu[i] = d_mul_ru((double)s[i], c->recip_ru[i]);
+        sumu = OFN(ptree_d)(fu, 1);
+        sumu = d_sub_ru(sumu, (double)(unsigned)sumu);
+        K += k;
+    }
+    for (int i = 0; i < ON; i++) fl[i] = d_mul_rd((double)s[i], c->recip_rd[i]);
+    suml = OFN(ptree_d)(fl, 0);
     suml = d_sub_rd(suml, (double)(unsigned)suml);
     or_er_set_d(&out->low, suml);
     or_er_set_d(&out->upp, sumu);
@@ -507,6 +573,7 @@ static void OFN(batch_eval)(const or_ctx *c, const int *x, long N, or_iv *out, i
     for (long k = 0; k < N; k++) {
         if (path == 0) OFN(eval_h)(c, out + k, x + k * ON);
         else if (path == 1) OFN(eval_d)(c, out + k, x + k * ON);
+        else if (path == 3) OFN(eval_dpar)(c, out + k, x + k * ON);
         else OFN(eval_fast_h)(c, out + k, x + k * ON);
     }
 }

@@ -21,7 +21,7 @@ from . import build_oracle
 ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
 IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
 
-PATH_HOST, PATH_DEVICE, PATH_HOST_FAST = 0, 1, 2
+PATH_HOST, PATH_DEVICE, PATH_HOST_FAST, PATH_DEVICE_PARALLEL = 0, 1, 2, 3
 SUPPORTED_N = (4, 8, 12, 16, 32, 64)
 
 _lib = None
@@ -105,16 +105,16 @@ class Oracle:
         lib().oracle_eval(ctypes.c_void_p(self._h), _p(x), ctypes.c_long(x.shape[0]), _p(out), path, threads)
         return out
 
-    def log2_inputs(self, x, cap=1 << 20):
+    def log2_inputs(self, x, cap=1 << 20, path=PATH_DEVICE):
         """the distinct values whose ceil(log2) the device-path refinement loop
         evaluates for these numbers (sorted)"""
         buf = np.zeros(cap)
         lib().oracle_log2_record(_p(buf), cap)
-        self.eval(x, path=PATH_DEVICE)
+        self.eval(x, path=path)
         n = lib().oracle_log2_recorded()
         return np.unique(buf[:n])
 
-    def eval_with_device_log2(self, x, xs, cs):
+    def eval_with_device_log2(self, x, xs, cs, path=PATH_DEVICE):
         """device-path evaluation using the device's ceil(log2 x) values `cs` for inputs `xs`"""
         xs = np.ascontiguousarray(xs, dtype=np.float64)
         cs = np.ascontiguousarray(cs, dtype=np.int32)
@@ -122,7 +122,7 @@ class Oracle:
         xs, cs = xs[order], cs[order]
         lib().oracle_log2_table(_p(xs), _p(cs), len(xs))
         try:
-            return self.eval(x, path=PATH_DEVICE)
+            return self.eval(x, path=path)
         finally:
             lib().oracle_log2_table(ctypes.c_void_p(0), ctypes.c_void_p(0), 0)
 
