@@ -194,6 +194,15 @@ class RNSContext:
                                      _stream(stream)), "grns_eval")
         return out
 
+    def rns_eval_compute_fast(self, x, layout="soa", flags=None, stream=None):
+        """cuda::rns_eval_compute_fast (src/rnseval.cuh:266): numbers below about M/2"""
+        import torch
+        count = self._count(x, layout)
+        out = torch.empty(count * 32, dtype=torch.uint8, device=x.device)
+        check(native.lib().grns_eval_fast(self._h, _ptr(x), count, LAYOUTS[layout], _ptr(out), _ptr(flags),
+                                          _stream(stream)), "grns_eval_fast")
+        return out
+
     def rns_eval_tight(self, x, layout="soa", flags=None, stream=None):
         """one-ulp certified enclosures of X/M, never wider than rns_eval_compute's
         (not bit-identical to them)"""

@@ -474,6 +474,7 @@ namespace grns {
 size_t batch_staging_bytes(int njobs) { return sizeof(JobDev) * (size_t)(njobs > 0 ? njobs : 1); }
 
 grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *staging, cudaStream_t s) {
+    NvtxRange range("grns batch_run");
     grns_batch b;
     b.ctx = c;
     b.njobs = njobs;
@@ -584,6 +585,7 @@ grns_status grns_batch_update(grns_batch *b, const grns_job *jobs, int njobs) {
 }
 
 grns_status grns_batch_launch(grns_batch *b, void *stream) {
+    grns::NvtxRange range("grns_batch_launch");
     if (!b) return GRNS_ERR_INVALID_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
     if (!b->use_graph || s == nullptr) return enqueue(b, s);

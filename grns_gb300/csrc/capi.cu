@@ -22,6 +22,15 @@ grns_status grns_eval(grns_ctx *c, const int32_t *x, int64_t count, int layout, 
     return grns::launch_eval(c, (const uint32_t *)x, ld_of(layout, count), count, out, flags, (cudaStream_t)stream);
 }
 
+grns_status grns_eval_fast(grns_ctx *c, const int32_t *x, int64_t count, int layout, interval_t *out, uint8_t *flags,
+                           void *stream) {
+    if (!c || count < 0 || !layout_ok(layout)) return GRNS_ERR_INVALID_ARGUMENT;
+    if (count == 0) return GRNS_OK;
+    if (!x || !out) return GRNS_ERR_INVALID_ARGUMENT;
+    return grns::launch_eval(c, (const uint32_t *)x, ld_of(layout, count), count, out, flags, (cudaStream_t)stream,
+                             true);
+}
+
 grns_status grns_eval_tight(grns_ctx *c, const int32_t *x, int64_t count, int layout, interval_t *out, uint8_t *flags,
                             void *stream) {
     if (!c || count < 0 || !layout_ok(layout)) return GRNS_ERR_INVALID_ARGUMENT;

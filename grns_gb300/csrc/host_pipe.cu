@@ -56,6 +56,7 @@ int auto_chunks(int64_t count, int64_t min_chunk) {
 template <class Launch>
 grns_status pipeline(const grns_ctx *c, int64_t count, int chunks, const std::vector<HostArr> &in,
                      const std::vector<HostArr> &out, cudaStream_t user, Launch launch) {
+    NvtxRange range("grns host-buffer call");
     constexpr int kSlots = 2;
     if (chunks < 1) chunks = 1;
     if (chunks > count) chunks = (int)count;

@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <mutex>
@@ -57,6 +58,15 @@ inline const Consts<N> &consts_of(const grns_ctx *c) {
 
 constexpr uint64_t kPoolKeepBytes = 256ull << 20;
 
+/* an NVTX range over a host-side scope (batched launches, served launches,
+ * host-buffer calls): visible in Nsight timelines, a no-op without a tool */
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 /* scratch from the context's pool (the device's default pool if it has none) */
 inline cudaError_t scratch_alloc(const grns_ctx *c, void **p, size_t bytes, cudaStream_t s) {
     return c->pool ? cudaMallocFromPoolAsync(p, bytes, c->pool, s) : cudaMallocAsync(p, bytes, s);
@@ -82,7 +92,7 @@ inline unsigned grid_for(const grns_ctx *c, int64_t work, int block, int per_sm 
 grns_status launch_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                               uint8_t *flags, cudaStream_t s);
 grns_status launch_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
-                        uint8_t *flags, cudaStream_t s);
+                        uint8_t *flags, cudaStream_t s, bool fast = false);
 grns_status launch_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, int64_t ld, int64_t count,
                        int32_t *out, uint8_t *flags, cudaStream_t s);
 /* min_per_warp > 0 launches fewer warps when that gives each warp at least

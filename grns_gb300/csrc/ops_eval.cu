@@ -11,13 +11,14 @@
 
 namespace grns {
 
-template <int N>
+template <int N, bool FAST = false>
 __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
                                               Er *__restrict__ out, uint8_t *__restrict__ flags) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = 0;
         Er lo, up;
-        eval<N>(C, [&](int i) { return x.load(k, i); }, lo, up, f);
+        auto get = [&](int i) { return x.load(k, i); };
+        eval<N, decltype(get), FAST>(C, get, lo, up, f);
         out[2 * k] = lo;
         out[2 * k + 1] = up;
         if (flags) flags[k] = (uint8_t)f;
@@ -27,7 +28,7 @@ __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> 
 /* the same, with the next number's residues loaded into registers while the
  * current one is evaluated (the common path is latency-bound on its loads
  * otherwise); the rare branch re-reads its residues from memory */
-template <int N>
+template <int N, bool FAST = false>
 __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Consts<N> C, Operand<N> x,
                                                       int64_t count, Er *__restrict__ out,
                                                       uint8_t *__restrict__ flags) {
@@ -47,7 +48,8 @@ __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Co
         }
         uint32_t f = 0, bad = 0;
         Er lo, up;
-        const int st = eval_int<N>(C, [&](int i) { return cur[i]; }, lo, up, bad);
+        auto getc = [&](int i) { return cur[i]; };
+        const int st = eval_int<N, decltype(getc), FAST>(C, getc, lo, up, bad);
         if (bad) {
             f = kFlagInvalidInput;
             lo = up = Er{0.0, 0};
@@ -55,7 +57,8 @@ __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Co
             lo = up = Er{0.0, 0};
         } else if (st == kEvalRare) {
             const int64_t kk = k;
-            eval_full<N>(C, [&](int i) { return x.load(kk, i); }, lo, up, f);
+            auto getm = [&](int i) { return x.load(kk, i); };
+            eval_full<N, decltype(getm), FAST>(C, getm, lo, up, f);
         }
         out[2 * k] = lo;
         out[2 * k + 1] = up;
@@ -259,15 +262,16 @@ __global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ Con
     }
 }
 
-template <int N>
+template <int N, bool FAST>
 static grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                             uint8_t *flags, cudaStream_t s) {
     const int B = 256;
     if (N <= 32)
-        k_eval_pipe<N><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
-                                                             flags);
+        k_eval_pipe<N, FAST><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
+                                                                   (Er *)out, flags);
     else
-        k_eval<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out, flags);
+        k_eval<N, FAST><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
+                                                           flags);
     return cuda_status(cudaGetLastError());
 }
 
@@ -308,8 +312,8 @@ grns_status launch_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, 
 }
 
 grns_status launch_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
-                        uint8_t *flags, cudaStream_t s) {
-#define C_(n) return run_eval<n>(c, x, ld, count, out, flags, s)
+                        uint8_t *flags, cudaStream_t s, bool fast) {
+#define C_(n) return fast ? run_eval<n, true>(c, x, ld, count, out, flags, s) : run_eval<n, false>(c, x, ld, count, out, flags, s)
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }

@@ -117,7 +117,7 @@ __device__ __forceinline__ void mrc_digits(const Consts<N> &C, Get get, uint32_t
 /* ---------------- interval evaluation (src/rnseval.cuh:182-256) ---------------- */
 
 /* Full reference algorithm with arrays; used for the rare branches. */
-template <int N, class Get>
+template <int N, class Get, bool FAST = false>
 __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &flags) {
     uint32_t s[N];
     PTree<N, false> tl;
@@ -141,7 +141,7 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
     low = er_from_double(suml);
     upp = er_from_double(sumu);
     int mr = -1;
-    if (whl != whu) {
+    if (!FAST && whl != whu) {  // rns_eval_compute_fast skips the ambiguity step
         uint32_t d[N];
         mrc_digits<N>(C, get, d);
         mr = (int)d[N - 1];
@@ -185,10 +185,10 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
 /* Common path on the integer pipe (eval_int, rns_fast.cuh: the same doubles as
  * the FP64 directed-rounding trees, computed exactly); falls back to eval_full
  * for ambiguous integer parts or small values (rare for uniform X). */
-template <int N, class Get>
+template <int N, class Get, bool FAST = false>
 __device__ __forceinline__ void eval(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &flags) {
     uint32_t bad = 0;
-    const int st = eval_int<N>(C, get, low, upp, bad);
+    const int st = eval_int<N, Get, FAST>(C, get, low, upp, bad);
     if (bad) {
         flags |= kFlagInvalidInput;
         low = Er{0.0, 0};
@@ -200,7 +200,7 @@ __device__ __forceinline__ void eval(const Consts<N> &C, Get get, Er &low, Er &u
         upp = Er{0.0, 0};
         return;
     }
-    if (st == kEvalRare) eval_full<N>(C, get, low, upp, flags);
+    if (st == kEvalRare) eval_full<N, Get, FAST>(C, get, low, upp, flags);
 }
 
 /* ---------------- comparison (src/rnscmp.cuh:55-74) ---------------- */

@@ -248,7 +248,7 @@ enum : int { kEvalOk = 0, kEvalRare = 1, kEvalZero = 2 };
  * X = 0, kEvalRare when the integer parts of the two sums differ or the upper
  * fraction is below RNS_EVAL_ACCURACY (the reference's mixed-radix and
  * refinement branches decide then).  bad collects residues >= m_i. */
-template <int N, class Get>
+template <int N, class Get, bool FAST = false>
 GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
     Fx100Tree<N, false> tl;
     Fx100Tree<N, true> tu;
@@ -265,7 +265,9 @@ GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &ba
     const uint64_t whl = sl.hi >> 36, whu = su.hi >> 36;  // integer parts (scale 2^100 = 2^(64+36))
     sl.hi &= (((uint64_t)1) << 36) - 1;
     su.hi &= (((uint64_t)1) << 36) - 1;
-    if (whl != whu || fx100_less(su, C.acc_lo, C.acc_hi)) return kEvalRare;
+    /* rns_eval_compute_fast (src/rnseval.cuh:266) keeps the fractions when the
+     * integer parts differ; rns_eval_compute resolves that case by mixed radix */
+    if ((!FAST && whl != whu) || fx100_less(su, C.acc_lo, C.acc_hi)) return kEvalRare;
     low = er_from_fx100(sl);
     upp = er_from_fx100(su);
     return kEvalOk;

@@ -264,6 +264,7 @@ void schedule_locked(grns_server *sv) {
             jobs.push_back(j);
         }
         if (jobs.empty()) continue;
+        grns::NvtxRange range("grns_server launch");
         grns_status st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
         if (st == GRNS_OK) st = grns::cuda_status(cudaLaunchHostFunc(sl->s, on_launch_done, sl));
         if (st != GRNS_OK) {

@@ -37,6 +37,7 @@ SIGNATURES = {
     "grns_mpint_div": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "grns_ctx_binary_limbs": (c_int, [c_void_p]),
     "grns_mrc": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
+    "grns_eval_fast": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_div_host": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_int,
                               c_void_p]),
     "grns_scale2pow_host": (c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_uint32, c_int64, c_int, c_void_p, c_void_p,

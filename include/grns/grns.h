@@ -129,6 +129,14 @@ grns_status grns_eval(grns_ctx *ctx, const int32_t *x, int64_t count, int layout
 grns_status grns_eval_tight(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, interval_t *out,
                             uint8_t *flags, void *stream);
 
+/* out[k] = cuda::rns_eval_compute_fast's interval (reference
+ * src/rnseval.cuh:266) bit for bit: rns_eval_compute without the mixed-radix
+ * step, for numbers "not too large" (below about M/2).  Near M, where the
+ * reference's refinement reads outside its tables, the loop stops with
+ * GRNS_FLAG_ITER_CAP. */
+grns_status grns_eval_fast(grns_ctx *ctx, const int32_t *x, int64_t count, int layout, interval_t *out,
+                           uint8_t *flags, void *stream);
+
 /* ---- magnitude comparison ----
  * out[k] = sign(X_k - Y_k) in {-1, 0, 1}, as cuda::rns_cmp
  * (reference src/rnscmp.cuh:55); the evaluations stay in registers. */

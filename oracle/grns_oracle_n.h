@@ -218,6 +218,41 @@ static void OFN(eval_d)(const or_ctx *c, or_iv *out, const int *x) {
     out->upp.exp -= K;
 }
 
+/* device cuda::rns_eval_compute_fast, src/rnseval.cuh:266-322: the device
+ * algorithm without the mixed-radix ambiguity step */
+static void OFN(eval_fast_d)(const or_ctx *c, or_iv *out, const int *x) {
+    int s[ON];
+    double fl[ON], fu[ON];
+    for (int i = 0; i < ON; i++) s[i] = or_modmul(x[i], c->w[i], c->m[i]);
+    for (int i = 0; i < ON; i++) {
+        fl[i] = d_mul_rd((double)s[i], c->recip_rd[i]);
+        fu[i] = d_mul_ru((double)s[i], c->recip_ru[i]);
+    }
+    double suml = OFN(tree_d_rd)(fl), sumu = OFN(tree_d_ru)(fu);
+    if (suml == 0 && sumu == 0) { out->low.frac = out->upp.frac = 0; out->low.exp = out->upp.exp = 0; return; }
+    suml = d_sub_rd(suml, (double)(unsigned)suml);
+    sumu = d_sub_ru(sumu, (double)(unsigned)sumu);
+    if (sumu >= c->acc) { or_er_set_d(&out->low, suml); or_er_set_d(&out->upp, sumu); return; }
+    int K = 0;
+    while (sumu < c->acc) {
+        double a = -(or_ceil_log2_dev(sumu) + 1);
+        int k = (int)(a > c->ref_factor ? a : (double)c->ref_factor);
+        const int *p2 = c->pow2 + (long)k * ON;
+        for (int i = 0; i < ON; i++) s[i] = or_modmul(s[i], p2[i], c->m[i]);
+        for (int i = 0; i < ON; i++) fu[i] = d_mul_ru((double)s[i], c->recip_ru[i]);
+        sumu = OFN(tree_d_ru)(fu);
+        sumu = d_sub_ru(sumu, (double)(unsigned)sumu);
+        K += k;
+    }
+    for (int i = 0; i < ON; i++) fl[i] = d_mul_rd((double)s[i], c->recip_rd[i]);
+    suml = OFN(tree_d_rd)(fl);
+    suml = d_sub_rd(suml, (double)(unsigned)suml);
+    or_er_set_d(&out->low, suml);
+    or_er_set_d(&out->upp, sumu);
+    out->low.exp -= K;
+    out->upp.exp -= K;
+}
+
 /* device cuda::rns_eval_compute_parallel, src/rnseval.cuh:332-418: the
  * serial algorithm with the n-threaded schedule's sums (ptree_d) */
 static void OFN(eval_dpar)(const or_ctx *c, or_iv *out, const int *x) {
@@ -574,6 +609,7 @@ static void OFN(batch_eval)(const or_ctx *c, const int *x, long N, or_iv *out, i
         if (path == 0) OFN(eval_h)(c, out + k, x + k * ON);
         else if (path == 1) OFN(eval_d)(c, out + k, x + k * ON);
         else if (path == 3) OFN(eval_dpar)(c, out + k, x + k * ON);
+        else if (path == 4) OFN(eval_fast_d)(c, out + k, x + k * ON);
         else OFN(eval_fast_h)(c, out + k, x + k * ON);
     }
 }

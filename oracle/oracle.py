@@ -21,7 +21,7 @@ from . import build_oracle
 ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
 IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
 
-PATH_HOST, PATH_DEVICE, PATH_HOST_FAST, PATH_DEVICE_PARALLEL = 0, 1, 2, 3
+PATH_HOST, PATH_DEVICE, PATH_HOST_FAST, PATH_DEVICE_PARALLEL, PATH_DEVICE_FAST = 0, 1, 2, 3, 4
 SUPPORTED_N = (4, 8, 12, 16, 32, 64)
 
 _lib = None
@@ -211,9 +211,14 @@ class Exact:
         return [sum(int(r) * b for r, b in zip(row, B)) % M for row in np.asarray(rows)]
 
     def encloses(self, iv, values):
-        """Bool array: low <= X/M <= upp for each interval and integer X."""
+        """Bool array: low <= X/M <= upp for each interval and integer X (False
+        for exponents no evaluation of X/M can have)."""
         out = []
+        lim = 4 * self.M.bit_length() + 64
         for rec, v in zip(iv, values):
+            if abs(int(rec["low"]["exp"])) > lim or abs(int(rec["upp"]["exp"])) > lim:
+                out.append(False)
+                continue
             lo = er_value(rec["low"]["frac"], rec["low"]["exp"])
             up = er_value(rec["upp"]["frac"], rec["upp"]["exp"])
             out.append(lo <= Fraction(v, self.M) <= up)

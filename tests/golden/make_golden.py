@@ -104,6 +104,11 @@ def main():
             fx[f"scale_{path}"] = ref.scale2pow(x, S, dev=dev)
             fx[f"mrc_{path}"] = ref.mrc(x, dev=dev)
         fx["eval_fast_host"] = ref.eval(x, dev=False, fast=True).view(np.uint8)
+        # cuda::rns_eval_compute_fast requires a number "not too large" (src/rnseval.cuh:259):
+        # near M the reference reads outside its tables, so only X < M/2 here
+        xf = res([v for v in X if v < M // 2])
+        fx["xf"] = xf
+        fx["eval_fast_dev"] = ref.eval(xf, dev=True, fast=True).view(np.uint8)
         # mp_int inputs through the reference's own constructor (host eval), then both op paths
         ma = np.concatenate([ref.mpint_from_str(v).view(np.uint8) for v in A])
         mb = np.concatenate([ref.mpint_from_str(v).view(np.uint8) for v in B])

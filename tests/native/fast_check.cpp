@@ -87,6 +87,18 @@ int fc_eval(void *p, const uint32_t *x, long cnt, int32_t *status, Er *iv) {
     return 0;
 }
 
+/* the same for rns_eval_compute_fast (no mixed-radix step) */
+int fc_eval_fast(void *p, const uint32_t *x, long cnt, int32_t *status, Er *iv) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) { uint32_t bad = 0; Er lo{0, 0}, up{0, 0}; \
+        auto g = [&](int i) { return x[k * N + i]; }; \
+        int st = eval_int<N, decltype(g), true>(K<N>(b), g, lo, up, bad); \
+        status[k] = bad ? 8 : st; iv[2 * k] = lo; iv[2 * k + 1] = up; }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
 /* one-ulp evaluation: 1 where certified (interval written), 0 where the
  * bit-exact evaluation would be used */
 int fc_eval_tight(void *p, const uint32_t *x, long cnt, int32_t *ok, Er *iv) {

@@ -30,7 +30,8 @@ def fc(tmp_path_factory):
     L.fc_E.restype = ctypes.c_uint64
     L.fc_E.argtypes = [ctypes.c_void_p]
     L.fc_binary_limbs.argtypes = [ctypes.c_void_p]
-    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary"):
+    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary",
+              "fc_eval_fast"):
         getattr(L, f).argtypes = None
     return L
 
@@ -241,6 +242,26 @@ def test_integer_eval_is_bit_exact(fc, tag):
     assert iv[ok].tobytes() == want[ok].tobytes()
     assert all((s == 2) == (v == 0) for s, v in zip(st, vals))
     assert not (st == 8).any()
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_integer_fast_eval_is_bit_exact(fc, tag):
+    """the integer-pipe form of rns_eval_compute_fast (no mixed-radix step)
+    returns the reference's device doubles on its common path, numbers below M/2"""
+    from oracle import oracle as O
+    mods = moduli_for(tag)
+    f, orc = FC(fc, mods), O.Oracle(mods)
+    M = f.M
+    rng = random.Random(47)
+    vals = [rng.randrange(M // 2) for _ in range(3000)] + [M // 2 - 1, 1, 2] + [M >> j for j in range(2, 200, 7)]
+    x = f.res(vals)
+    st = np.zeros(len(vals), np.int32)
+    iv = np.zeros(len(vals), IV)
+    fc.fc_eval_fast(f.h, f.P(x), ctypes.c_long(len(vals)), f.P(st), f.P(iv))
+    want = orc.eval(x.view(np.int32), path=O.PATH_DEVICE_FAST)
+    ok = st == 0
+    assert ok.sum() > 2500
+    assert iv[ok].tobytes() == want[ok].tobytes()
 
 
 def er_fraction(frac, exp):

@@ -99,6 +99,30 @@ def test_eval_golden(case, layout):
 
 
 @pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_eval_fast(case, layout):
+    """cuda::rns_eval_compute_fast (src/rnseval.cuh:266) on numbers below M/2"""
+    tag, ctx, orc, g = case
+    P = O.PATH_DEVICE_FAST
+    xs = orc.log2_inputs(g["xf"], path=P)
+    want = orc.eval_with_device_log2(g["xf"], xs, ctx.device_ceil_log2(xs) if len(xs) else np.zeros(0, np.int32), path=P)
+    got = ctx.rns_eval_compute_fast(to_dev(g["xf"], layout), layout=layout).cpu().numpy()
+    assert got.tobytes() == want.tobytes()
+    if len(xs) == 0 or np.array_equal(ctx.device_ceil_log2(xs), np.ceil(np.log2(xs)).astype(np.int32)):
+        assert got.tobytes() == g["eval_fast_dev"].tobytes()
+    rng = random.Random(9)
+    vals = [rng.randrange(orc.M // 2) for _ in range(3000 if orc.n <= 16 else 1000)]
+    vals += [rng.randrange(1, 1 << rng.randrange(1, orc.log2M)) for _ in range(300)]
+    x = orc.exact.to_rns(vals)
+    flags = flags_buf(len(x))
+    got = ctx.rns_eval_compute_fast(to_dev(x, layout), layout=layout, flags=flags).cpu().numpy().view(IV_DTYPE)
+    xs = orc.log2_inputs(x, path=P)
+    want = orc.eval_with_device_log2(x, xs, ctx.device_ceil_log2(xs) if len(xs) else np.zeros(0, np.int32), path=P)
+    assert got.tobytes() == want.tobytes()
+    assert int(flags.sum()) == 0
+    assert orc.exact.encloses(got, vals).all()
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
 def test_eval_random_bit_exact_and_enclosing(case, layout):
     tag, ctx, orc, g = case
     N = 6000 if orc.n <= 16 else 2000

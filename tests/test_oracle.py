@@ -42,6 +42,12 @@ def test_eval_fast_host_matches_golden(case):
     assert orc.eval(g["x"], path=O.PATH_HOST_FAST).view(np.uint8).tobytes() == g["eval_fast_host"].tobytes()
 
 
+def test_eval_fast_device_matches_golden(case):
+    """cuda::rns_eval_compute_fast, src/rnseval.cuh:266"""
+    tag, orc, g = case
+    assert orc.eval(g["xf"], path=O.PATH_DEVICE_FAST).view(np.uint8).tobytes() == g["eval_fast_dev"].tobytes()
+
+
 @pytest.mark.parametrize("path,code", PATHS)
 def test_cmp_div_scale_mrc_match_golden(case, path, code):
     tag, orc, g = case
