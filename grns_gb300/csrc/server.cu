@@ -149,6 +149,7 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
         case GRNS_OP_DIV: return (2 * 4 * (size_t)n + 12) * k;
         case GRNS_OP_SCALE2POW: return (4 * (size_t)n + 12) * k;
         case GRNS_OP_MAX: return ((4 * (size_t)n + 7) / 8) * 8 + 8;
+        case GRNS_OP_MPINT_DIV: return (GRNS_MPINT_BYTES(n) + 16 * (size_t)n + 25) * k;  // + digit columns, division scratch
         default: return GRNS_MPINT_BYTES(n) * (size_t)k;
     }
 }
@@ -183,8 +184,8 @@ void schedule_locked(grns_server *sv) {
     for (Slot *sl : sv->slots) {
         if (sl->busy || sv->pending.empty()) continue;
         const int ctx = sv->reqs[sv->pending.front()].r.ctx_index;
-        std::vector<grns_job> jobs;
-        while (!sv->pending.empty() && (int)jobs.size() < sv->opt.max_jobs_per_launch) {
+        std::vector<grns_job> jobs, divs;
+        while (!sv->pending.empty() && (int)(jobs.size() + divs.size()) < sv->opt.max_jobs_per_launch) {
             const uint64_t id = sv->pending.front();
             Req &q = sv->reqs[id];
             if (q.r.ctx_index != ctx) break;
@@ -261,11 +262,16 @@ void schedule_locked(grns_server *sv) {
             if (q.r.op == GRNS_OP_EVAL && q.count == A.count) sv->arrays[q.r.a].eval = q.out0;
             q.state = 1;
             sl->reqs.push_back(id);
-            jobs.push_back(j);
+            if (q.r.op == GRNS_OP_MPINT_DIV) divs.push_back(j);  // its own launches (grns_mpint_div)
+            else jobs.push_back(j);
         }
-        if (jobs.empty()) continue;
+        if (jobs.empty() && divs.empty()) continue;
         grns::NvtxRange range("grns_server launch");
-        grns_status st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
+        grns_status st = GRNS_OK;
+        if (!jobs.empty())
+            st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
+        for (size_t t = 0; st == GRNS_OK && t < divs.size(); t++)
+            st = grns::launch_mpint(sv->ctxs[ctx], 3, divs[t].a, divs[t].b, divs[t].count, divs[t].out0, nullptr, sl->s);
         if (st == GRNS_OK) st = grns::cuda_status(cudaLaunchHostFunc(sl->s, on_launch_done, sl));
         if (st != GRNS_OK) {
             for (uint64_t id : sl->reqs) {
@@ -279,7 +285,7 @@ void schedule_locked(grns_server *sv) {
         }
         sl->busy = true;
         sv->launches++;
-        sv->jobs_launched += jobs.size();
+        sv->jobs_launched += jobs.size() + divs.size();
     }
 }
 
@@ -458,7 +464,7 @@ grns_status grns_server_submit(grns_server *sv, const grns_request *r, uint64_t 
     if (!sv || !r || !request_id) return GRNS_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> g(sv->mu);
     if (r->ctx_index < 0 || r->ctx_index >= (int)sv->ctxs.size()) return GRNS_ERR_INVALID_ARGUMENT;
-    if (r->op < GRNS_OP_EVAL || r->op > GRNS_OP_MPINT_MUL) return GRNS_ERR_INVALID_ARGUMENT;
+    if (r->op < GRNS_OP_EVAL || r->op > GRNS_OP_MPINT_DIV) return GRNS_ERR_INVALID_ARGUMENT;
     auto ia = sv->arrays.find(r->a);
     if (ia == sv->arrays.end() || ia->second.ctx != r->ctx_index) return GRNS_ERR_INVALID_ARGUMENT;
     const bool mp = r->op >= GRNS_OP_MPINT_ADD;

@@ -115,7 +115,7 @@ class ServerStats(ctypes.Structure):
 
 ARRAY_RNS, ARRAY_U32, ARRAY_MPINT, ARRAY_INTERVAL, ARRAY_MAXOUT = range(5)
 
-OP_EVAL, OP_CMP, OP_DIV, OP_SCALE2POW, OP_MAX, OP_MPINT_ADD, OP_MPINT_SUB, OP_MPINT_MUL = range(8)
+OP_EVAL, OP_CMP, OP_DIV, OP_SCALE2POW, OP_MAX, OP_MPINT_ADD, OP_MPINT_SUB, OP_MPINT_MUL, OP_MPINT_DIV = range(9)
 
 
 class GrnsError(RuntimeError):

@@ -7,7 +7,8 @@ import numpy as np
 from . import native
 from .native import check
 
-OPS = {"eval": 0, "cmp": 1, "div": 2, "scale2pow": 3, "max": 4, "mpint_add": 5, "mpint_sub": 6, "mpint_mul": 7}
+OPS = {"eval": 0, "cmp": 1, "div": 2, "scale2pow": 3, "max": 4, "mpint_add": 5, "mpint_sub": 6, "mpint_mul": 7,
+       "mpint_div": 8}
 
 
 class Server:

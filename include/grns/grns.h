@@ -279,7 +279,9 @@ typedef enum {
     GRNS_OP_MAX = 4,        /* a: x;  out0: int32[n] value, out1: int64 index (or NULL) */
     GRNS_OP_MPINT_ADD = 5,  /* a, b, out0: mp_int_t arrays */
     GRNS_OP_MPINT_SUB = 6,
-    GRNS_OP_MPINT_MUL = 7
+    GRNS_OP_MPINT_MUL = 7,
+    GRNS_OP_MPINT_DIV = 8   /* a, b, out0: mp_int_t arrays; served only (its own launches, as grns_mpint_div),
+                               not a job type of grns_batch */
 } grns_op;
 
 typedef struct {

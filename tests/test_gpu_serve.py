@@ -224,3 +224,33 @@ def test_failures_are_reported_not_fatal(env):
         assert st == 0
     finally:
         srv.close()
+
+
+def test_served_mpint_division(env):
+    """mp_int division requests (GRNS_OP_MPINT_DIV) next to packed requests:
+    the same records as grns_mpint_div"""
+    G, native, ctxs = env
+    from grns_gb300.serve import Server
+    ctx = ctxs[32]
+    cnt = 20000
+    mb = G.mpint_bytes(32)
+    ma = torch.empty(cnt * mb, dtype=torch.uint8, device="cuda")
+    mc = torch.empty_like(ma)
+    native.check(native.lib().grns_gen_mpint(ctx.handle, 5, cnt, 900, P(ma), None))
+    native.check(native.lib().grns_gen_mpint(ctx.handle, 6, cnt, 450, P(mc), None))
+    torch.cuda.synchronize()
+    want = ctx.mpint_div(ma, mc).cpu().numpy().tobytes()
+    x = gen(native, ctx, cnt, 1, 9)
+    srv = Server(slots=2)
+    try:
+        ci = srv.add_context(ctx)
+        ha = srv.put(ci, ma.view(cnt, mb), kind=native.ARRAY_MPINT)
+        hc = srv.put(ci, mc.view(cnt, mb), kind=native.ARRAY_MPINT)
+        hx = srv.put(ci, x)
+        rids = [srv.submit("eval", ci, hx), srv.submit("mpint_div", ci, ha, hc), srv.submit("mpint_div", ci, ha, hc, 777)]
+        outs = [srv.wait(r) for r in rids]
+        assert all(st == 0 for st, _, _ in outs)
+        assert srv.get(outs[1][1]).tobytes() == want
+        assert srv.get(outs[2][1]).tobytes() == want[:777 * mb]
+    finally:
+        srv.close()
