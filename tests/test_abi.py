@@ -61,3 +61,26 @@ def test_product_does_not_use_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
                 src = open(os.path.join(d, f)).read()
                 assert "oracle" not in src.replace("oracle is", ""), os.path.join(d, f)
+
+
+def test_header_is_plain_c(tmp_path, lib):
+    """include/grns/grns.h compiles as C99 and a C program links against the
+    library and calls it (no GPU needed for these entry points)"""
+    import subprocess
+    src = tmp_path / "user.c"
+    src.write_text('#include <stdio.h>\n#include <string.h>\n#include "grns/grns.h"\n'
+                   'int main(void) {\n'
+                   '  grns_ctx *c = 0; int n = 0, lg = 0; int32_t m[8];\n'
+                   '  const char *t = "#define RNS_MODULI_SIZE (4)\\n#define RNS_MODULI_VALUES {3,5,7,11}\\n";\n'
+                   '  if (strcmp(grns_status_string(GRNS_OK), "ok")) return 1;\n'
+                   '  if (grns_params_parse(t, m, 8, &n, &lg) != GRNS_OK || n != 4 || m[3] != 11) return 2;\n'
+                   '  if (grns_ctx_create(0, 8, &c) != GRNS_ERR_INVALID_ARGUMENT) return 3;\n'
+                   '  printf("%s\\n", grns_version());\n  return 0;\n}\n')
+    exe = tmp_path / "user"
+    cuda_inc = "/usr/local/cuda/include"
+    libdir = os.path.dirname(native.lib_path())
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc,
+                    str(src), "-o", str(exe), "-L", libdir, "-lgrns_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    assert "sm_103a" in out.stdout
