@@ -208,7 +208,7 @@ def run_only(args):
     from grns_gb300.workload import S_X, S_Y
     L = native.lib(build_if_missing=True)
     n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32, "mpint64": 64,
-         "mpdiv32": 32, "tobin32": 32, "frombin32": 32, "tobin64": 64}[args.only]
+         "mpdiv32": 32, "tobin32": 32, "frombin32": 32, "tobin64": 64, "mrc32": 32}[args.only]
     ctx = G.RNSContext(greedy(n))
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -259,6 +259,8 @@ def run_only(args):
             native.check(L.grns_to_binary(ctx.handle, P(x), cnt, 0, P(words), LM, None, sp))
         elif args.only == "frombin32":
             native.check(L.grns_from_binary(ctx.handle, P(words), LM, cnt, 0, P(a), sp))
+        elif args.only == "mrc32":
+            native.check(L.grns_mrc(ctx.handle, P(x), cnt, 0, P(a), None, sp))
 
     for _ in range(args.warmup):
         call()
@@ -694,7 +696,7 @@ def main():
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
     ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "evtight32", "mpint64",
-                                           "mpdiv32", "tobin32", "frombin32", "tobin64"], default=None,
+                                           "mpdiv32", "tobin32", "frombin32", "tobin64", "mrc32"], default=None,
                     help="profiling: run just this op --warmup + --steps times on --pairs numbers, no JSON line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.only is None else args.warmup
