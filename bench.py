@@ -740,13 +740,27 @@ def main():
     q, r, so = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
     flush = torch.empty(64 << 20, dtype=torch.int32, device=dev)  # 256 MiB > L2
 
+    # the two operations of a step are independent: the scaling runs on a second
+    # stream beside the division, so it fills the SMs the division leaves idle
+    # (its tails, the sort between its passes); the step ends when both have
+    s_scale = torch.cuda.Stream()
+    sp_scale = ctypes.c_void_p(s_scale.cuda_stream)
+    fork, join = torch.cuda.Event(), torch.cuda.Event()
+
     def step(timers=None):
-        e0, e1, e2 = (timers or (None, None, None))
+        e0, e1, e2, e3, e4, e5 = (timers or (None,) * 6)
         if e0: e0.record(stream)
-        native.check(L.grns_div(ctx.handle, P(x), P(d), PAIRS, 0, P(q), P(r), None, sp))
+        fork.record(stream)
+        s_scale.wait_event(fork)
+        if e3: e3.record(s_scale)
+        native.check(L.grns_scale2pow(ctx.handle, P(xs), P(D), 0, PAIRS, 0, P(so), None, sp_scale))
+        if e4: e4.record(s_scale)
+        join.record(s_scale)
         if e1: e1.record(stream)
-        native.check(L.grns_scale2pow(ctx.handle, P(xs), P(D), 0, PAIRS, 0, P(so), None, sp))
+        native.check(L.grns_div(ctx.handle, P(x), P(d), PAIRS, 0, P(q), P(r), None, sp))
         if e2: e2.record(stream)
+        stream.wait_event(join)
+        if e5: e5.record(stream)
 
     step_ms, div_ms, scale_ms = [], [], []
     with Clocks(local) as clk:
@@ -760,12 +774,12 @@ def main():
             done += 1
         for _ in range(args.steps):
             flush.zero_()
-            t = (_ev(), _ev(), _ev())
+            t = tuple(_ev() for _ in range(6))
             step(t)
             torch.cuda.synchronize()
-            div_ms.append(t[0].elapsed_time(t[1]))
-            scale_ms.append(t[1].elapsed_time(t[2]))
-            step_ms.append(t[0].elapsed_time(t[2]))
+            div_ms.append(t[1].elapsed_time(t[2]))     # division, on its stream (sharing the GPU)
+            scale_ms.append(t[3].elapsed_time(t[4]))   # scaling, on its stream
+            step_ms.append(t[0].elapsed_time(t[5]))    # the whole step
         # ---- end to end through the C ABI's host-buffer forms (pinned host arrays), every
         # copy inside the timed region: grns_div_host and grns_scale2pow_host pipeline their
         # chunks' copies with their kernels; the two operations run on two streams, so one's
@@ -822,6 +836,8 @@ def main():
         "data": "synthetic (seeded splitmix64 generator, device-generated)",
         "config": {"workload": "div 2^18 pairs (divisor bits uniform in [1,959]) + scale2pow 2^18 numbers "
                                "(D uniform in [1,900]), n=32 greedy moduli from 2^30-1, SoA",
+                   "streams": "the division and the scaling of a step on two streams at once (independent); "
+                              "kernels_ms are each one's span on its stream while they share the GPU",
                    "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": "k_div_a<32> + k_div_sort + k_div_b<32> (one division call)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
