@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -86,6 +87,27 @@ inline unsigned grid_for(const grns_ctx *c, int64_t work, int block, int per_sm 
     int64_t cap = (int64_t)c->sm_count * per_sm;
     if (need < 1) need = 1;
     return (unsigned)(need < cap ? need : cap);
+}
+
+/* resident blocks per SM of `kernel` at `block` threads and `smem` dynamic
+ * bytes, with its shared-memory limit raised first; computed once per device
+ * (`cache` holds one entry per device, a zero-initialised static array).  The
+ * entry is published after the attribute is set, so a thread that reads a
+ * nonzero entry may launch with that much shared memory at once; two threads
+ * that both see zero both compute the same value. */
+constexpr int kOccDevices = 16;
+template <class K>
+int resident_blocks(std::atomic<int> (&cache)[kOccDevices], const grns_ctx *c, K kernel, int block, size_t smem) {
+    std::atomic<int> *slot = c->device >= 0 && c->device < kOccDevices ? &cache[c->device] : nullptr;
+    if (slot) {
+        const int v = slot->load(std::memory_order_acquire);
+        if (v) return v;
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, block, smem) != cudaSuccess || nb < 1) nb = 1;
+    if (slot) slot->store(nb, std::memory_order_release);
+    return nb;
 }
 
 /* launchers (one translation unit per op family) */

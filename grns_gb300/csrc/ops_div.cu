@@ -189,19 +189,9 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
     /* fast path: pass A, a counting sort by step count, pass B (div_warp.cuh),
      * each over the whole grid with numbers claimed from counters */
     const size_t smem = div_smem_bytes<N>(kDivBlock), smem_a = divnorm_smem_bytes<N>(kDivBlock);
-    static int per_sm[8][2] = {};  // resident blocks per SM of k_div_a / k_div_b, per device
-    int *occ = per_sm[c->device & 7];
-    if (occ[0] == 0) {
-        if (smem_a > 48 * 1024) cudaFuncSetAttribute(k_div_a<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a);
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_div_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int na = 0, nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&na, k_div_a<N>, kDivBlock, smem_a) != cudaSuccess || na < 1)
-            na = 1;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_div_b<N>, kDivBlock, smem) != cudaSuccess || nb < 1)
-            nb = 1;
-        occ[0] = na;
-        occ[1] = nb;
-    }
+    static std::atomic<int> occ_a[kOccDevices], occ_b[kOccDevices];  // resident blocks per SM, per device
+    const int occ[2] = {resident_blocks(occ_a, c, k_div_a<N>, kDivBlock, smem_a),
+                        resident_blocks(occ_b, c, k_div_b<N>, kDivBlock, smem)};
     /* warps: every resident one, fewer when a warp would get under min_per_warp
      * numbers (or one per lane's worth) */
     auto grid_of = [&](int o) {
@@ -251,17 +241,8 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
     }
     /* fast path: warps over contiguous ranges (scale_warp.cuh) */
     const size_t smem = scale_smem_bytes<N>(kDivBlock);
-    static int per_sm[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident blocks per SM, per device
-    int &occ = per_sm[c->device & 7];
-    if (occ == 0) {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_scale_warp<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_scale_warp<N>, kDivBlock, smem) != cudaSuccess ||
-            nb < 1)
-            nb = 1;
-        occ = nb;
-    }
+    static std::atomic<int> per_sm[kOccDevices];  // resident blocks per SM, per device
+    const int occ = resident_blocks(per_sm, c, k_scale_warp<N>, kDivBlock, smem);
     const int64_t warps_cap = (int64_t)c->sm_count * occ * (kDivBlock / 32);
     int64_t warps = (count + 31) / 32;
     if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)

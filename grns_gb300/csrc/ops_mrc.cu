@@ -52,15 +52,8 @@ template <int N>
 static grns_status run_mrc(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out,
                            uint8_t *flags, cudaStream_t s) {
     const size_t smem = (size_t)N * N * sizeof(uint2) + (size_t)N * kMrcBlock * 4;
-    static int per_sm[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // resident blocks per SM, per device
-    int &occ = per_sm[c->device & 7];
-    if (occ == 0) {
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k_mrc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_mrc<N>, kMrcBlock, smem) != cudaSuccess || nb < 1)
-            nb = 1;
-        occ = nb;
-    }
+    static std::atomic<int> per_sm[kOccDevices];  // resident blocks per SM, per device
+    const int occ = resident_blocks(per_sm, c, k_mrc<N>, kMrcBlock, smem);
     k_mrc<N><<<grid_for(c, count, kMrcBlock, occ), kMrcBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
                                                                           Output<N>{out, ld}, flags);
     return cuda_status(cudaGetLastError());
