@@ -138,10 +138,13 @@ grns_status pipeline(const grns_ctx *c, int64_t count, int chunks, const std::ve
             continue;
         }
         cudaEvent_t done = nullptr;
-        if (cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess) {
-            joined &= cudaEventRecord(done, st[k]) == cudaSuccess && cudaStreamWaitEvent(user, done, 0) == cudaSuccess;
+        bool waits = cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess;
+        if (waits) {
+            waits = cudaEventRecord(done, st[k]) == cudaSuccess && cudaStreamWaitEvent(user, done, 0) == cudaSuccess;
             cudaEventDestroy(done);
-        } else {
+        }
+        if (!waits) {  // the slots are freed on the caller's stream: this stream's copies end first
+            cudaStreamSynchronize(st[k]);
             joined = false;
         }
     }
