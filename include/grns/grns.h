@@ -83,6 +83,7 @@ grns_status grns_ctx_destroy(grns_ctx *ctx);
  * creates the context (grns_ctx_create's rules on n and the moduli apply). */
 grns_status grns_params_parse(const char *text, int32_t *moduli, int capacity, int *n_out, int *log2_out);
 grns_status grns_ctx_create_from_params(const char *text, grns_ctx **out);
+/* the queries below answer 0 for a NULL context */
 int grns_ctx_n(const grns_ctx *ctx);
 /* floor(log2 M): the reference's RNS_MODULI_PRODUCT_LOG2 (src/params.h:16) */
 int grns_ctx_log2(const grns_ctx *ctx);

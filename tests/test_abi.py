@@ -84,3 +84,39 @@ def test_header_is_plain_c(tmp_path, lib):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, (out.returncode, out.stderr)
     assert "sm_103a" in out.stdout
+
+
+# entry points whose first argument is a handle (context, batch, server)
+_NOT_HANDLE_FIRST = {"grns_status_string", "grns_version", "grns_ctx_create", "grns_params_parse",
+                     "grns_ctx_create_from_params", "grns_server_create", "grns_device_ceil_log2", "grns_gen_shifts"}
+# queries that answer with a value rather than a status
+_QUERIES = {"grns_ctx_n": 0, "grns_ctx_log2": 0, "grns_ctx_binary_limbs": 0, "grns_batch_chunks": -1,
+            "grns_batch_grid": -1}
+
+
+def test_null_handle_rejected_by_every_entry(lib):
+    """Each entry point checks its handle before touching anything else: a
+    NULL context, batch or server gives GRNS_ERR_INVALID_ARGUMENT (the
+    context queries answer 0, the batch queries -1), whatever the other
+    arguments."""
+    from grns_gb300.native import SIGNATURES
+    checked = 0
+    for name, (_, args) in SIGNATURES.items():
+        if name in _NOT_HANDLE_FIRST:
+            continue
+        vals = []
+        for a in args:
+            if a in (ctypes.c_int64, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t):
+                vals.append(1)
+            elif a is ctypes.c_double:
+                vals.append(0.0)
+            else:
+                vals.append(None)
+        got = getattr(lib, name)(*vals)
+        want = _QUERIES.get(name, 1)
+        assert got == want, (name, got)
+        checked += 1
+    assert checked >= 45
+    # the two entries without a handle check their pointers first
+    assert lib.grns_device_ceil_log2(None, None, 1, None) == 1
+    assert lib.grns_gen_shifts(1, 1, 1, None, None) == 1
