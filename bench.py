@@ -145,7 +145,6 @@ def aggregate(per_rank_ms, count_per_rank, world):
 def cpu_baseline(threads=None, sample=4096):
     """the reference's CPU path (host rns_div + host rns_scale2pow, restated in
     oracle/) on the host cores; returns (Mnum/s, cores, description)"""
-    import numpy as np
     from grns_gb300 import workload as W
     from oracle import oracle as O
     moduli = O.greedy_moduli(N32)

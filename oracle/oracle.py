@@ -10,7 +10,6 @@ AoS layout ([x1..xn][x1..xn]...).  Interval evaluations are numpy structured
 arrays with the interval_t layout (reference src/types.cuh:25).
 """
 import ctypes
-import os
 from fractions import Fraction
 from math import gcd
 

@@ -3,10 +3,8 @@ graph replay, n-threaded vs serial schedules, autotuner).  Every job's
 outputs must equal the per-call entry points' outputs bit for bit (those are
 checked against the oracle and exact arithmetic in test_gpu_parity.py)."""
 import ctypes
-import os
 import random
 
-import numpy as np
 import pytest
 
 from oracle.oracle import greedy_moduli

@@ -6,7 +6,6 @@ server) and inside the mix."""
 import ctypes
 import random
 
-import numpy as np
 import pytest
 
 from oracle.oracle import greedy_moduli
