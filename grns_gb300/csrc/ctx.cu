@@ -101,7 +101,12 @@ bool params_numbers(const std::string &v, std::vector<long long> &out, bool allo
             while (j < v.size() && (isdigit((unsigned char)v[j]) || (allow_fraction && (v[j] == '.' || v[j] == 'e' ||
                                                                                        v[j] == 'E' || v[j] == '-'))))
                 j++;
-            out.push_back(allow_fraction ? 0 : atoll(v.substr(i, j - i).c_str()));
+            if (!allow_fraction) {
+                if (j - i > 18) return false;  // beyond any size, modulus or exponent (and long long)
+                out.push_back(strtoll(v.substr(i, j - i).c_str(), nullptr, 10));
+            } else {
+                out.push_back(0);
+            }
             i = j;
         } else {
             return false;
@@ -193,10 +198,14 @@ grns_status grns_params_parse(const char *text, int32_t *moduli, int capacity, i
     if (!th.empty() && (!params_numbers(th, thr) || thr.size() != 1 || thr[0] != grns::kScaleStep))
         return GRNS_ERR_UNSUPPORTED;
     const std::string re = params_define(t, "RNS_EVAL_RELATIVE_ERROR");
-    if (!re.empty() && std::fabs(strtod(re.c_str() + re.find_first_not_of(" \t("), nullptr) - 0.0000001) > 1e-15)
-        return GRNS_ERR_UNSUPPORTED;
+    if (!re.empty()) {
+        const size_t at = re.find_first_not_of(" \t(");
+        if (at == std::string::npos || std::fabs(strtod(re.c_str() + at, nullptr) - 0.0000001) > 1e-15)
+            return GRNS_ERR_UNSUPPORTED;
+    }
     for (long long v : vals)
         if (v < 1 || v > 0x7fffffffLL) return GRNS_ERR_INVALID_ARGUMENT;
+    if (!lg.empty() && lg[0] > (1 << 20)) return GRNS_ERR_INVALID_ARGUMENT;
     *n_out = (int)size[0];
     if (log2_out) *log2_out = lg.empty() ? -1 : (int)lg[0];
     if (moduli) {

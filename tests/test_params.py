@@ -64,6 +64,11 @@ def test_parse_without_optional_defines():
     ("#define RNS_MODULI_SIZE (4)\n#define RNS_MODULI_VALUES {3,5,x,11}\n", 1),        # not a number
     (params_text([3, 5, 7, 11], threshold=31), 2),                                     # other scaling step
     (params_text([3, 5, 7, 11], error="0.000001"), 2),                                 # other error bound
+    (params_text([3, 5, 7, 11], error=" "), 2),                                        # empty error bound
+    ("#define RNS_MODULI_SIZE 2\n#define RNS_MODULI_VALUES {3,5}\n#define RNS_EVAL_RELATIVE_ERROR  (\n", 2),
+    ("#define RNS_MODULI_SIZE (4)\n#define RNS_MODULI_VALUES {3,5,7," + "9" * 40 + "}\n", 1),  # overlong
+    ("#define RNS_MODULI_SIZE (" + "9" * 25 + ")\n#define RNS_MODULI_VALUES {3}\n", 1),  # overlong size
+    (params_text([3, 5, 7, 11], log2=1 << 30), 1),                                     # absurd log2
 ])
 def test_parse_rejects(bad, status):
     with pytest.raises(G.GrnsError) as e:
@@ -74,3 +79,36 @@ def test_parse_rejects(bad, status):
 def test_commented_out_definitions_are_ignored():
     text = params_text([3, 5, 7, 11]) + "/* #define RNS_MODULI_SIZE (8) */\n// #define RNS_MODULI_VALUES {1}\n"
     assert G.parse_params(text)[0] == [3, 5, 7, 11]
+
+
+def test_mutated_files_parse_or_fail_cleanly():
+    """byte mutations and truncations of a valid file: the parser returns the
+    original set or an error status, never anything else"""
+    import random
+    mods = moduli_for("g12")
+    text = params_text(mods)
+    rng = random.Random(11)
+    alphabet = "0123456789(){},;/*\\\n #defineRNS_MODULI_SIZEVALUES.-x\t"
+    outcomes = set()
+    for trial in range(3000):
+        t = list(text)
+        for _ in range(rng.randint(1, 6)):
+            k = rng.randrange(len(t))
+            op = rng.random()
+            if op < 0.4:
+                t[k] = rng.choice(alphabet)
+            elif op < 0.7:
+                del t[k]
+            else:
+                t.insert(k, rng.choice(alphabet))
+        if trial % 7 == 0:
+            t = t[:rng.randrange(len(t))]
+        try:
+            got, lg = G.parse_params("".join(t))
+        except G.GrnsError as e:
+            assert e.status in (1, 2)
+            outcomes.add(e.status)
+            continue
+        assert len(got) >= 0 and all(1 <= v <= 0x7FFFFFFF for v in got)
+        outcomes.add(0)
+    assert outcomes >= {0, 1}
