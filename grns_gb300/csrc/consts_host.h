@@ -337,6 +337,39 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
     }
 }
 
+/* The precomputed table `which` in the layout of the reference's device
+ * globals (rns_const_init, src/rnsbase.cuh:324-451), as bytes; empty for an
+ * unknown index.  0 RNS_ORTHOGONAL_BASE weights (int32[n]); 1/2 reciprocals of
+ * the moduli rounded down/up (double[n]); 3 RNS_EVAL_ACCURACY (double); 4
+ * RNS_EVAL_REF_FACTOR (int32); 5 RNS_EVAL_UNIT and 6 RNS_EVAL_INV_UNIT
+ * (interval_t); 7 MRC inverses (int32[n][n]); 8 powers of two (int32[log2+1][n]);
+ * 9 M mod 2^j, 10 M_i mod 2^j and 11 2^-j mod m_i (j < 30). */
+inline std::vector<uint8_t> table_bytes(const HostTables &T, int which) {
+    auto raw = [](const void *p, size_t bytes) {
+        const uint8_t *b = static_cast<const uint8_t *>(p);
+        return std::vector<uint8_t>(b, b + bytes);
+    };
+    const size_t n = (size_t)T.n;
+    switch (which) {
+        case 0: return raw(T.w.data(), 4 * n);
+        case 1: return raw(T.rrd.data(), 8 * n);
+        case 2: return raw(T.rru.data(), 8 * n);
+        case 3: return raw(&T.acc, 8);
+        case 4: return raw(&T.ref_factor, 4);
+        case 5:
+        case 6: {
+            const Er iv[2] = {which == 5 ? T.unit_low : T.inv_unit_low, which == 5 ? T.unit_upp : T.inv_unit_upp};
+            return raw(iv, sizeof(iv));
+        }
+        case 7: return raw(T.mrc_inv.data(), 4 * T.mrc_inv.size());
+        case 8: return raw(T.pow2.data(), 4 * T.pow2.size());
+        case 9: return raw(T.m_pow2.data(), 4 * 30);
+        case 10: return raw(T.mi_pow2.data(), 4 * T.mi_pow2.size());
+        case 11: return raw(T.pow2_inv.data(), 4 * T.pow2_inv.size());
+        default: return {};
+    }
+}
+
 /* The device-table blob (one allocation) and the pointer layout inside it. */
 inline std::vector<uint32_t> table_blob(const HostTables &T) {
     std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows (every size below the

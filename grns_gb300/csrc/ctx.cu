@@ -250,37 +250,10 @@ int grns_ctx_log2(const grns_ctx *c) { return c ? c->log2M : 0; }
 
 grns_status grns_ctx_get_table(const grns_ctx *c, int which, void *dst, size_t bytes) {
     if (!c || !dst) return GRNS_ERR_INVALID_ARGUMENT;
-    const grns::HostTables &T = c->T;
-    const int n = c->n;
-    std::vector<int32_t> tmp;
-    const void *src = nullptr;
-    size_t size = 0;
-    interval_t iv;
-    switch (which) {
-        case 0: src = T.w.data(); size = 4 * n; break;
-        case 1: src = T.rrd.data(); size = 8 * n; break;
-        case 2: src = T.rru.data(); size = 8 * n; break;
-        case 3: src = &T.acc; size = 8; break;
-        case 4: src = &T.ref_factor; size = 4; break;
-        case 5:
-            iv.low = er_float_t{T.unit_low.frac, T.unit_low.exp};
-            iv.upp = er_float_t{T.unit_upp.frac, T.unit_upp.exp};
-            src = &iv; size = sizeof(iv); break;
-        case 6:
-            iv.low = er_float_t{T.inv_unit_low.frac, T.inv_unit_low.exp};
-            iv.upp = er_float_t{T.inv_unit_upp.frac, T.inv_unit_upp.exp};
-            src = &iv; size = sizeof(iv); break;
-        case 7:  /* [i][j] = m_i^-1 mod m_j for j > i (the flat layout is the same) */
-            tmp.assign(T.mrc_inv.begin(), T.mrc_inv.end());
-            src = tmp.data(); size = 4 * tmp.size(); break;
-        case 8: src = T.pow2.data(); size = 4 * T.pow2.size(); break;
-        case 9: src = T.m_pow2.data(); size = 4 * 30; break;
-        case 10: src = T.mi_pow2.data(); size = 4 * T.mi_pow2.size(); break;
-        case 11: src = T.pow2_inv.data(); size = 4 * T.pow2_inv.size(); break;
-        default: return GRNS_ERR_INVALID_ARGUMENT;
-    }
-    if (bytes != size) return GRNS_ERR_INVALID_ARGUMENT;
-    std::memcpy(dst, src, size);
+    static_assert(sizeof(interval_t) == 2 * sizeof(grns::Er), "interval_t is two er_float_t");
+    const std::vector<uint8_t> t = grns::table_bytes(c->T, which);
+    if (t.empty() || bytes != t.size()) return GRNS_ERR_INVALID_ARGUMENT;
+    std::memcpy(dst, t.data(), t.size());
     return GRNS_OK;
 }
 

@@ -137,4 +137,12 @@ int fc_binary_limbs(void *p) { return ((Box *)p)->T.bin_limbs; }
 
 uint64_t fc_E(void *p) { return ((Box *)p)->T.E; }
 
+/* table `which` as grns_ctx_get_table returns it: bytes copied to dst, or -1 */
+long fc_table(void *p, int which, void *dst, long cap) {
+    const std::vector<uint8_t> t = table_bytes(((Box *)p)->T, which);
+    if (t.empty() || (long)t.size() > cap) return -1;
+    memcpy(dst, t.data(), t.size());
+    return (long)t.size();
+}
+
 }

@@ -30,6 +30,8 @@ def fc(tmp_path_factory):
     L.fc_E.restype = ctypes.c_uint64
     L.fc_E.argtypes = [ctypes.c_void_p]
     L.fc_binary_limbs.argtypes = [ctypes.c_void_p]
+    L.fc_table.restype = ctypes.c_long
+    L.fc_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_long]
     for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary",
               "fc_eval_fast"):
         getattr(L, f).argtypes = None
@@ -347,3 +349,25 @@ def test_binary_conversion(fc, tag):
     bad[0, 0] = f.moduli[0]
     back, ok = f.to_binary(bad)
     assert ok[0] == 0 and back[0] == 0
+
+
+TABLE_KEYS = ["w", "recip_rd", "recip_ru", "acc", "ref_factor", "unit", "inv_unit", "mrc_inv", "pow2", "m_pow2_res",
+              "mi_pow2_res", "pow2_inv"]
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_host_tables_match_oracle(fc, tag):
+    """the host-built tables (without GMP) equal the oracle's, which are pinned
+    on the reference's rns_const_init, byte for byte, for every set including
+    the catalogue's; the same bytes grns_ctx_get_table returns"""
+    from oracle import oracle as O
+    mods = moduli_for(tag)
+    f = FC(fc, mods)
+    want = O.Oracle(mods).consts()
+    buf = np.zeros(1 << 20, np.uint8)
+    for which, key in enumerate(TABLE_KEYS):
+        got = fc.fc_table(f.h, which, ctypes.c_void_p(buf.ctypes.data), buf.size)
+        assert got == want[key].nbytes, key
+        assert buf[:got].tobytes() == want[key].tobytes(), key
+    assert fc.fc_table(f.h, len(TABLE_KEYS), ctypes.c_void_p(buf.ctypes.data), buf.size) == -1
+    fc.fc_destroy(f.h)
