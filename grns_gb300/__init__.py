@@ -234,6 +234,10 @@ class RNSContext:
                                     _ptr(flags), _stream(stream)), "grns_div")
         return q, r
 
+    # rns_div_fast (reference src/rnsdiv.cuh:67 host, :180 device) returns the
+    # same q and r as rns_div; both map to grns_div
+    rns_div_fast = rns_div
+
     def rns_scale2pow(self, x, D, layout="soa", flags=None, stream=None):
         """D: int (same exponent for all) or a uint32/int32 CUDA tensor of per-element exponents"""
         import torch

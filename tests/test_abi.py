@@ -120,3 +120,12 @@ def test_null_handle_rejected_by_every_entry(lib):
     # the two entries without a handle check their pointers first
     assert lib.grns_device_ceil_log2(None, None, 1, None) == 1
     assert lib.grns_gen_shifts(1, 1, 1, None, None) == 1
+
+
+def test_mirror_keeps_reference_operation_names():
+    import grns_gb300 as G
+    for name in ("rns_eval_compute", "rns_eval_compute_fast", "rns_cmp", "rns_div", "rns_div_fast", "rns_scale2pow",
+                 "mpint_add", "mpint_sub", "mpint_mul", "mpint_div", "mrc", "rns_max", "rns_from_binary",
+                 "rns_to_binary"):
+        assert callable(getattr(G.RNSContext, name)), name
+    assert G.RNSContext.rns_div_fast is G.RNSContext.rns_div
