@@ -742,6 +742,7 @@ def main():
     # the two operations of a step are independent: the scaling runs on a second
     # stream beside the division, so it fills the SMs the division leaves idle
     # (its tails, the sort between its passes); the step ends when both have
+    # finished
     s_scale = torch.cuda.Stream()
     sp_scale = ctypes.c_void_p(s_scale.cuda_stream)
     fork, join = torch.cuda.Event(), torch.cuda.Event()
