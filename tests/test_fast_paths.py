@@ -371,3 +371,63 @@ def test_host_tables_match_oracle(fc, tag):
         assert buf[:got].tobytes() == want[key].tobytes(), key
     assert fc.fc_table(f.h, len(TABLE_KEYS), ctypes.c_void_p(buf.ctypes.data), buf.size) == -1
     fc.fc_destroy(f.h)
+
+
+def _fuzz_value(rng, M, L):
+    """uniform, of uniform bit length, just below M, near powers of two, near
+    M / k, short, or a fixed edge value"""
+    k = rng.random()
+    if k < 0.3:
+        return rng.randrange(M)
+    if k < 0.5:
+        b = rng.randrange(1, L + 1)
+        return rng.randrange(1 << (b - 1), 1 << b)
+    if k < 0.6:
+        return M - 1 - rng.randrange(1 << rng.randrange(1, 64))
+    if k < 0.7:
+        return (1 << rng.randrange(L + 1)) + rng.randrange(-3, 4)
+    if k < 0.8:
+        return M // rng.randrange(1, 1 << 20) + rng.randrange(-3, 4)
+    if k < 0.9:
+        return rng.randrange(1 << rng.randrange(1, 70))
+    return rng.choice([0, 1, 2, M - 1, M - 2, M // 2, (M + 1) // 2])
+
+
+def test_differential_fuzz(fc):
+    """comparison, division (with dividends near multiples of the divisor),
+    scaling (with values near multiples of 2^D) and RNS -> binary against
+    exact arithmetic on mixed value distributions over every set, for
+    GRNS_FUZZ_SECONDS (default 5) seconds"""
+    import time
+    seconds = float(os.environ.get("GRNS_FUZZ_SECONDS", "5"))
+    rng = random.Random(int(os.environ.get("GRNS_FUZZ_SEED", "2024")))
+    ctxs = {t: FC(fc, moduli_for(t)) for t in TAGS}
+    deadline, rounds = time.time() + seconds, 0
+    while time.time() < deadline or rounds < len(TAGS):
+        tag = TAGS[rounds % len(TAGS)]
+        f = ctxs[tag]
+        M = f.M
+        L = M.bit_length() - 1
+        N = 100
+        X = [_fuzz_value(rng, M, L) % M for _ in range(N)]
+        Y = [_fuzz_value(rng, M, L) % M for _ in range(N)]
+        for k in range(0, N, 10):
+            Y[k] = X[k]
+        assert list(f.cmp(X, Y)) == [sgn(a, b) for a, b in zip(X, Y)], tag
+        D = [max(1, y) for y in Y]
+        for k in range(1, N, 7):
+            q = rng.randrange((M - 1) // D[k] + 1)
+            X[k] = min(M - 1, max(0, q * D[k] + rng.randrange(-2, 3)))
+        q, r, fl = f.div(X, D)
+        assert q == [a // b for a, b in zip(X, D)] and r == [a % b for a, b in zip(X, D)], tag
+        assert not fl.any()
+        S = [rng.randrange(1, min(L + 40, 2047)) for _ in range(N)]
+        for k in range(0, N, 5):
+            base = rng.randrange(max(1, M >> S[k])) << S[k]
+            X[k] = min(M - 1, max(0, base + rng.randrange(-2, 3)))
+        assert f.scale(X, S) == [a >> s for a, s in zip(X, S)], tag
+        vals, ok = f.to_binary(f.res(X))
+        assert ok.all() and vals == X, tag
+        rounds += 1
+    for f in ctxs.values():
+        fc.fc_destroy(f.h)
