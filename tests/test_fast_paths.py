@@ -396,12 +396,15 @@ def _fuzz_value(rng, M, L):
 def test_differential_fuzz(fc):
     """comparison, division (with dividends near multiples of the divisor),
     scaling (with values near multiples of 2^D) and RNS -> binary against
-    exact arithmetic on mixed value distributions over every set, for
-    GRNS_FUZZ_SECONDS (default 5) seconds"""
+    exact arithmetic, and the integer-pipe evaluation against the oracle's
+    restatement of the reference's device path, on mixed value distributions
+    over every set, for GRNS_FUZZ_SECONDS (default 5) seconds"""
     import time
     seconds = float(os.environ.get("GRNS_FUZZ_SECONDS", "5"))
     rng = random.Random(int(os.environ.get("GRNS_FUZZ_SEED", "2024")))
+    from oracle import oracle as O
     ctxs = {t: FC(fc, moduli_for(t)) for t in TAGS}
+    orcs = {t: O.Oracle(moduli_for(t)) for t in TAGS}
     deadline, rounds = time.time() + seconds, 0
     while time.time() < deadline or rounds < len(TAGS):
         tag = TAGS[rounds % len(TAGS)]
@@ -428,6 +431,15 @@ def test_differential_fuzz(fc):
         assert f.scale(X, S) == [a >> s for a, s in zip(X, S)], tag
         vals, ok = f.to_binary(f.res(X))
         assert ok.all() and vals == X, tag
+        # the integer-pipe evaluation: the reference's device doubles on its
+        # common path, the rare path exactly for zero
+        x = f.res(X)
+        st, iv = np.zeros(N, np.int32), np.zeros(N, IV)
+        fc.fc_eval(f.h, f.P(x), ctypes.c_long(N), f.P(st), f.P(iv))
+        want = orcs[tag].eval(x.view(np.int32), path=O.PATH_DEVICE)
+        common = st == 0
+        assert iv[common].tobytes() == want[common].tobytes(), tag
+        assert all((s == 2) == (v == 0) for s, v in zip(st, X)) and not (st == 8).any(), tag
         rounds += 1
     for f in ctxs.values():
         fc.fc_destroy(f.h)
