@@ -395,7 +395,7 @@ def _fuzz_value(rng, M, L):
 
 def test_differential_fuzz(fc):
     """comparison, division (with dividends near multiples of the divisor),
-    scaling (with values near multiples of 2^D) and RNS -> binary against
+    scaling (with values near multiples of 2^D) and binary <-> RNS against
     exact arithmetic, and the integer-pipe evaluation against the oracle's
     restatement of the reference's device path, on mixed value distributions
     over every set, for GRNS_FUZZ_SECONDS (default 5) seconds"""
@@ -431,6 +431,7 @@ def test_differential_fuzz(fc):
         assert f.scale(X, S) == [a >> s for a, s in zip(X, S)], tag
         vals, ok = f.to_binary(f.res(X))
         assert ok.all() and vals == X, tag
+        assert np.array_equal(f.from_binary(X, fc.fc_binary_limbs(f.h)), f.res(X)), tag
         # the integer-pipe evaluation: the reference's device doubles on its
         # common path, the rare path exactly for zero
         x = f.res(X)
