@@ -303,7 +303,10 @@ typedef struct {
 
 typedef struct grns_batch grns_batch;
 grns_status grns_batch_create(grns_ctx *ctx, const grns_job *jobs, int njobs, int use_graph, grns_batch **out);
-/* new pointers for the same job shapes (op, count, layout); keeps the graph */
+/* new pointers for the same job shapes (op, count, layout); keeps the graph.
+ * The job table is copied synchronously from the host: call it once the
+ * batch's earlier launches have completed (their stream synchronised or an
+ * event after them waited on), since they read the table while they run. */
 grns_status grns_batch_update(grns_batch *batch, const grns_job *jobs, int njobs);
 grns_status grns_batch_launch(grns_batch *batch, void *stream);
 grns_status grns_batch_destroy(grns_batch *batch);
