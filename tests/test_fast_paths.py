@@ -396,9 +396,10 @@ def _fuzz_value(rng, M, L):
 def test_differential_fuzz(fc):
     """comparison, division (with dividends near multiples of the divisor),
     scaling (with values near multiples of 2^D) and binary <-> RNS against
-    exact arithmetic, and the integer-pipe evaluation against the oracle's
-    restatement of the reference's device path, on mixed value distributions
-    over every set, for GRNS_FUZZ_SECONDS (default 5) seconds"""
+    exact arithmetic, the integer-pipe evaluation and its fast form against
+    the oracle's restatement of the reference's device path, and the one-ulp
+    evaluation's enclosure, on mixed value distributions over every set, for
+    GRNS_FUZZ_SECONDS (default 5) seconds"""
     import time
     seconds = float(os.environ.get("GRNS_FUZZ_SECONDS", "5"))
     rng = random.Random(int(os.environ.get("GRNS_FUZZ_SEED", "2024")))
@@ -441,6 +442,23 @@ def test_differential_fuzz(fc):
         common = st == 0
         assert iv[common].tobytes() == want[common].tobytes(), tag
         assert all((s == 2) == (v == 0) for s, v in zip(st, X)) and not (st == 8).any(), tag
+        # the fast form (no mixed-radix step) on the numbers below M/2
+        low = [v for v in X if v < M // 2]
+        if low:
+            xl = f.res(low)
+            st, iv = np.zeros(len(low), np.int32), np.zeros(len(low), IV)
+            fc.fc_eval_fast(f.h, f.P(xl), ctypes.c_long(len(low)), f.P(st), f.P(iv))
+            want = orcs[tag].eval(xl.view(np.int32), path=O.PATH_DEVICE_FAST)
+            assert iv[st == 0].tobytes() == want[st == 0].tobytes(), tag
+        # the one-ulp evaluation encloses X/M wherever it certifies
+        few = X[:12]
+        xf = f.res(few)  # kept alive across the call
+        ok, iv = np.zeros(len(few), np.int32), np.zeros(len(few), IV)
+        fc.fc_eval_tight(f.h, f.P(xf), ctypes.c_long(len(few)), f.P(ok), f.P(iv))
+        for k in np.nonzero(ok)[0]:
+            lo = er_fraction(iv[k]["low"]["frac"], iv[k]["low"]["exp"])
+            up = er_fraction(iv[k]["upp"]["frac"], iv[k]["upp"]["exp"])
+            assert lo < Fraction(few[k], M) <= up and up - lo <= Fraction(2) ** (int(iv[k]["low"]["exp"]) - 52), tag
         rounds += 1
     for f in ctxs.values():
         fc.fc_destroy(f.h)
