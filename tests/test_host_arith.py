@@ -25,4 +25,3 @@ def arith(tmp_path_factory):
                                1431655765, 1431655761, 536870913, 536870911])
 def test_modular_primitives(arith, m):
     assert arith.check_modular(m, 200000, m * 7919) == 0
-
