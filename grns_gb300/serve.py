@@ -38,8 +38,12 @@ class Server:
         return idx.value
 
     def put(self, ctx_index, array, kind=native.ARRAY_RNS, layout=0, count=None):
-        """array: torch CUDA tensor or numpy array (copied into server memory)"""
-        if hasattr(array, "is_cuda"):
+        """array: torch CUDA tensor or numpy array (copied into server memory;
+        a CUDA tensor's pending work on the current stream finishes first,
+        since the server copies on its own stream)"""
+        if hasattr(array, "is_cuda") and array.is_cuda:
+            import torch
+            torch.cuda.current_stream(array.device).synchronize()
             src, on_dev = ctypes.c_void_p(array.data_ptr()), 1
         else:
             array = np.ascontiguousarray(array)

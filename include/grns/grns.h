@@ -383,7 +383,10 @@ typedef struct {
 grns_status grns_server_create(const grns_server_options *opt, grns_server **out);
 grns_status grns_server_destroy(grns_server *srv);
 grns_status grns_server_add_context(grns_server *srv, grns_ctx *ctx, int *index);
-/* copy an array in (host or device source); GRNS_ERR_REJECTED when over budget */
+/* copy an array in (host or device source); GRNS_ERR_REJECTED when over budget.
+ * The copy has finished when the call returns.  It runs on the server's own
+ * stream and does not wait for the caller's streams: a device source must
+ * already hold its data (the work producing it finished). */
 grns_status grns_server_put(grns_server *srv, int ctx_index, int kind, const void *src, int src_on_device,
                             int64_t count, int layout, uint64_t *handle);
 /* copy an array out; waits for the request that produces it */
