@@ -197,6 +197,13 @@ void schedule_locked(grns_server *sv) {
                 };
                 if (busy(q.r.a) || (q.r.b && busy(q.r.b))) break;
             }
+            if (sv->arrays.find(q.r.a) == sv->arrays.end() || (q.r.b && sv->arrays.find(q.r.b) == sv->arrays.end())) {
+                sv->pending.pop_front();  // an operand was freed before the request ran
+                q.state = 2;
+                q.status = GRNS_ERR_INVALID_ARGUMENT;
+                q.t_done = now_us();
+                continue;
+            }
             const grns_ctx *c = sv->ctxs[ctx];
             const Array A = sv->arrays[q.r.a];  /* copies: inserting outputs below may rehash the map */
             Array Bv;
@@ -448,6 +455,25 @@ grns_status grns_server_free(grns_server *sv, uint64_t h) {
     if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
     const uint64_t prod = it->second.producer;
     if (prod && !wait_done(sv, lk, prod, -1)) return GRNS_ERR_TIMEOUT;
+    /* unfinished requests that read this array (as an operand, or as the
+     * cached evaluation of one): wait for them, so no launch reads freed memory */
+    auto reads = [&](const Req &q) {
+        auto evaluated_as = [&](uint64_t operand) {
+            auto a = operand ? sv->arrays.find(operand) : sv->arrays.end();
+            return a != sv->arrays.end() && a->second.eval == h;
+        };
+        return q.r.a == h || q.r.b == h || evaluated_as(q.r.a) || evaluated_as(q.r.b);
+    };
+    for (;;) {
+        uint64_t reader = 0;
+        for (const auto &kv : sv->reqs)
+            if (kv.second.state != 2 && reads(kv.second)) {
+                reader = kv.first;
+                break;
+            }
+        if (!reader) break;
+        if (!wait_done(sv, lk, reader, -1)) return GRNS_ERR_TIMEOUT;
+    }
     it = sv->arrays.find(h);
     if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
     cudaFreeAsync(it->second.p, sv->copy);
