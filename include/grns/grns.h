@@ -392,6 +392,8 @@ grns_status grns_server_put(grns_server *srv, int ctx_index, int kind, const voi
 /* copy an array out; waits for the request that produces it */
 grns_status grns_server_get(grns_server *srv, uint64_t handle, void *host_dst, size_t bytes);
 grns_status grns_server_array_info(grns_server *srv, uint64_t handle, int64_t *count, size_t *bytes, void **device_ptr);
+/* release an array; waits for the request that produces it and for unfinished
+ * requests that read it (directly or as a cached evaluation) */
 grns_status grns_server_free(grns_server *srv, uint64_t handle);
 /* non-blocking; a request whose footprint can never fit completes at once with GRNS_ERR_REJECTED */
 grns_status grns_server_submit(grns_server *srv, const grns_request *req, uint64_t *request_id);
