@@ -142,28 +142,93 @@ def aggregate(per_rank_ms, count_per_rank, world):
     return ms, world * count_per_rank / (ms * 1e-3) / 1e6
 
 
-def cpu_baseline(threads=None, sample=4096):
-    """the reference's CPU path (host rns_div + host rns_scale2pow, restated in
-    oracle/) on the host cores; returns (Mnum/s, cores, description)"""
+HEADLINE_OPS = ("div_n32", "div_fast_n32", "scale2pow_n32")
+
+
+def cpu_ops(threads=None, scale=1.0, which=None):
+    """the reference's CPU path op by op (host rns_eval_compute, rns_cmp,
+    rns_div, rns_div_fast, rns_scale2pow, mpint_add/sub/mul, restated in
+    oracle/ and pinned bit for bit to the reference compiled for the CPU), on
+    the workloads' own seeded inputs: each op on all host threads (OpenMP)
+    and on one.  Returns {op: {"Mnum_s", "Mnum_s_1core", "sample", ...}} and
+    the thread count.  `scale` shrinks the samples (the reference arm's
+    per-step samples); `which` limits the ops timed."""
     from grns_gb300 import workload as W
     from oracle import oracle as O
-    moduli = O.greedy_moduli(N32)
-    orc = O.Oracle(moduli)
     threads = threads or O.lib().oracle_max_threads()
-    x = W.uniform_residues(moduli, sample, SEED, W.S_X, layout="aos")
-    d, _ = W.divisors(moduli, orc.log2M, sample, SEED, layout="aos")
-    xs = W.uniform_residues(moduli, sample, SEED, W.S_Y, layout="aos")
-    D = W.shifts(sample, DMAX, SEED)
-    t0 = time.perf_counter()
-    orc.div(x, d, path=O.PATH_HOST, fast=0, threads=threads)
-    t1 = time.perf_counter()
-    orc.scale2pow(xs, D, path=O.PATH_HOST, threads=threads)
-    t2 = time.perf_counter()
-    rate = 2 * sample / (t2 - t0) / 1e6
-    return rate, threads, (f"{sample} div pairs + {sample} scale2pow numbers (n=32, same generator), host path "
-                           f"(rns_div, rns_scale2pow) restated in oracle/, {threads} threads: "
-                           f"div {1e6 * (t1 - t0) / sample * threads:.0f} us/pair/core, "
-                           f"scale {1e6 * (t2 - t1) / sample * threads:.1f} us/num/core")
+    H = O.PATH_HOST
+
+    def timed(fn, count, cores):
+        t0 = time.perf_counter()
+        fn(cores)
+        return count / (time.perf_counter() - t0) / 1e6
+
+    def run(name, call, count, count1, **info):
+        if which is not None and name not in which:
+            return
+        all_c = timed(call(count), count, threads)
+        one_c = timed(call(count1), count1, 1)
+        res[name] = dict(Mnum_s=all_c, Mnum_s_1core=one_c, sample=count, sample_1core=count1, **info)
+
+    res = {}
+    k = lambda c: max(64, int(c * scale))  # noqa: E731
+    # n = 32 (960 bits): division, scaling, evaluation, comparison
+    m32 = O.greedy_moduli(N32)
+    o32 = O.Oracle(m32)
+    nd = k(8192)
+    ne = k(1 << 18)
+    x = W.uniform_residues(m32, max(ne, nd), SEED, W.S_X, layout="aos")
+    y = W.uniform_residues(m32, max(ne, nd), SEED, W.S_Y, layout="aos")
+    d, _ = W.divisors(m32, o32.log2M, nd, SEED, layout="aos")
+    D = W.shifts(nd, DMAX, SEED)
+    run("div_n32", lambda c: lambda t: o32.div(x[:c], d[:c], path=H, fast=0, threads=t), nd, max(16, nd // 64),
+        ref="rns_div (src/rnsdiv.cuh:19), one quotient bit per iteration")
+    run("div_fast_n32", lambda c: lambda t: o32.div(x[:c], d[:c], path=H, fast=1, threads=t), nd, max(64, nd // 8),
+        ref="rns_div_fast (src/rnsdiv.cuh:67)")
+    run("scale2pow_n32", lambda c: lambda t: o32.scale2pow(y[:c], D[:c], path=H, threads=t), nd, max(64, nd // 8),
+        ref="rns_scale2pow (src/rnsscal.cuh:93)")
+    run("eval_n32", lambda c: lambda t: o32.eval(x[:c], path=H, threads=t), ne, max(256, ne // 8),
+        ref="rns_eval_compute (src/rnseval.cuh:29)")
+    run("eval_cmp_n32", lambda c: lambda t: o32.cmp(x[:c], y[:c], path=H, threads=t), ne, max(256, ne // 8),
+        ref="rns_cmp (src/rnscmp.cuh:20), two evaluations per pair")
+    if which is not None and not any(w.endswith(("_n8", "_n64")) for w in which):
+        return res, threads
+    # n = 8 (240 bits): comparison
+    m8 = O.greedy_moduli(8)
+    o8 = O.Oracle(m8)
+    x8 = W.uniform_residues(m8, ne, SEED, W.S_X, layout="aos")
+    y8 = W.uniform_residues(m8, ne, SEED, W.S_Y, layout="aos")
+    run("eval_cmp_n8", lambda c: lambda t: o8.cmp(x8[:c], y8[:c], path=H, threads=t), ne, max(256, ne // 8),
+        ref="rns_cmp (src/rnscmp.cuh:20)")
+    # n = 64 (1920 bits): mp_int add / sub / mul, magnitudes below 2^950
+    m64 = O.greedy_moduli(64)
+    o64 = O.Oracle(m64)
+    nm = k(1 << 16)
+    ma = o64.mpint_from_ints(W.mpint_values(nm, MP_BITS, SEED), path=H)
+    mc = o64.mpint_from_ints(W.mpint_values(nm, MP_BITS, SEED + 1), path=H)
+    for op in ("add", "sub", "mul"):
+        run(f"mpint_{op}_n64", lambda c, op=op: lambda t: o64.mpint(op, ma[:c], mc[:c], path=H, threads=t), nm,
+            max(256, nm // 8), ref=f"mpint_{op} (src/mpint.cuh:{ {'add': 160, 'sub': 215, 'mul': 270}[op] })")
+    return res, threads
+
+
+def cpu_baseline(threads=None, scale=1.0, every_op=True):
+    """the headline's CPU figure: division (the faster of host rns_div and
+    rns_div_fast, which give the same q and r) plus power-of-two scaling at
+    n = 32, as numbers per second over the two ops; and each op's figure
+    (every op of the path, or the headline's three)"""
+    ops, threads = cpu_ops(threads, scale, None if every_op else HEADLINE_OPS)
+    div = max(ops["div_n32"]["Mnum_s"], ops["div_fast_n32"]["Mnum_s"])
+    div1 = max(ops["div_n32"]["Mnum_s_1core"], ops["div_fast_n32"]["Mnum_s_1core"])
+    sc, sc1 = ops["scale2pow_n32"]["Mnum_s"], ops["scale2pow_n32"]["Mnum_s_1core"]
+    rate = 2.0 / (1.0 / div + 1.0 / sc)
+    rate1 = 2.0 / (1.0 / div1 + 1.0 / sc1)
+    desc = (f"{ops['div_fast_n32']['sample']} div pairs + {ops['scale2pow_n32']['sample']} scale2pow numbers "
+            f"(n=32, the workload's generators); host path restated in oracle/ (bit-identical to the reference "
+            f"compiled for the CPU), {threads} threads; division = the faster of rns_div "
+            f"({ops['div_n32']['Mnum_s'] * 1e6:.0f}/s) and rns_div_fast ({ops['div_fast_n32']['Mnum_s'] * 1e6:.0f}/s); "
+            f"one core: {rate1:.4f} Mnum/s")
+    return rate, threads, desc, ops
 
 
 def run_reference(args):
@@ -171,18 +236,20 @@ def run_reference(args):
     if rank != 0:
         return
     vals = []
-    for i in range(args.warmup + args.steps):
-        v, cores, desc = cpu_baseline(sample=2048)
+    for i in range(args.warmup + args.steps):  # a step: the headline's ops on a bounded sample
+        v, cores, desc, ops = cpu_baseline(scale=0.5, every_op=False)
         if i >= args.warmup:
             vals.append(v)
     v = statistics.median(vals)
+    ops, _ = cpu_ops(cores)  # every op of the path once, for the record
     line = {"impl": "reference", "metric": "RNS Mnum/s div+scale2pow (960-bit, n=32)", "value": v,
             "unit": "Mnum/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
             "data": "synthetic (seeded splitmix64 generator)",
             "config": {"workload": "div 2^18 pairs + scale2pow 2^18 numbers, n=32 greedy moduli from 2^30-1",
-                       "sample_per_step": "2048 div pairs + 2048 scale2pow numbers"},
-            "cpu_baseline": {"value": v, "unit": "Mnum/s", "cores": cores, "kind": "port", "sample": desc},
+                       "sample_per_step": desc.split(";")[0]},
+            "cpu_baseline": {"value": v, "unit": "Mnum/s", "cores": cores, "kind": "port", "sample": desc,
+                             "ops": ops},
             "e2e": {"value": v, "unit": "Mnum/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -453,16 +520,35 @@ def bench_next_ops(ctx_for, L, dev, stream, sp, P, seed, steps, flush, peak):
 # batched uneven workload (n = 32): one persistent launch (CUDA graph) vs one plain call per job
 
 def bench_batched(ctx_for, L, dev, stream, sp, P, seed, steps, flush):
+    """three uneven job sets at n = 32 (4096 jobs, log-uniform lengths): the
+    mixed one (eval+cmp, div, scale2pow, max), eval+cmp only and div only --
+    each as one persistent launch (CUDA graph) and as one plain call per job"""
+    import ctypes
+    from grns_gb300 import native
+    c = ctx_for(32)
+    tuned = {}
+    for op in (native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX):
+        sc, ms = native.Schedule(), ctypes.c_double()
+        native.check(L.grns_autotune(c.handle, op, 1 << 18, None, ctypes.byref(sc), ctypes.byref(ms)))
+        tuned[str(op)] = {"coop": sc.coop, "chunk": sc.chunk}
+    out = {"schedules": tuned}
+    sets = (("mixed", (native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX)),
+            ("eval_cmp_only", (native.OP_CMP,)), ("div_only", (native.OP_DIV,)))
+    for k, (name, ops) in enumerate(sets):
+        out[name] = batched_job_set(c, L, dev, stream, sp, seed + k, steps, flush, ops)
+    return out
+
+
+def batched_job_set(c, L, dev, stream, sp, seed, steps, flush, op_choices):
     import random
     import ctypes
     import torch
     from grns_gb300 import native
     from grns_gb300.workload import S_X, S_Y
-    c = ctx_for(32)
     n = 32
     rng = random.Random(seed)
     lens = log_uniform_lengths(rng, BATCH_JOBS, *BATCH_LEN)
-    ops = [rng.choice((native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX)) for _ in lens]
+    ops = [rng.choice(op_choices) for _ in lens]
     pool = max(lens)
     # operand pools in the reference's AoS layout: a job is a window [o, o + len) of them
     X = torch.empty((pool, n), dtype=torch.int32, device=dev)
@@ -474,7 +560,7 @@ def bench_batched(ctx_for, L, dev, stream, sp, P, seed, steps, flush):
     native.check(L.grns_gen_divisors(c.handle, seed, pool, 1, P(Dv), sp))
     native.check(L.grns_gen_shifts(seed, pool, DMAX, P(Sh), sp))
     offs = [rng.randrange(pool - ln + 1) for ln in lens]
-    # outputs: one region per kind, carved per job
+    # outputs: one region per kind, carved per job (every job writes its own outputs)
     tot = {op: sum(ln for ln, o in zip(lens, ops) if o == op) for op in set(ops)}
     q_all = torch.empty(max(1, tot.get(native.OP_DIV, 0)) * n, dtype=torch.int32, device=dev)
     r_all = torch.empty_like(q_all)
@@ -514,20 +600,15 @@ def bench_batched(ctx_for, L, dev, stream, sp, P, seed, steps, flush):
             calls.append((L.grns_max, (c.handle, a, ln, 1, o0, o1, None, 0, sp)))
     total = sum(lens)
 
-    def per_call(sub=calls):
-        for fn, args in sub:
+    def per_call():
+        for fn, args in calls:
             native.check(fn(*args))
 
-    # plain per-call form (integer fast path)
+    # plain per-call form (integer fast path), one call per job
     per_call()
     torch.cuda.synchronize()
     t_call = statistics.median(time_calls(per_call, max(2, steps // 2), stream, flush))
-    # autotuned schedules, then one persistent launch captured as a CUDA graph
-    tuned = {}
-    for op in (native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX):
-        sc, ms = native.Schedule(), ctypes.c_double()
-        native.check(L.grns_autotune(c.handle, op, 1 << 18, None, ctypes.byref(sc), ctypes.byref(ms)))
-        tuned[str(op)] = {"coop": sc.coop, "chunk": sc.chunk}
+    # one persistent launch of every job, captured as a CUDA graph
     h = ctypes.c_void_p()
     native.check(L.grns_batch_create(c.handle, jobs, BATCH_JOBS, 1, ctypes.byref(h)))
     launch = lambda: native.check(L.grns_batch_launch(h, sp))  # noqa
@@ -536,28 +617,18 @@ def bench_batched(ctx_for, L, dev, stream, sp, P, seed, steps, flush):
     torch.cuda.synchronize()
     t_batch = statistics.median(time_calls(launch, max(3, steps), stream, flush))
     L.grns_batch_destroy(h)
-    # the reference-faithful per-call form on a sample: the 64 shortest jobs (its division is
-    # orders of magnitude slower, so the full job list would take minutes)
-    L.grns_ctx_set_path(c.handle, 1)
-    samp = sorted(range(BATCH_JOBS), key=lambda k: lens[k])[:64]
-    sub = [calls[k] for k in samp]
-    per_call(sub)
-    torch.cuda.synchronize()
-    t_ref = statistics.median(time_calls(lambda: per_call(sub), 2, stream, flush))
-    L.grns_ctx_set_path(c.handle, 0)
-    ref_numbers = sum(lens[k] for k in samp)
-    return {
+    names = {native.OP_CMP: "eval+cmp", native.OP_DIV: "div", native.OP_SCALE2POW: "scale2pow",
+             native.OP_MAX: "max"}
+    res = {
         "jobs": BATCH_JOBS, "numbers": total, "lengths": f"log-uniform [{BATCH_LEN[0]:g}, {BATCH_LEN[1]:g}]",
-        "ops": "uniform over eval+cmp, div, scale2pow, max; AoS operand windows",
+        "ops": "uniform over " + ", ".join(names[o] for o in op_choices) + "; AoS operand windows",
         "batched_Mnum_s": total / (t_batch * 1e-3) / 1e6, "batched_ms": t_batch,
         "per_call_Mnum_s": total / (t_call * 1e-3) / 1e6, "per_call_ms": t_call,
-        "batched_vs_per_call": t_call / t_batch,
-        "reference_path_per_call_Mnum_s": ref_numbers / (t_ref * 1e-3) / 1e6,
-        "reference_path_sample": f"the {len(samp)} shortest jobs ({ref_numbers} numbers), reference-faithful "
-                                 "kernels, one plain call per job",
-        "batched_vs_reference_path_per_call": (total / t_batch) / (ref_numbers / t_ref),
-        "schedules": tuned, "graph": True,
+        "batched_vs_per_call": t_call / t_batch, "graph": True,
     }
+    del X, Y, Dv, Sh, q_all, r_all, s_all, c_all, mv_all, mi_all
+    torch.cuda.empty_cache()
+    return res
 
 
 # ---------------------------------------------------------------------------
@@ -859,8 +930,9 @@ def main():
     }
     line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu:
-        v, cores, desc = cpu_baseline()
-        line["cpu_baseline"] = {"value": v, "unit": "Mnum/s", "cores": cores, "kind": "port", "sample": desc}
+        v, cores, desc, ops = cpu_baseline()
+        line["cpu_baseline"] = {"value": v, "unit": "Mnum/s", "cores": cores, "kind": "port", "sample": desc,
+                                "ops": ops}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

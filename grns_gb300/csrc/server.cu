@@ -8,15 +8,23 @@
  * eval request's output is remembered as that array's evaluation so later
  * comparisons read 32-byte intervals instead of the residues.  A scheduler
  * thread:
- *   - admits pending requests in arrival order while their HBM footprint
- *     (output arrays) fits the budget, allocating outputs from the server's
- *     memory pool (stream-ordered, no device-wide synchronisation);
- *   - packs the admitted requests of one moduli set into ONE launch of the
- *     persistent batched kernel on a free launch slot (stream); with several
- *     slots, requests arriving while launches are in flight are admitted and
- *     launched alongside them, so their work overlaps on the device;
+ *   - gives each free launch slot (stream) the moduli set of the oldest
+ *     pending request that can run, and packs every pending request of that
+ *     set whose HBM footprint (output arrays) fits the budget into ONE launch
+ *     of the persistent batched kernel, allocating outputs from the server's
+ *     memory pool (stream-ordered, no device-wide synchronisation).  A
+ *     request that does not fit is passed by later ones that do, until it has
+ *     waited kPassCapUs: then nothing is admitted past it, so freed memory
+ *     goes to it.  With several slots, requests arriving while launches are
+ *     in flight are admitted and launched alongside them, so their work
+ *     overlaps on the device;
  *   - marks requests done from a host callback at the end of each launch and
  *     records submit-to-completion latency (p50/p99 in grns_server_stats).
+ * Each array counts the unfinished requests that read it (counted at
+ * submission, and for a cached evaluation when a launch uses it); freeing an
+ * array waits until that count is zero.  A finished request's status and
+ * output handles stay readable for kKeepFinishedUs after it finishes and are
+ * then dropped (at most kKeepFinishedMax finished requests are kept).
  * Every per-element computation is independent of its neighbours, so a
  * result does not depend on what else shares its launch.
  */
@@ -37,6 +45,10 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+constexpr double kPassCapUs = 50e3;          // after this wait for memory, later requests stop passing one
+constexpr double kKeepFinishedUs = 60e6;     // finished requests stay readable this long
+constexpr size_t kKeepFinishedMax = 1 << 16; // and at most this many of them
+
 double now_us() {
     return std::chrono::duration<double, std::micro>(Clock::now().time_since_epoch()).count();
 }
@@ -50,6 +62,7 @@ struct Array {
     size_t bytes = 0;
     uint64_t eval = 0;      // handle of this array's evaluation (RNS arrays), 0 if none
     uint64_t producer = 0;  // request that writes it (0: put by the client)
+    int readers = 0;        // unfinished requests that read it
 };
 
 struct Req {
@@ -60,6 +73,7 @@ struct Req {
     size_t footprint = 0;
     int64_t count = 0;
     double t_submit = 0, t_done = 0;
+    uint64_t reads[4] = {0, 0, 0, 0};  // arrays whose reader count this request holds
 };
 
 struct Slot {
@@ -92,6 +106,7 @@ struct grns_server {
     std::unordered_map<uint64_t, Array> arrays;
     std::unordered_map<uint64_t, Req> reqs;
     std::deque<uint64_t> pending;
+    std::deque<std::pair<uint64_t, double>> finished;  // (request, completion time), oldest first
     std::vector<Slot *> slots;
     uint64_t next_handle = 1, next_req = 1;
     size_t in_use = 0;
@@ -119,6 +134,38 @@ void CUDART_CB on_launch_done(void *arg) {
     sl->t_done = now_us();
     sl->done.store(1, std::memory_order_release);
     sl->srv->cv.notify_all();
+}
+
+/* true when request `id` has finished (or has been dropped after finishing) */
+bool req_finished(const grns_server *sv, uint64_t id) {
+    auto it = sv->reqs.find(id);
+    return it == sv->reqs.end() || it->second.state == 2;
+}
+
+/* the request holds a reader count on array h until it finishes */
+void hold_read(grns_server *sv, Req &q, uint64_t h) {
+    auto it = h ? sv->arrays.find(h) : sv->arrays.end();
+    if (it == sv->arrays.end()) return;
+    for (uint64_t &slot : q.reads)
+        if (!slot) {
+            slot = h;
+            it->second.readers++;
+            return;
+        }
+}
+
+/* marks a request finished: status, time, reader counts released */
+void finish(grns_server *sv, uint64_t id, Req &q, int32_t status, double t) {
+    q.state = 2;
+    q.status = status;
+    q.t_done = t;
+    for (uint64_t &h : q.reads) {
+        auto it = h ? sv->arrays.find(h) : sv->arrays.end();
+        if (it != sv->arrays.end() && it->second.readers > 0) it->second.readers--;
+        h = 0;
+    }
+    sv->finished.emplace_back(id, t);
+    sv->cv.notify_all();
 }
 
 grns_status alloc_array(grns_server *sv, cudaStream_t s, int ctx, int kind, int64_t count, int layout, Array &a) {
@@ -159,9 +206,10 @@ void schedule_locked(grns_server *sv) {
     for (Slot *sl : sv->slots) {
         if (!sl->busy || !sl->done.load(std::memory_order_acquire)) continue;
         for (uint64_t id : sl->reqs) {
-            Req &q = sv->reqs[id];
-            q.state = 2;
-            q.t_done = sl->t_done;
+            auto it = sv->reqs.find(id);
+            if (it == sv->reqs.end()) continue;
+            Req &q = it->second;
+            finish(sv, id, q, q.status, sl->t_done);
             sv->lat.push_back(q.t_done - q.t_submit);
             sv->completed++;
             sv->numbers += (double)q.count;
@@ -172,38 +220,60 @@ void schedule_locked(grns_server *sv) {
         sl->done.store(0);
     }
     const double now = now_us();
-    while (!sv->pending.empty()) {  /* requests that waited too long for memory */
-        Req &q = sv->reqs[sv->pending.front()];
-        if (now - q.t_submit < 1e3 * sv->opt.admission_timeout_ms) break;
-        q.state = 2;
-        q.status = GRNS_ERR_REJECTED;
-        q.t_done = now;
+    /* finished requests past their retention */
+    while (!sv->finished.empty() &&
+           (now - sv->finished.front().second > kKeepFinishedUs || sv->finished.size() > kKeepFinishedMax)) {
+        auto it = sv->reqs.find(sv->finished.front().first);
+        if (it != sv->reqs.end() && it->second.state == 2) sv->reqs.erase(it);
+        sv->finished.pop_front();
+    }
+    /* requests that waited too long for memory */
+    for (auto it = sv->pending.begin(); it != sv->pending.end();) {
+        Req &q = sv->reqs.at(*it);
+        if (now - q.t_submit < 1e3 * sv->opt.admission_timeout_ms) {
+            ++it;
+            continue;
+        }
+        finish(sv, *it, q, GRNS_ERR_REJECTED, now);
         sv->rejected++;
-        sv->pending.pop_front();
+        it = sv->pending.erase(it);
     }
     for (Slot *sl : sv->slots) {
         if (sl->busy || sv->pending.empty()) continue;
-        const int ctx = sv->reqs[sv->pending.front()].r.ctx_index;
+        int ctx = -1;  // the moduli set of this launch: that of the oldest request admitted
         std::vector<grns_job> jobs, divs;
-        while (!sv->pending.empty() && (int)(jobs.size() + divs.size()) < sv->opt.max_jobs_per_launch) {
-            const uint64_t id = sv->pending.front();
-            Req &q = sv->reqs[id];
-            if (q.r.ctx_index != ctx) break;
-            if (sv->in_use + q.footprint > sv->opt.hbm_budget_bytes) break;  // wait for memory (arrival order kept)
-            {  /* operands written by requests still in flight: wait for them (arrival order kept) */
-                auto busy = [&](uint64_t h) {
-                    auto it = sv->arrays.find(h);
-                    return it != sv->arrays.end() && it->second.producer && sv->reqs[it->second.producer].state != 2;
-                };
-                if (busy(q.r.a) || (q.r.b && busy(q.r.b))) break;
-            }
-            if (sv->arrays.find(q.r.a) == sv->arrays.end() || (q.r.b && sv->arrays.find(q.r.b) == sv->arrays.end())) {
-                sv->pending.pop_front();  // an operand was freed before the request ran
-                q.state = 2;
-                q.status = GRNS_ERR_INVALID_ARGUMENT;
-                q.t_done = now_us();
+        for (auto it = sv->pending.begin();
+             it != sv->pending.end() && (int)(jobs.size() + divs.size()) < sv->opt.max_jobs_per_launch;) {
+            const uint64_t id = *it;
+            Req &q = sv->reqs.at(id);
+            if (ctx >= 0 && q.r.ctx_index != ctx) {
+                ++it;
                 continue;
             }
+            {  /* operands written by requests still in flight: not runnable yet */
+                auto busy = [&](uint64_t h) {
+                    auto a = sv->arrays.find(h);
+                    return a != sv->arrays.end() && a->second.producer && !req_finished(sv, a->second.producer);
+                };
+                if (busy(q.r.a) || (q.r.b && busy(q.r.b))) {
+                    ++it;
+                    continue;
+                }
+            }
+            if (sv->arrays.find(q.r.a) == sv->arrays.end() || (q.r.b && sv->arrays.find(q.r.b) == sv->arrays.end())) {
+                /* a defensive guard: freeing an array waits for the requests that read it, so an
+                 * operand of a pending request is never gone; counted as a rejection */
+                finish(sv, id, q, GRNS_ERR_INVALID_ARGUMENT, now_us());
+                sv->rejected++;
+                it = sv->pending.erase(it);
+                continue;
+            }
+            if (sv->in_use + q.footprint > sv->opt.hbm_budget_bytes) {
+                if (now - q.t_submit > kPassCapUs) break;  // no later request passes it any more
+                ++it;                                      // later requests that fit go first
+                continue;
+            }
+            ctx = q.r.ctx_index;
             const grns_ctx *c = sv->ctxs[ctx];
             const Array A = sv->arrays[q.r.a];  /* copies: inserting outputs below may rehash the map */
             Array Bv;
@@ -225,15 +295,13 @@ void schedule_locked(grns_server *sv) {
                 case GRNS_OP_MAX: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_MAXOUT, 1, 0, o0); break;
                 default: st = alloc_array(sv, sl->s, ctx, GRNS_ARRAY_MPINT, q.count, 0, o0); break;
             }
-            sv->pending.pop_front();
+            it = sv->pending.erase(it);
             if (st != GRNS_OK) {
                 if (o0.p) {
                     cudaFreeAsync(o0.p, sl->s);
                     sv->allocated -= std::min(sv->allocated, o0.bytes);
                 }
-                q.state = 2;
-                q.status = st;
-                q.t_done = now_us();
+                finish(sv, id, q, st, now_us());
                 continue;
             }
             sv->in_use += q.footprint;
@@ -259,12 +327,16 @@ void schedule_locked(grns_server *sv) {
                 j.layout = GRNS_LAYOUT_SOA;
             } else if (q.r.op == GRNS_OP_MAX) {
                 j.out1 = (char *)o0.p + ((4 * (size_t)c->n + 7) / 8) * 8;
-            } else if (q.r.op == GRNS_OP_CMP && A.eval && B && B->eval && sv->arrays[A.eval].count >= q.count &&
-                       sv->arrays[B->eval].count >= q.count &&
-                       sv->reqs[sv->arrays[A.eval].producer].state == 2 &&
-                       sv->reqs[sv->arrays[B->eval].producer].state == 2) {  /* finished evaluations only */
-                j.eval_a = (const interval_t *)sv->arrays[A.eval].p;
-                j.eval_b = (const interval_t *)sv->arrays[B->eval].p;
+            } else if (q.r.op == GRNS_OP_CMP && A.eval && B && B->eval) {  /* finished evaluations only */
+                auto ea = sv->arrays.find(A.eval), eb = sv->arrays.find(B->eval);
+                if (ea != sv->arrays.end() && eb != sv->arrays.end() && ea->second.count >= q.count &&
+                    eb->second.count >= q.count && req_finished(sv, ea->second.producer) &&
+                    req_finished(sv, eb->second.producer)) {
+                    j.eval_a = (const interval_t *)ea->second.p;
+                    j.eval_b = (const interval_t *)eb->second.p;
+                    hold_read(sv, q, A.eval);  // freeing them now waits for this launch
+                    hold_read(sv, q, B->eval);
+                }
             }
             if (q.r.op == GRNS_OP_EVAL && q.count == A.count) sv->arrays[q.r.a].eval = q.out0;
             q.state = 1;
@@ -281,12 +353,7 @@ void schedule_locked(grns_server *sv) {
             st = grns::launch_mpint(sv->ctxs[ctx], 3, divs[t].a, divs[t].b, divs[t].count, divs[t].out0, nullptr, sl->s);
         if (st == GRNS_OK) st = grns::cuda_status(cudaLaunchHostFunc(sl->s, on_launch_done, sl));
         if (st != GRNS_OK) {
-            for (uint64_t id : sl->reqs) {
-                Req &q = sv->reqs[id];
-                q.state = 2;
-                q.status = st;
-                q.t_done = now_us();
-            }
+            for (uint64_t id : sl->reqs) finish(sv, id, sv->reqs.at(id), st, now_us());
             sl->reqs.clear();
             continue;
         }
@@ -310,11 +377,22 @@ void worker_main(grns_server *sv) {
 bool wait_done(grns_server *sv, std::unique_lock<std::mutex> &lk, uint64_t id, int64_t timeout_us) {
     const int64_t cap = (int64_t)600 * 1000 * 1000;  // 10 minutes
     auto until = Clock::now() + std::chrono::microseconds(timeout_us < 0 || timeout_us > cap ? cap : timeout_us);
-    while (sv->reqs[id].state != 2) {
+    while (!req_finished(sv, id)) {
         if (Clock::now() >= until) return false;
         sv->cv.wait_for(lk, std::chrono::milliseconds(1));
     }
     return true;
+}
+
+/* waits (bounded) until no unfinished request reads array h; false on timeout */
+bool wait_unread(grns_server *sv, std::unique_lock<std::mutex> &lk, uint64_t h) {
+    auto until = Clock::now() + std::chrono::minutes(10);
+    for (;;) {
+        auto it = sv->arrays.find(h);
+        if (it == sv->arrays.end() || it->second.readers == 0) return true;
+        if (Clock::now() >= until) return false;
+        sv->cv.wait_for(lk, std::chrono::milliseconds(1));
+    }
 }
 
 }  // namespace
@@ -455,25 +533,10 @@ grns_status grns_server_free(grns_server *sv, uint64_t h) {
     if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
     const uint64_t prod = it->second.producer;
     if (prod && !wait_done(sv, lk, prod, -1)) return GRNS_ERR_TIMEOUT;
-    /* unfinished requests that read this array (as an operand, or as the
-     * cached evaluation of one): wait for them, so no launch reads freed memory */
-    auto reads = [&](const Req &q) {
-        auto evaluated_as = [&](uint64_t operand) {
-            auto a = operand ? sv->arrays.find(operand) : sv->arrays.end();
-            return a != sv->arrays.end() && a->second.eval == h;
-        };
-        return q.r.a == h || q.r.b == h || evaluated_as(q.r.a) || evaluated_as(q.r.b);
-    };
-    for (;;) {
-        uint64_t reader = 0;
-        for (const auto &kv : sv->reqs)
-            if (kv.second.state != 2 && reads(kv.second)) {
-                reader = kv.first;
-                break;
-            }
-        if (!reader) break;
-        if (!wait_done(sv, lk, reader, -1)) return GRNS_ERR_TIMEOUT;
-    }
+    /* unfinished requests that read this array (as an operand, or a launch
+     * reading it as a cached evaluation): wait for them, so no launch reads
+     * freed memory */
+    if (!wait_unread(sv, lk, h)) return GRNS_ERR_TIMEOUT;
     it = sv->arrays.find(h);
     if (it == sv->arrays.end()) return GRNS_ERR_INVALID_ARGUMENT;
     cudaFreeAsync(it->second.p, sv->copy);
@@ -515,10 +578,10 @@ grns_status grns_server_submit(grns_server *sv, const grns_request *r, uint64_t 
     q.t_submit = now_us();
     if (sv->t_first == 0) sv->t_first = q.t_submit;
     *request_id = id;
+    hold_read(sv, q, r->a);
+    if (r->b) hold_read(sv, q, r->b);
     if (q.footprint > sv->opt.hbm_budget_bytes) {  // can never be admitted
-        q.state = 2;
-        q.status = GRNS_ERR_REJECTED;
-        q.t_done = q.t_submit;
+        finish(sv, id, q, GRNS_ERR_REJECTED, q.t_submit);
         sv->rejected++;
         return GRNS_OK;
     }
@@ -545,7 +608,9 @@ grns_status grns_server_wait(grns_server *sv, uint64_t id, int64_t timeout_us, i
     std::unique_lock<std::mutex> lk(sv->mu);
     if (sv->reqs.find(id) == sv->reqs.end()) return GRNS_ERR_INVALID_ARGUMENT;
     if (!wait_done(sv, lk, id, timeout_us)) return GRNS_ERR_TIMEOUT;
-    const Req &q = sv->reqs[id];
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return GRNS_ERR_INVALID_ARGUMENT;  // dropped after its retention
+    const Req &q = it->second;
     if (status) *status = q.status;
     if (out0) *out0 = q.out0;
     if (out1) *out1 = q.out1;
@@ -562,11 +627,8 @@ grns_status grns_server_cancel(grns_server *sv, uint64_t id) {
     if (q.state == 2) return GRNS_OK;
     auto pos = std::find(sv->pending.begin(), sv->pending.end(), id);
     if (pos != sv->pending.end()) sv->pending.erase(pos);
-    q.state = 2;
-    q.status = GRNS_ERR_CANCELLED;
-    q.t_done = now_us();
+    finish(sv, id, q, GRNS_ERR_CANCELLED, now_us());
     sv->cancelled++;
-    sv->cv.notify_all();
     return GRNS_OK;
 }
 

@@ -38,13 +38,20 @@ class Server:
         return idx.value
 
     def put(self, ctx_index, array, kind=native.ARRAY_RNS, layout=0, count=None):
-        """array: torch CUDA tensor or numpy array (copied into server memory;
-        a CUDA tensor's pending work on the current stream finishes first,
-        since the server copies on its own stream)"""
+        """array: torch tensor or numpy array, copied into server memory as
+        contiguous bytes (int32 for RNS and U32 arrays, uint8 records for
+        mp_int arrays).  A CUDA tensor's pending work on the current stream
+        finishes first, since the server copies on its own stream; a tensor
+        written on another stream must be synchronised by the caller."""
+        want = {native.ARRAY_RNS: (4,), native.ARRAY_U32: (4,), native.ARRAY_MPINT: (1,)}.get(kind, (1, 4))
+        if array.dtype.itemsize not in want:
+            raise ValueError(f"array of kind {kind} must have elements of {want[0]} bytes, not {array.dtype}")
         if hasattr(array, "is_cuda") and array.is_cuda:
             import torch
+            array = array.contiguous()
             torch.cuda.current_stream(array.device).synchronize()
             src, on_dev = ctypes.c_void_p(array.data_ptr()), 1
+            self._keep = array
         else:
             array = np.ascontiguousarray(array)
             src, on_dev = ctypes.c_void_p(array.ctypes.data), 0

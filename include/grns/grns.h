@@ -334,10 +334,15 @@ grns_status grns_autotune_load(grns_ctx *ctx, const char *cache_path, int *appli
 /* ---- serving: a request stream with continuous batching ----
  * No counterpart in the reference.  Arrays live in server-owned device memory
  * (handles); requests name operand handles and get output handles.  A
- * scheduler thread admits requests in arrival order while their output
- * footprint fits the HBM budget, packs the admitted requests of one moduli
- * set into one launch of the batched kernel on a free launch slot, and keeps
- * admitting and launching while earlier launches run.  An eval request's
+ * scheduler thread gives each free launch slot the moduli set of the oldest
+ * pending request that can run and packs every pending request of that set
+ * whose output footprint fits the HBM budget into one launch of the batched
+ * kernel; a request that does not fit is passed by later ones that do until
+ * it has waited 50 ms, after which nothing is admitted past it.  It keeps
+ * admitting and launching while earlier launches run.  A finished request's
+ * status and output handles stay readable (poll, wait) for 60 s after it
+ * finishes, for at most the 65,536 most recent ones; later calls naming it
+ * return GRNS_ERR_INVALID_ARGUMENT.  An eval request's
  * output is remembered as its operand's evaluation; comparisons of two
  * evaluated arrays decide from the intervals first.  Latency = submit to
  * completion (host callback), summarised as p50 / p99. */

@@ -12,10 +12,10 @@ oracle/_ref/ is pre-included ahead of the reference's src/params.h, whose
 include guard (GRNS_PARAMS_H) then skips the shipped default set; the tag
 "ref8" keeps the shipped default set instead.
 
-Reads the reference sources where they lie (default /root/reference, or
-$GRNS_REFERENCE); writes only into oracle/_ref/.  When the sources or the
-GMP/MPFR runtime libraries are absent (e.g. on a machine without the
-reference checkout) it builds nothing and says so.
+Reads the reference sources where they lie -- the checkout named by the
+`ref` argument of build() or by $GRNS_REFERENCE (no default) -- and writes
+only into oracle/_ref/.  When no checkout is named, or its sources or the
+GMP/MPFR runtime libraries are absent, it builds nothing and says so.
 """
 import os
 import subprocess
@@ -26,7 +26,7 @@ from math import gcd
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
-REF = os.environ.get("GRNS_REFERENCE", "/root/reference")
+REF = os.environ.get("GRNS_REFERENCE")  # the reference checkout (build(ref=...) overrides)
 
 
 def greedy_moduli(n, start=2 ** 30 - 1):
@@ -115,9 +115,13 @@ def build_one(tag, gmp, mpfr):
     return out
 
 
-def build(tags=None, quiet=False):
-    """Compile the checker libraries; returns {tag: path} (empty if unavailable)."""
-    if not os.path.isdir(os.path.join(REF, "src")):
+def build(tags=None, quiet=False, ref=None):
+    """Compile the checker libraries from the checkout `ref` (else
+    $GRNS_REFERENCE); returns {tag: path} (empty if unavailable)."""
+    global REF
+    if ref:
+        REF = ref
+    if not REF or not os.path.isdir(os.path.join(REF, "src")):
         if not quiet:
             print(f"oracle/_ref: reference sources not found at {REF}; nothing built")
         return {}
@@ -134,6 +138,11 @@ def build(tags=None, quiet=False):
 
 
 if __name__ == "__main__":
-    res = build(sys.argv[1:] or None)
+    # python oracle/ref/build_ref.py [--ref CHECKOUT] [tag ...]
+    argv = sys.argv[1:]
+    where = None
+    if argv[:1] == ["--ref"]:
+        where, argv = argv[1], argv[2:]
+    res = build(argv or None, ref=where)
     for k, v in res.items():
         print(k, v)

@@ -13,7 +13,8 @@ mp_int division operands with the Euclidean sign cases, binary <-> RNS
 conversions through the reference's GMP routines, and the
 extended-range doubles of tests/test_verify_extrange.cu:115-117.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:
+    GRNS_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 (needs the reference checkout and libgmp/libmpfr; the fixtures it writes are
 committed, so the tests themselves never need the reference).
 """

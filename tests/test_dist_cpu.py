@@ -49,7 +49,8 @@ def _ref_worker(rank, world, port, out):
     import bench
     buf = io.StringIO()
     calls = []
-    bench.cpu_baseline = lambda sample=0, threads=None: (calls.append(sample) or (1.0, 1, "stub"))
+    bench.cpu_baseline = lambda threads=None, scale=1.0, every_op=True: (calls.append(scale) or (1.0, 1, "stub", {}))
+    bench.cpu_ops = lambda threads=None, scale=1.0, which=None: ({}, 1)
     with contextlib.redirect_stdout(buf):
         bench.run_reference(types.SimpleNamespace(gpus=world, steps=2, warmup=1))
     out[rank] = (buf.getvalue(), len(calls))

@@ -1,13 +1,16 @@
 """GPU: batched execution (one persistent launch for many uneven jobs, CUDA
 graph replay, n-threaded vs serial schedules, autotuner).  Every job's
-outputs must equal the per-call entry points' outputs bit for bit (those are
-checked against the oracle and exact arithmetic in test_gpu_parity.py)."""
+outputs must equal the per-call entry points' outputs bit for bit, and a
+seeded sample of every job's outputs must equal the oracle's (intervals,
+mp_int records) and exact big-integer arithmetic (signs, quotients and
+remainders, scaled values, the maximum and its index) -- tests/jobcheck.py."""
 import ctypes
 import random
 
 import pytest
 
-from oracle.oracle import greedy_moduli
+from oracle.oracle import Oracle, greedy_moduli
+from tests.jobcheck import check_job
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -32,7 +35,7 @@ def make_jobs(ctx, n, rng, njobs, stream):
     L = native.lib()
     jobs, bufs = [], []
     for t in range(njobs):
-        op = rng.choice([0, 1, 2, 3, 4, 5, 7])
+        op = rng.choice([0, 1, 2, 3, 4, 5, 6, 7])
         count = rng.choice([0, 1, 3, 31, 100, 1000, 5000, 20000 if op not in (2, 3) else 2000])
         layout = rng.choice([0, 1]) if op < 5 else 0
         j = native.Job()
@@ -41,8 +44,10 @@ def make_jobs(ctx, n, rng, njobs, stream):
             nb = mpint_bytes(n)
             a = torch.zeros(max(1, count) * nb, dtype=torch.uint8, device="cuda")
             b = torch.zeros_like(a)
-            if count:  # digits uniform, sign 0/1, evals left zero (valid enclosure of 0 only for 0)
-                pass
+            if count:  # signed operands whose products stay below M, evaluations from the device path
+                bits = L.grns_ctx_log2(ctx) // 2 - 10
+                native.check(L.grns_gen_mpint(ctx, 70 + t, count, bits, P(a), stream))
+                native.check(L.grns_gen_mpint(ctx, 170 + t, count, bits, P(b), stream))
             o0 = torch.zeros_like(a)
             j.a, j.b, j.out0 = a.data_ptr(), b.data_ptr(), o0.data_ptr()
             bufs.append((op, count, layout, a, b, o0, None))
@@ -121,6 +126,7 @@ def test_batch_matches_per_call(L, n, coop, graph):
     native.check(L.grns_ctx_create(mods, n, ctypes.byref(ctx)))
     s = torch.cuda.Stream()
     sp = ctypes.c_void_p(s.cuda_stream)
+    orc = Oracle(greedy_moduli(n))
     try:
         for op in (1, 4):
             sc = native.Schedule(coop, 256 if n == 8 else 1024)
@@ -145,6 +151,8 @@ def test_batch_matches_per_call(L, n, coop, graph):
                     assert torch.equal(o0, r0), (t, op, count, layout)
                     if o1 is not None:
                         assert torch.equal(o1, r1), (t, op, count, layout)
+                    if rep == 0:
+                        check_job(orc, op, count, layout, a, bb, o0, o1, seed=t)
         finally:
             L.grns_batch_destroy(b)
     finally:

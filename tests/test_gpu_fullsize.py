@@ -1,9 +1,12 @@
 """GPU: division and power-of-two scaling at the benchmark's sizes (2^18
 numbers each, n = 32, the benchmark's device generators), checked through
 size-independent properties (tests/fullsize_props.py) with the library's own
-comparison and evaluation; and the comparison against the evaluation at the
-same size.  The reference-faithful kernels are too slow at this size; the
-smaller parity tests cover them."""
+comparison and evaluation on every number, and exactly against Python big
+integers on a seeded sample of 4096 numbers spread over every 4096-number
+segment (each segment's longest divisions and largest shifts included); and
+the comparison against the evaluation at the same size.  The
+reference-faithful kernels are too slow at this size; the smaller parity
+tests cover them."""
 import ctypes
 
 import numpy as np
@@ -88,6 +91,64 @@ def test_scale2pow_full_size(env):
     cmp, lb = device_ops(ctx)
     bad = F.scale_violations(mods, aos(x), D.cpu().numpy().astype(np.uint32), aos(out), cmp, lb)
     assert len(bad) == 0, bad[:10]
+
+
+SEGMENT = 4096  # the division sorts and schedules its numbers in segments of this many
+
+
+def exact_sample(ctx, d_log2_upper, seed=7):
+    """indices of a seeded sample spread over every 4096-number segment: in each
+    segment the 16 smallest divisors (the longest quotients, the most digit
+    steps) and 48 uniform indices -- 4096 in all at 2^18 numbers"""
+    rng = np.random.default_rng(seed)
+    idx = []
+    for b0 in range(0, COUNT, SEGMENT):
+        seg = np.arange(b0, min(COUNT, b0 + SEGMENT))
+        longest = seg[np.argsort(d_log2_upper[seg], kind="stable")[:16]]
+        idx.append(longest)
+        idx.append(rng.choice(seg, 48, replace=False))
+    return np.unique(np.concatenate(idx))
+
+
+def test_division_full_size_exact_sample(env):
+    """the benchmark's own 2^18 divisions: q and r equal floor(X/d) and X mod d
+    (Python big integers) on a sample that covers every segment"""
+    from oracle.oracle import Exact
+    mods, ctx, x, y, d, D = env
+    q, r = ctx.rns_div(x, d)
+    cmp, lb = device_ops(ctx)
+    xa, da, qa, ra = aos(x), aos(d), aos(q), aos(r)
+    _, du = lb(da)
+    idx = exact_sample(ctx, du)
+    assert len(idx) >= 4096
+    ex = Exact(mods)
+    X, Dd = ex.from_rns(xa[idx]), ex.from_rns(da[idx])
+    Q, R = ex.from_rns(qa[idx]), ex.from_rns(ra[idx])
+    bad = [int(k) for k, a, b, qq, rr in zip(idx, X, Dd, Q, R) if (qq, rr) != divmod(a, b)]
+    assert not bad, bad[:10]
+    # the sample reaches the longest divisions: quotients of more than 900 bits
+    assert max(qq.bit_length() for qq in Q) > 900
+
+
+def test_scale2pow_full_size_exact_sample(env):
+    """the benchmark's own 2^18 scalings: floor(X / 2^D) (Python big integers)
+    on 64 numbers of every segment, including each segment's largest shifts"""
+    from oracle.oracle import Exact
+    mods, ctx, x, y, d, D = env
+    out = aos(ctx.rns_scale2pow(x, D))
+    xa, Dh = aos(x), D.cpu().numpy().astype(np.int64)
+    rng = np.random.default_rng(11)
+    idx = []
+    for b0 in range(0, COUNT, SEGMENT):
+        seg = np.arange(b0, min(COUNT, b0 + SEGMENT))
+        idx.append(seg[np.argsort(-Dh[seg], kind="stable")[:8]])
+        idx.append(rng.choice(seg, 56, replace=False))
+    idx = np.unique(np.concatenate(idx))
+    assert len(idx) >= 4096
+    ex = Exact(mods)
+    X, Y = ex.from_rns(xa[idx]), ex.from_rns(out[idx])
+    bad = [int(k) for k, a, yy in zip(idx, X, Y) if yy != a >> int(Dh[k])]
+    assert not bad, bad[:10]
 
 
 def test_cmp_agrees_with_evaluation_full_size(env):

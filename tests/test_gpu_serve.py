@@ -2,13 +2,16 @@
 stream over two resident moduli sets (n = 32 and n = 64), admission by HBM
 footprint, cached evaluations, latency stats.  Every request's result must be
 the same alone (through the per-call entry points, and alone through the
-server) and inside the mix."""
+server) and inside the mix, and a seeded sample of it must equal the oracle's
+and exact big-integer arithmetic (tests/jobcheck.py)."""
 import ctypes
 import random
 
+import numpy as np
 import pytest
 
-from oracle.oracle import greedy_moduli
+from oracle.oracle import Oracle, greedy_moduli
+from tests.jobcheck import check_job
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -43,6 +46,10 @@ def gen(native, ctx, count, stream_id, seed, divisors=False):
 def per_call(native, ctx, op, x, y, count):
     """the op through the per-call entry points on the first `count` numbers"""
     L = native.lib()
+    if op == "mpint_mul":
+        from grns_gb300 import mpint_bytes
+        nb = count * mpint_bytes(ctx.n)
+        return [ctx.mpint_mul(x[:nb], y[:nb])]
     xs = x[:, :count].contiguous()
     ys = y[:, :count].contiguous() if y is not None and y.dim() == 2 else y
     if op == "eval":
@@ -68,6 +75,23 @@ def per_call(native, ctx, op, x, y, count):
         native.check(L.grns_max(ctx.handle, P(xs), count, 0, P(v), P(i), None, 0, None))
         return [v, i]
     raise ValueError(op)
+
+
+def check_served(A, op, count, got, seed):
+    """a served result (the bytes server_bytes returns) against the oracle"""
+    n = A["ctx"].n
+    raw = np.frombuffer(got, np.uint8)
+    code = {"eval": 0, "cmp": 1, "div": 2, "scale2pow": 3, "max": 4, "mpint_mul": 7}[op]
+    if op == "max":
+        check_job(A["orc"], 4, count, 0, A["x"], None, raw[:4 * n], raw[4 * n:], seed=seed)
+    elif op == "div":
+        half = len(raw) // 2
+        check_job(A["orc"], 2, count, 0, A["x"], A["d"], raw[:half], raw[half:], seed=seed)
+    elif op == "mpint_mul":
+        check_job(A["orc"], 7, count, 0, A["ma"], A["mc"], raw, None, seed=seed)
+    else:
+        b = {"cmp": A["y"], "scale2pow": A["D"]}.get(op)
+        check_job(A["orc"], code, count, 0, A["x"], b, raw, None, seed=seed)
 
 
 def as_bytes(ts):
@@ -101,17 +125,27 @@ def test_results_alone_and_in_the_mix(env):
             y = gen(native, ctx, cnt, 2, 100 + n)
             d = gen(native, ctx, cnt, 0, 200 + n, divisors=True)
             D = torch.randint(1, 900, (cnt,), dtype=torch.int32, device="cuda")
-            arrays[n] = dict(ci=ci, ctx=ctx, x=x, y=y, d=d, D=D, cnt=cnt,
+            mb = G.mpint_bytes(n)
+            ma = torch.empty(cnt * mb, dtype=torch.uint8, device="cuda")
+            mc = torch.empty_like(ma)
+            bits = ctx.log2M // 2 - 10  # products stay below M
+            native.check(native.lib().grns_gen_mpint(ctx.handle, 300 + n, cnt, bits, P(ma), None))
+            native.check(native.lib().grns_gen_mpint(ctx.handle, 400 + n, cnt, bits, P(mc), None))
+            torch.cuda.synchronize()
+            arrays[n] = dict(ci=ci, ctx=ctx, x=x, y=y, d=d, D=D, ma=ma, mc=mc, cnt=cnt, orc=Oracle(ctx.moduli),
                              hx=srv.put(ci, x), hy=srv.put(ci, y), hd=srv.put(ci, d),
-                             hD=srv.put(ci, D, kind=native.ARRAY_U32))
+                             hD=srv.put(ci, D, kind=native.ARRAY_U32),
+                             hma=srv.put(ci, ma.view(cnt, mb), kind=native.ARRAY_MPINT),
+                             hmc=srv.put(ci, mc.view(cnt, mb), kind=native.ARRAY_MPINT))
         rng = random.Random(3)
         reqs = []
         for t in range(60):
             n = rng.choice([32, 64])
             A = arrays[n]
-            op = rng.choice(["eval", "cmp", "div", "scale2pow", "max"])
+            op = rng.choice(["eval", "cmp", "div", "scale2pow", "max", "mpint_mul"])
             count = rng.choice([1, 7, 100, 1000, 10000, A["cnt"]]) if op not in ("div",) else rng.choice([1, 50, 2000])
-            a, b = A["hx"], {"cmp": A["hy"], "div": A["hd"], "scale2pow": A["hD"]}.get(op, 0)
+            a = A["hma"] if op == "mpint_mul" else A["hx"]
+            b = {"cmp": A["hy"], "div": A["hd"], "scale2pow": A["hD"], "mpint_mul": A["hmc"]}.get(op, 0)
             reqs.append((n, op, count, a, b))
         # the mix: everything submitted back to back (they overlap on the device)
         ids = [srv.submit(op, arrays[n]["ci"], a, b, count) for (n, op, count, a, b) in reqs]
@@ -121,12 +155,15 @@ def test_results_alone_and_in_the_mix(env):
         assert 0 < st["p50_us"] <= st["p99_us"]
         assert st["launches"] < len(reqs)  # requests were packed into shared launches
         # each alone: through the server with nothing else queued, and through the per-call API
-        for (n, op, count, a, b), got in zip(reqs, mixed):
+        for t, ((n, op, count, a, b), got) in enumerate(zip(reqs, mixed)):
             A = arrays[n]
             alone = server_bytes(srv, srv.submit(op, A["ci"], a, b, count), op, n)
             assert alone == got, (n, op, count)
-            y = {"cmp": A["y"], "div": A["d"], "scale2pow": A["D"]}.get(op)
-            assert as_bytes(per_call(native, A["ctx"], op, A["x"], y, count)) == got, (n, op, count)
+            y = {"cmp": A["y"], "div": A["d"], "scale2pow": A["D"], "mpint_mul": A["mc"]}.get(op)
+            x = A["ma"] if op == "mpint_mul" else A["x"]
+            assert as_bytes(per_call(native, A["ctx"], op, x, y, count)) == got, (n, op, count)
+            # and the oracle / exact arithmetic on a sample of the mixed result
+            check_served(A, op, count, got, seed=t)
     finally:
         srv.close()
 
@@ -251,5 +288,45 @@ def test_served_mpint_division(env):
         assert all(st == 0 for st, _, _ in outs)
         assert srv.get(outs[1][1]).tobytes() == want
         assert srv.get(outs[2][1]).tobytes() == want[:777 * mb]
+    finally:
+        srv.close()
+
+
+def test_free_waits_for_pending_readers(env):
+    """freeing an operand and its cached evaluation right after submitting
+    requests that read them: each free returns OK once those requests have
+    finished, the results equal the per-call API's, and the freed handles are
+    gone (get fails)"""
+    G, native, ctxs = env
+    from grns_gb300.serve import Server
+    ctx = ctxs[32]
+    cnt = 1 << 17
+    x = gen(native, ctx, cnt, 1, 21)
+    y = gen(native, ctx, cnt, 2, 21)
+    d = gen(native, ctx, cnt, 0, 22, divisors=True)
+    srv = Server(slots=2)
+    try:
+        ci = srv.add_context(ctx)
+        hx, hy, hd = srv.put(ci, x), srv.put(ci, y), srv.put(ci, d)
+        evs = []
+        for h in (hx, hy):
+            st, ev, _ = srv.wait(srv.submit("eval", ci, h))
+            assert st == 0
+            evs.append(ev)
+        # a long division first, so the comparison (reading the cached evaluations) is still pending
+        r_div = srv.submit("div", ci, hx, hd)
+        r_cmp = srv.submit("cmp", ci, hx, hy)
+        for h in (evs[0], hx, evs[1]):  # operand and evaluations freed at once
+            srv.free(h)
+        for h in (evs[0], hx, evs[1]):
+            with pytest.raises(G.GrnsError):
+                srv.get(h)
+        st, c0, _ = srv.wait(r_cmp)
+        assert st == 0
+        st, q0, r0 = srv.wait(r_div)
+        assert st == 0
+        assert srv.get(c0).tobytes() == as_bytes(per_call(native, ctx, "cmp", x, y, cnt))
+        assert srv.get(q0).tobytes() + srv.get(r0).tobytes() == as_bytes(per_call(native, ctx, "div", x, d, cnt))
+        assert srv.stats()["rejected"] == 0
     finally:
         srv.close()
