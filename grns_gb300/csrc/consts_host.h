@@ -38,6 +38,7 @@ struct HostTables {
     uint64_t acc_lo = 0, acc_hi = 0;             // ceil(acc * 2^100)
     std::vector<uint32_t> c128w;                 // n x 4 words: ceil(2^128 w_i / m_i) mod 2^128
     std::vector<uint32_t> pow2neg, pow2neg_sh;   // kPow2NegRows x n: 2^-j mod m_i
+    std::vector<uint32_t> pow2neg64, pow2neg64_sh;  // pow2neg64_rows(log2M) x n: 2^-(64 a) mod m_i
     std::vector<uint64_t> mi64;                  // M_i mod 2^64
     uint64_t m64 = 0;                            // M mod 2^64
     uint64_t E = 0;  // sum_i (m_i - 1)
@@ -261,6 +262,21 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
             u = (u * half) % m[i];
         }
     }
+    /* division: 2^-(64 a) mod m_i, so 2^-s = pow2neg[s % 64] pow2neg64[s / 64] for every shift s <= log2M + 64 */
+    const int rows64 = pow2neg64_rows(T.log2M);
+    T.pow2neg64.resize((size_t)rows64 * n);
+    T.pow2neg64_sh.resize(T.pow2neg64.size());
+    for (int i = 0; i < n; i++) {
+        const uint64_t half = (m[i] + 1) / 2;
+        uint64_t step = 1;  // 2^-64 mod m_i
+        for (int j = 0; j < 64; j++) step = (step * half) % m[i];
+        uint64_t u = 1;
+        for (int a = 0; a < rows64; a++) {
+            T.pow2neg64[(size_t)a * n + i] = (uint32_t)u;
+            T.pow2neg64_sh[(size_t)a * n + i] = shoup((uint32_t)u, m[i]);
+            u = (u * step) % m[i];
+        }
+    }
     /* scaling: M_i mod 2^64 and M mod 2^64 */
     T.mi64.assign(n, 0);
     T.m64 = 1;
@@ -375,7 +391,7 @@ inline std::vector<uint32_t> table_blob(const HostTables &T) {
     std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows (every size below the
                                             conversion tables is a multiple of 4 words) */
     for (const auto *v : {&T.bin_p26, &T.bin_mi26, &T.bin_m26, &T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
-                          &T.pow2_inv_sh, &T.pow2neg, &T.pow2neg_sh})
+                          &T.pow2_inv_sh, &T.pow2neg, &T.pow2neg_sh, &T.pow2neg64, &T.pow2neg64_sh})
         blob.insert(blob.end(), v->begin(), v->end());
     return blob;
 }
@@ -442,7 +458,9 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     C.pow2_inv = blob + off;    off += T.pow2_inv.size();
     C.pow2_inv_sh = blob + off; off += T.pow2_inv_sh.size();
     C.pow2neg = blob + off;     off += T.pow2neg.size();
-    C.pow2neg_sh = blob + off;
+    C.pow2neg_sh = blob + off;  off += T.pow2neg_sh.size();
+    C.pow2neg64 = blob + off;   off += T.pow2neg64.size();
+    C.pow2neg64_sh = blob + off;
 }
 
 }  // namespace grns

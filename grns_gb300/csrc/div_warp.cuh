@@ -13,6 +13,9 @@
  * In both passes a finished lane stores its result and the lanes take the
  * next numbers of the range together once kDivRefill of them wait (one
  * coalesced batch of loads instead of one divergent load per finishing lane).
+ * The batched kernel runs the two passes over one warp's job chunk
+ * (div_range); the plain call runs them over the whole call through
+ * prepared rows, longest divisions first (divprep / divrow_range below).
  *
  * Memory layout: each thread owns a column of 3N words of shared memory
  * (R, D, Q rows, [row][stride], conflict-free), and the block holds one DivK
@@ -111,10 +114,10 @@ constexpr int kDivUnroll = 4;
 /* pass A over the numbers claim() hands out below end: rec[k] = record of
  * number k.  Column rows: the working value in rows [0, N), the dividend in
  * rows [N, 2N). */
-template <int N, class Claim>
-__device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
-                                              const Operand<N> &d, uint2 *rec, int64_t end, Claim claim,
-                                              int64_t prefetch, uint32_t *col, int stride) {
+template <int N, class Claim, class Finish>
+__device__ __forceinline__ void divnorm_range_f(const DivK *K, const Consts<N> &C, const Operand<N> &x,
+                                                const Operand<N> &d, Finish finish, int64_t end, Claim claim,
+                                                int64_t prefetch, uint32_t *col, int stride) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -130,7 +133,7 @@ __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C,
         const unsigned wt = __ballot_sync(FULL, ph == Done || ph == Idle);
         if (lv == 0 || __popc(wt) >= kDivRefill) {
             if (ph == Done) {
-                rec[idx] = out;
+                finish(idx, out, X);
                 ph = Idle;
             }
             const unsigned need = __ballot_sync(FULL, ph == Idle);
@@ -221,6 +224,15 @@ __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C,
             }
         }
     }
+}
+
+/* pass A writing records rec[k] (the batched kernel's per-warp form) */
+template <int N, class Claim>
+__device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
+                                              const Operand<N> &d, uint2 *rec, int64_t end, Claim claim,
+                                              int64_t prefetch, uint32_t *col, int stride) {
+    divnorm_range_f<N>(K, C, x, d, [&](int64_t idx, uint2 r, const uint32_t *) { rec[idx] = r; }, end, claim,
+                       prefetch, col, stride);
 }
 
 /* pass B over [begin, end) with the records of pass A, numbers taken in the
@@ -389,6 +401,259 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
     }
 }
 
+/* ---------------- the plain call's division through prepared rows ----------------
+ * (rns_fast.cuh: div_row_setup / div_row_final are the one-number forms)
+ *
+ * Pass A (divprep) runs divnorm_range_f and, as each number's normalisation
+ * ends, writes its row: the digit steps' starting state, or q and r at once.
+ * A global counting sort by step count (k_div_place, ops_div.cu) orders all
+ * numbers longest first; pass B (divrow_range) takes positions of that order
+ * from a grid-wide counter, reads each row with 16-byte loads, runs the
+ * steps and writes q and r back into the row; a last kernel moves them to
+ * the caller's layout.  The schedule is longest-processing-time first over
+ * the whole call (the grid ends on its shortest divisions), while every
+ * access to a number's data stays one contiguous row. */
+
+constexpr int kDivRowBins = 256;  // step counts 0..255 (a division takes at most (log2M + 49) / 48 + 1)
+
+/* pass A's row of one division (the device form of div_row_setup).  Xc: the
+ * dividend's residues in this lane's shared-memory column (stride `stride`);
+ * the divisor is read again from d; row: the number's row in global memory.
+ * Returns the digit steps (0: q and r written, flags set in f). */
+template <int N>
+__device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, uint2 rec, const uint32_t *Xc,
+                                             int stride, const Operand<N> &d, int64_t idx, uint32_t *row,
+                                             uint32_t &f) {
+    constexpr int P = kRowPad<N>();
+    const uint32_t status = rec.x >> 16;
+    uint32_t xnz = 0;
+#pragma unroll 8
+    for (int i = 0; i < N; i++) xnz |= Xc[i * stride];
+    if (status != kDnOk || !xnz) {  // no digit step: q = 0, r = x unless stated below
+        bool one = false;
+        if (status == kDnBad) f |= kFlagInvalidInput;  // q = r = 0
+        else if (status == kDnZero) f |= kFlagDivByZero;
+        else if (status == kDnCap) f |= kFxIterCap;
+        else if (status == kDnNear && xnz) {  // d > M (1 - E / 2^96): the quotient is 0 or 1
+            uint32_t a[N], b[N];
+            for (int i = 0; i < N; i++) {
+                a[i] = Xc[i * stride];
+                b[i] = d.load(idx, i);
+            }
+            one = dv_cmp_vec<N>(C, a, b) >= 0;
+        }
+#pragma unroll 1
+        for (int i0 = 0; i0 < P; i0 += 4) {
+            uint32_t qv[4], rv[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int i = i0 + j;
+                qv[j] = rv[j] = 0;
+                if (N % 4 == 0 || i < N) {
+                    const uint32_t xv = status == kDnBad ? 0u : Xc[i * stride];
+                    qv[j] = one ? 1u : 0u;
+                    rv[j] = one ? submod(xv, d.load(idx, i), K[i].a.x) : xv;
+                }
+            }
+            *reinterpret_cast<uint4 *>(row + i0) = make_uint4(qv[0], qv[1], qv[2], qv[3]);
+            *reinterpret_cast<uint4 *>(row + P + i0) = make_uint4(rv[0], rv[1], rv[2], rv[3]);
+        }
+        return 0;
+    }
+    const int s = (int)(rec.x & 0xffffu), e = dv_rec_e(rec);
+    const uint32_t *ps = C.pow2 + (int64_t)s * N, *pss = C.pow2_sh + (int64_t)s * N;
+    const uint32_t *pe = e < 0 ? C.pow2neg + (int64_t)(-e) * N : C.pow2 + (int64_t)e * N;
+    const uint32_t *pes = e < 0 ? C.pow2neg_sh + (int64_t)(-e) * N : C.pow2_sh + (int64_t)e * N;
+    Fx96 fd, fxx, fr;
+#pragma unroll 1
+    for (int i0 = 0; i0 < P; i0 += 4) {
+        uint32_t dv[4], rv[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int i = i0 + j;
+            dv[j] = rv[j] = 0;
+            if (N % 4 == 0 || i < N) {
+                const DivK k = K[i];
+                const uint32_t xv = Xc[i * stride];
+                dv[j] = mulmod_shoup(d.load(idx, i), __ldg(ps + i), __ldg(pss + i), k.a.x);
+                rv[j] = mulmod_shoup(xv, __ldg(pe + i), __ldg(pes + i), k.a.x);
+                fd.add(dv[j], k);
+                fxx.add(xv, k);
+                fr.add(rv[j], k);
+            }
+        }
+        *reinterpret_cast<uint4 *>(row + i0) = make_uint4(dv[0], dv[1], dv[2], dv[3]);
+        *reinterpret_cast<uint4 *>(row + P + i0) = make_uint4(rv[0], rv[1], rv[2], rv[3]);
+    }
+    DivSt st;
+    dv_setup(st, fd.value(), s, e);
+    const u128 U = (rec.y >> 31) ? (((u128)1) << 96) : (e < 0 ? fxx.value() : fr.value());
+    uint32_t h[kRowHdr];
+    div_hdr_put(h, st, U, s);
+    uint4 *hp = reinterpret_cast<uint4 *>(row + 2 * P);
+#pragma unroll
+    for (int j = 0; j < kRowHdr / 4; j++) hp[j] = make_uint4(h[4 * j], h[4 * j + 1], h[4 * j + 2], h[4 * j + 3]);
+    return st.left;
+}
+
+/* pass B over positions [0, end) of `order` (numbers with digit steps,
+ * longest first) claimed with claim(); rows: kRowWords(N) words per number.
+ * Column rows: R in [0, N), D in [N, 2N), Q in [2N, 3N). */
+template <int N, class Claim>
+__device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, uint32_t *rows,
+                                             const int32_t *order, uint8_t *flags, int64_t end, Claim claim,
+                                             uint32_t *col, int stride) {
+    constexpr int P = kRowPad<N>();
+    constexpr int RW = kRowWords<N>();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    enum { Idle, Iter, Final, Dead };
+    uint32_t *__restrict__ Rc = col;
+    uint32_t *__restrict__ Dc = col + N * stride;
+    uint32_t *__restrict__ Qc = col + 2 * N * stride;
+    DivSt st;
+    st.f = 0;
+    st.left = 0;
+    st.b = kDivB;
+    u128 U = 0;
+    int s = 0, ph = Idle;
+    uint32_t *row = rows;
+    int64_t idx = 0;
+    for (;;) {
+        const unsigned lv = __ballot_sync(FULL, ph == Iter);
+        const unsigned wt = __ballot_sync(FULL, ph == Final || ph == Idle);
+        if (lv == 0 || __popc(wt) >= kDivRefill) {
+            if (ph == Final) {  // q = Q + c, r = (R - c D) 2^-s, into the row
+                int c = dv_final_fx(st, U, C.E);
+                if (c < 0) {
+                    uint32_t a[N], b[N];
+                    for (int i = 0; i < N; i++) {
+                        a[i] = Rc[i * stride];
+                        b[i] = Dc[i * stride];
+                    }
+                    c = dv_final_exact<N>(C, a, b);
+                }
+                const uint32_t *pa = C.pow2neg + (int64_t)(s & 63) * N, *pas = C.pow2neg_sh + (int64_t)(s & 63) * N;
+                const uint32_t *pb = C.pow2neg64 + (int64_t)(s >> 6) * N;
+                const uint32_t *pbs = C.pow2neg64_sh + (int64_t)(s >> 6) * N;
+#pragma unroll 1
+                for (int i0 = 0; i0 < P; i0 += 4) {
+                    uint32_t qv[4], rv[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const int i = i0 + j;
+                        qv[j] = rv[j] = 0;
+                        if (N % 4 == 0 || i < N) {
+                            const DivK k = K[i];
+                            const uint32_t m = k.a.x, cm = (uint32_t)c % m;
+                            const uint32_t v = submod(Rc[i * stride], kmulmod(cm, Dc[i * stride], k), m);
+                            qv[j] = addmod(Qc[i * stride], cm, m);
+                            rv[j] = mulmod_shoup(mulmod_shoup(v, __ldg(pa + i), __ldg(pas + i), m), __ldg(pb + i),
+                                                 __ldg(pbs + i), m);
+                        }
+                    }
+                    *reinterpret_cast<uint4 *>(row + i0) = make_uint4(qv[0], qv[1], qv[2], qv[3]);
+                    *reinterpret_cast<uint4 *>(row + P + i0) = make_uint4(rv[0], rv[1], rv[2], rv[3]);
+                }
+                if (flags) flags[idx] = (uint8_t)st.f;
+                ph = Idle;
+            }
+            const unsigned need = __ballot_sync(FULL, ph == Idle);
+            const int64_t my = claim(__popc(need)) + __popc(need & lt);
+            if (ph == Idle) {
+                if (my < end) {
+                    idx = order[my];
+                    row = rows + idx * RW;
+                    const uint4 *hp = reinterpret_cast<const uint4 *>(row + 2 * P);
+                    uint32_t h[kRowHdr];
+#pragma unroll
+                    for (int j = 0; j < kRowHdr / 4; j++) {
+                        const uint4 v = hp[j];
+                        h[4 * j] = v.x;
+                        h[4 * j + 1] = v.y;
+                        h[4 * j + 2] = v.z;
+                        h[4 * j + 3] = v.w;
+                    }
+                    div_hdr_get(h, st, U, s);
+#pragma unroll 2
+                    for (int i0 = 0; i0 < P; i0 += 4) {
+                        const uint4 dv = *reinterpret_cast<const uint4 *>(row + i0);
+                        const uint4 rv = *reinterpret_cast<const uint4 *>(row + P + i0);
+                        const uint32_t d4[4] = {dv.x, dv.y, dv.z, dv.w}, r4[4] = {rv.x, rv.y, rv.z, rv.w};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int i = i0 + j;
+                            if (N % 4 == 0 || i < N) {
+                                Dc[i * stride] = d4[j];
+                                Rc[i * stride] = r4[j];
+                                Qc[i * stride] = 0u;
+                            }
+                        }
+                    }
+                    ph = Iter;
+                } else {
+                    ph = Dead;
+                }
+            }
+            if (__ballot_sync(FULL, ph != Dead) == 0) break;
+            if (__ballot_sync(FULL, ph == Iter) == 0) continue;
+        }
+
+        /* one step: digit, residue update, evaluation of the new remainder */
+        const bool live = ph == Iter;
+        const uint64_t qd = live ? dv_digit(st, U, C.E, st.f) : 0;
+        Fx96 fx;
+#pragma unroll 1
+        for (int i0 = 0; i0 < N; i0 += 4) {  // groups of 4: loads, arithmetic, stores
+            uint32_t rv[4], dv[4], qv[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int i = i0 + j < N ? i0 + j : N - 1;  // N not a multiple of 4: the last residue again
+                rv[j] = Rc[i * stride];
+                dv[j] = Dc[i * stride];
+                qv[j] = Qc[i * stride];
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int i = i0 + j < N ? i0 + j : N - 1;
+                const DivK k = K[i];
+                const uint32_t m = k.a.x;
+                const uint32_t qi = kred53(qd, k);
+                const uint32_t rn = submod(kmag(rv[j], k), kmulmod(qi, dv[j], k), m);
+                rv[j] = live ? rn : rv[j];
+                qv[j] = addmod(kmag(qv[j], k), qi, m);
+                if (N % 4 == 0 || i0 + j < N) fx.add(rv[j], k);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (N % 4 == 0 || i0 + j < N) {
+                    const int i = i0 + j;
+                    Rc[i * stride] = rv[j];
+                    if (live) Qc[i * stride] = qv[j];
+                }
+            }
+        }
+        if (live) {
+            U = fx.value();
+            st.b = kDivB;
+            if (--st.left == 0) ph = Final;
+        }
+    }
+}
+
+/* shared memory of pass A with rows: the DivK table, the block's step-count
+ * histogram, then two column rows per residue */
+template <int N>
+constexpr size_t divprep_smem_bytes(int threads) {
+    return sizeof(DivK) * N + (size_t)kDivRowBins * 4 + (size_t)2 * N * 4 * threads;
+}
+/* shared memory of pass B with rows: the DivK table, then the columns */
+template <int N>
+constexpr size_t divrow_smem_bytes(int threads) {
+    return sizeof(DivK) * N + (size_t)3 * N * 4 * threads;
+}
+
 /* digit steps of a division from its record (0: no step loop) */
 __device__ __forceinline__ int dv_rec_steps(const uint2 &r) {
     if ((r.x >> 16) != kDnOk) return 0;
@@ -468,26 +733,6 @@ __device__ __forceinline__ int64_t warp_claim(unsigned long long *ctr, int c) {
     return (int64_t)__shfl_sync(0xffffffffu, b, 0);
 }
 
-/* grid-wide form (three launches, ops_div.cu): pass A over numbers claimed
- * from one counter, a counting sort by step count, pass B over the sorted
- * order claimed from a second counter -- no per-warp ranges to drain */
-struct DivGlobal {
-    unsigned long long ctr_a, ctr_b;
-};
-
-/* shared memory of a block of `threads` threads running div_range: the DivK
- * table, the warps' counters, then the columns */
-template <int N>
-constexpr size_t div_smem_bytes(int threads) {
-    return sizeof(DivK) * N + (size_t)(threads / 32) * kDivBins * 4 + (size_t)3 * N * 4 * threads;
-}
-
-/* shared memory of a block of `threads` threads running pass A alone (two
- * column rows per residue) */
-template <int N>
-constexpr size_t divnorm_smem_bytes(int threads) {
-    return sizeof(DivK) * N + (size_t)(threads / 32) * kDivBins * 4 + (size_t)2 * N * 4 * threads;
-}
 
 /* scratch bytes per number of the global pass-A records and the order */
 constexpr size_t kDivScratchPerNumber = sizeof(uint2) + sizeof(int32_t);

@@ -130,6 +130,7 @@ grns_status launch_mpint(const grns_ctx *c, int op, const void *x, const void *y
 grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out_value,
                        int64_t *out_index, void *scratch, size_t scratch_bytes, cudaStream_t s);
 size_t max_scratch_bytes(const grns_ctx *c, int64_t count);
+size_t div_scratch_bytes(const grns_ctx *c, int64_t count);  // device scratch of one launch_div call
 size_t batch_staging_bytes(int njobs);
 grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *staging, cudaStream_t s);
 

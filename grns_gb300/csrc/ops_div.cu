@@ -2,13 +2,15 @@
  * grns_gb300 -- division and power-of-two scaling kernels.
  *   k_div      : q = floor(X/D), r = X - qD (reference src/rnsdiv.cuh:128),
  *                reference-faithful FP64 form, one thread per number
- *   k_div_a, k_div_sort, k_div_b : the same results on the integer fast
- *                path (div_warp.cuh): pass A over the whole grid, a counting
- *                sort by step count inside segments of consecutive numbers,
- *                pass B segment by segment, longest first, numbers claimed
- *                from grid-wide counters
+ *   k_div_a, k_div_place, k_div_b, k_div_out : the same results on the
+ *                integer fast path (div_warp.cuh): pass A writing one row
+ *                per number, a counting sort of all numbers by step count,
+ *                pass B over the rows longest first (numbers claimed from
+ *                grid-wide counters), the rows to the caller's layout
  *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
  */
+#include <algorithm>
+
 #include "div_warp.cuh"
 #include "scale_warp.cuh"
 #include "internal.h"
@@ -57,79 +59,130 @@ constexpr int div_min_blocks() {
     return N > 32 ? 2 : GRNS_DIV_MIN_BLOCKS;
 }
 
-/* pass A of the grid-wide division: numbers claimed from G->ctr_a, records
- * into rec */
+/* the division's scratch per chunk of numbers stays below this (the context's
+ * pool keeps kPoolKeepBytes across synchronisations) */
+constexpr size_t kDivScratchBytes = 192ull << 20;
+
+/* grid-wide state of one division call (one memset clears it) */
+struct DivRowsG {
+    unsigned long long ctr_a, ctr_b;  // pass A / pass B claim counters
+    uint32_t hist[kDivRowBins];       // numbers per digit-step count
+    uint32_t cursor[kDivRowBins];     // positions handed out per step count
+};
+
+/* pass A: numbers claimed from G->ctr_a in index order; per number its row,
+ * its step count and (no digit step) its flags; the step-count histogram */
 template <int N>
 __global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
-    k_div_a(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
-            DivGlobal *__restrict__ G, int64_t count) {
+    k_div_a(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint32_t *__restrict__ rows,
+            uint8_t *__restrict__ steps, uint8_t *__restrict__ flags, DivRowsG *__restrict__ G, int64_t count) {
     extern __shared__ uint4 div_smem[];
     DivK *K = reinterpret_cast<DivK *>(div_smem);
-    uint32_t *cols = reinterpret_cast<uint32_t *>(K + N) + (blockDim.x / 32) * kDivBins;  // layout of div_smem_bytes
+    uint32_t *hist = reinterpret_cast<uint32_t *>(K + N);
+    uint32_t *cols = hist + kDivRowBins;  // layout of divprep_smem_bytes
     divk_fill<N>(C, K);
+    for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     /* prefetch distance: one number per lane of the grid ahead, about what the
      * grid claims while a number is normalised */
     const int64_t lanes = (int64_t)gridDim.x * blockDim.x;
-    divnorm_range<N>(K, C, x, d, rec, count, [&](int c) { return warp_claim(&G->ctr_a, c); }, lanes,
-                     cols + threadIdx.x, blockDim.x);
+    const int stride = blockDim.x;
+    divnorm_range_f<N>(
+        K, C, x, d,
+        [&](int64_t idx, uint2 rec, const uint32_t *Xc) {
+            uint32_t f = 0;
+            const int st = div_row_build<N>(K, C, rec, Xc, stride, d, idx, rows + idx * kRowWords<N>(), f);
+            steps[idx] = (uint8_t)st;
+            atomicAdd(&hist[st], 1u);
+            if (flags && st == 0) flags[idx] = (uint8_t)f;
+        },
+        count, [&](int c) { return warp_claim(&G->ctr_a, c); }, lanes, cols + threadIdx.x, stride);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x)
+        if (hist[i]) atomicAdd(&G->hist[i], hist[i]);
 }
 
-constexpr int kDivSegment = 4096;  // numbers sorted together: contiguous, so pass B's loads stay L2-local
+constexpr int kDivPlaceChunk = 8192;  // numbers per block step of the placement
 
-/* order: within each segment of kDivSegment consecutive numbers, the numbers
- * by decreasing step count (one block per segment, a counting sort in shared
- * memory).  Pass B claims positions in order, so the grid works through the
- * segments one after another, longest divisions first inside each, and the
- * operands it touches at any time span a few segments (L2-resident). */
-__global__ void __launch_bounds__(256) k_div_sort(const uint2 *__restrict__ rec, int32_t *__restrict__ order,
-                                                  int64_t count) {
-    __shared__ uint32_t h[kDivBins];
-    for (int64_t b0 = (int64_t)blockIdx.x * kDivSegment; b0 < count; b0 += (int64_t)gridDim.x * kDivSegment) {
-        const int64_t b1 = b0 + kDivSegment < count ? b0 + kDivSegment : count;
-        for (int i = threadIdx.x; i < kDivBins; i += blockDim.x) h[i] = 0;
+/* order: the numbers by decreasing step count over the whole call (a
+ * counting sort: positions of step count b start after every number with
+ * more steps; each block reserves its range per count with one atomic) */
+__global__ void __launch_bounds__(256) k_div_place(const uint8_t *__restrict__ steps, DivRowsG *__restrict__ G,
+                                                   int32_t *__restrict__ order, int64_t count) {
+    __shared__ uint32_t loc[kDivRowBins], base[kDivRowBins], tot[kDivRowBins];
+    for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x) tot[i] = G->hist[i];
+    for (int64_t b0 = (int64_t)blockIdx.x * kDivPlaceChunk; b0 < count; b0 += (int64_t)gridDim.x * kDivPlaceChunk) {
+        const int64_t b1 = b0 + kDivPlaceChunk < count ? b0 + kDivPlaceChunk : count;
+        for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x) loc[i] = 0;
         __syncthreads();
-        for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) atomicAdd(&h[dv_rec_steps(rec[k])], 1u);
+        for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) atomicAdd(&loc[steps[k]], 1u);
         __syncthreads();
-        if (threadIdx.x < 32) {  /* exclusive prefix over bins in decreasing order (lane l: bins 63 - l, 31 - l) */
-            const int lane = threadIdx.x;
-            const uint32_t h0 = h[63 - lane], h1 = h[31 - lane];
-            uint32_t s0 = h0, s1 = h1;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t a0 = __shfl_up_sync(0xffffffffu, s0, o), a1 = __shfl_up_sync(0xffffffffu, s1, o);
-                if (lane >= o) {
-                    s0 += a0;
-                    s1 += a1;
-                }
-            }
-            s1 += __shfl_sync(0xffffffffu, s0, 31);
-            h[63 - lane] = s0 - h0;
-            h[31 - lane] = s1 - h1;
+        for (int t = threadIdx.x; t < kDivRowBins; t += blockDim.x) {
+            uint32_t start = 0;  // numbers with more steps than t
+            for (int u = t + 1; u < kDivRowBins; u++) start += tot[u];
+            base[t] = start + (loc[t] ? atomicAdd(&G->cursor[t], loc[t]) : 0u);
+            loc[t] = 0;
         }
         __syncthreads();
         for (int64_t k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
-            const uint32_t p = atomicAdd(&h[dv_rec_steps(rec[k])], 1u);
-            order[b0 + p] = (int32_t)k;
+            const uint32_t bin = steps[k];
+            order[base[bin] + atomicAdd(&loc[bin], 1u)] = (int32_t)k;
         }
         __syncthreads();
     }
 }
 
-/* pass B of the grid-wide division: positions of the sorted order claimed
- * from G->ctr_b, longest divisions first */
+/* pass B: positions of the order claimed from G->ctr_b, longest divisions
+ * first; the numbers without digit steps (the last G->hist[0] positions) are
+ * done already */
 template <int N>
 __global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
-    k_div_b(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, const uint2 *__restrict__ rec,
-            const int32_t *__restrict__ order, DivGlobal *__restrict__ G, int64_t count, Output<N> q, Output<N> r,
-            uint8_t *__restrict__ flags) {
+    k_div_b(const __grid_constant__ Consts<N> C, uint32_t *__restrict__ rows, const int32_t *__restrict__ order,
+            uint8_t *__restrict__ flags, DivRowsG *__restrict__ G, int64_t count) {
     extern __shared__ uint4 div_smem[];
     DivK *K = reinterpret_cast<DivK *>(div_smem);
-    uint32_t *cols = reinterpret_cast<uint32_t *>(K + N) + (blockDim.x / 32) * kDivBins;
+    uint32_t *cols = reinterpret_cast<uint32_t *>(K + N);  // layout of divrow_smem_bytes
     divk_fill<N>(C, K);
     __syncthreads();
-    divloop_range<N>(K, C, x, d, rec, order, q, r, flags, 0, count,
-                     [&](int c) { return warp_claim(&G->ctr_b, c); }, cols + threadIdx.x, blockDim.x);
+    const int64_t end = count - (int64_t)G->hist[0];
+    divrow_range<N>(K, C, rows, order, flags, end, [&](int c) { return warp_claim(&G->ctr_b, c); },
+                    cols + threadIdx.x, blockDim.x);
+}
+
+constexpr int kDivOutTile = 32;  // numbers per tile of the output kernel
+
+/* q and r from the rows into the caller's layout: a tile of rows read with
+ * coalesced loads into shared memory, written residue-major (SoA) or
+ * number-major (AoS) */
+template <int N>
+__global__ void __launch_bounds__(256) k_div_out(const uint32_t *__restrict__ rows, int64_t count, Output<N> q,
+                                                 Output<N> r) {
+    constexpr int P = kRowPad<N>(), RW = kRowWords<N>(), W = 2 * P + 1;  // tile row: q, r, one word of padding
+    __shared__ uint32_t tile[kDivOutTile * W];
+    for (int64_t k0 = (int64_t)blockIdx.x * kDivOutTile; k0 < count; k0 += (int64_t)gridDim.x * kDivOutTile) {
+        const int nk = count - k0 < kDivOutTile ? (int)(count - k0) : kDivOutTile;
+        for (int t = threadIdx.x; t < nk * 2 * P; t += blockDim.x) {
+            const int k = t / (2 * P), w = t - k * (2 * P);
+            tile[k * W + w] = rows[(k0 + k) * RW + w];
+        }
+        __syncthreads();
+        if (q.ld) {  // residue-major: a warp writes 32 consecutive numbers of one residue
+            for (int t = threadIdx.x; t < N * kDivOutTile; t += blockDim.x) {
+                const int i = t / kDivOutTile, k = t - i * kDivOutTile;
+                if (k < nk) {
+                    q.store(k0 + k, i, tile[k * W + i]);
+                    r.store(k0 + k, i, tile[k * W + P + i]);
+                }
+            }
+        } else {
+            for (int t = threadIdx.x; t < nk * N; t += blockDim.x) {
+                const int k = t / N, i = t - k * N;
+                q.store(k0 + k, i, tile[k * W + i]);
+                r.store(k0 + k, i, tile[k * W + P + i]);
+            }
+        }
+        __syncthreads();
+    }
 }
 
 template <int N>
@@ -186,45 +239,61 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
                                                                count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
         return cuda_status(cudaGetLastError());
     }
-    /* fast path: pass A, a counting sort by step count, pass B (div_warp.cuh),
-     * each over the whole grid with numbers claimed from counters */
-    const size_t smem = div_smem_bytes<N>(kDivBlock), smem_a = divnorm_smem_bytes<N>(kDivBlock);
+    /* fast path (div_warp.cuh): pass A writing rows, the longest-first order
+     * over the whole call, pass B over the rows, the rows to the caller's
+     * layout -- in chunks whose scratch stays below kDivScratchBytes */
+    constexpr size_t RB = (size_t)kRowWords<N>() * 4;
+    const size_t smem_a = divprep_smem_bytes<N>(kDivBlock), smem_b = divrow_smem_bytes<N>(kDivBlock);
     static std::atomic<int> occ_a[kOccDevices], occ_b[kOccDevices];  // resident blocks per SM, per device
     const int occ[2] = {resident_blocks(occ_a, c, k_div_a<N>, kDivBlock, smem_a),
-                        resident_blocks(occ_b, c, k_div_b<N>, kDivBlock, smem)};
+                        resident_blocks(occ_b, c, k_div_b<N>, kDivBlock, smem_b)};
+    const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 5)) & ~(size_t)4095);
+    const int64_t chunk = count < chunk_max ? count : chunk_max;
     /* warps: every resident one, fewer when a warp would get under min_per_warp
      * numbers (or one per lane's worth) */
-    auto grid_of = [&](int o) {
-        int64_t warps = (count + 31) / 32;
-        if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)
-            warps = (count + min_per_warp - 1) / min_per_warp;
+    auto grid_of = [&](int o, int64_t n) {
+        int64_t warps = (n + 31) / 32;
+        if (min_per_warp > 0 && warps > (n + min_per_warp - 1) / min_per_warp)
+            warps = (n + min_per_warp - 1) / min_per_warp;
         const int64_t cap = (int64_t)c->sm_count * o * (kDivBlock / 32);
         if (warps > cap) warps = cap;
         if (warps < 1) warps = 1;
         return (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
     };
-    /* scratch: records, order, the grid-wide counters */
+    /* scratch: rows, the order, the step counts, the grid-wide state */
+    const size_t rows_bytes = (size_t)chunk * RB, ord_bytes = ((size_t)chunk * 4 + 15) & ~(size_t)15;
+    const size_t steps_bytes = ((size_t)chunk + 15) & ~(size_t)15;  // every part 16-byte aligned
     void *scratch = nullptr;
-    const size_t rec_bytes = (size_t)count * sizeof(uint2), ord_bytes = ((size_t)count * 4 + 15) & ~(size_t)15;
-    cudaError_t e = scratch_alloc(c, &scratch, rec_bytes + ord_bytes + sizeof(DivGlobal), s);
+    cudaError_t e = scratch_alloc(c, &scratch, rows_bytes + ord_bytes + steps_bytes + sizeof(DivRowsG), s);
     if (e != cudaSuccess) return cuda_status(e);
-    uint2 *rec = (uint2 *)scratch;
-    int32_t *order = (int32_t *)((char *)scratch + rec_bytes);
-    DivGlobal *G = (DivGlobal *)((char *)scratch + rec_bytes + ord_bytes);
-    e = cudaMemsetAsync(G, 0, sizeof(DivGlobal), s);
-    const Operand<N> X{x, ld}, Dv{d, ld};
-    if (e == cudaSuccess) {
-        k_div_a<N><<<grid_of(occ[0]), kDivBlock, smem_a, s>>>(consts_of<N>(c), X, Dv, rec, G, count);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-        k_div_sort<<<grid_for(c, (count + kDivSegment - 1) / kDivSegment, 1, 8), 256, 0, s>>>(rec, order, count);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) {
-        k_div_b<N><<<grid_of(occ[1]), kDivBlock, smem, s>>>(consts_of<N>(c), X, Dv, rec, order, G, count,
-                                                             Output<N>{q, ld}, Output<N>{r, ld}, flags);
-        e = cudaGetLastError();
+    uint32_t *rows = (uint32_t *)scratch;
+    int32_t *order = (int32_t *)((char *)scratch + rows_bytes);
+    uint8_t *steps = (uint8_t *)scratch + rows_bytes + ord_bytes;
+    DivRowsG *G = (DivRowsG *)((char *)scratch + rows_bytes + ord_bytes + steps_bytes);
+    for (int64_t c0 = 0; c0 < count && e == cudaSuccess; c0 += chunk) {
+        const int64_t n = count - c0 < chunk ? count - c0 : chunk;
+        const int64_t off = ld ? c0 : c0 * N;  // first number of the chunk (SoA columns keep the leading dimension)
+        const Operand<N> X{x + off, ld}, Dv{d + off, ld};
+        uint8_t *fl = flags ? flags + c0 : nullptr;
+        e = cudaMemsetAsync(G, 0, sizeof(DivRowsG), s);
+        if (e == cudaSuccess) {
+            k_div_a<N><<<grid_of(occ[0], n), kDivBlock, smem_a, s>>>(consts_of<N>(c), X, Dv, rows, steps, fl, G, n);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            k_div_place<<<grid_for(c, (n + kDivPlaceChunk - 1) / kDivPlaceChunk, 1, 4), 256, 0, s>>>(steps, G, order,
+                                                                                                   n);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            k_div_b<N><<<grid_of(occ[1], n), kDivBlock, smem_b, s>>>(consts_of<N>(c), rows, order, fl, G, n);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            k_div_out<N><<<grid_for(c, (n + kDivOutTile - 1) / kDivOutTile, 1, 8), 256, 0, s>>>(
+                rows, n, Output<N>{q + off, ld}, Output<N>{r + off, ld});
+            e = cudaGetLastError();
+        }
     }
     scratch_free(scratch, s);
     return cuda_status(e);
@@ -260,6 +329,29 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
     e = cudaGetLastError();
     if (order) scratch_free(order, s);
     return cuda_status(e);
+}
+
+template <int N>
+static size_t div_scratch_of(int64_t count) {
+    constexpr size_t RB = (size_t)kRowWords<N>() * 4;
+    const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 5)) & ~(size_t)4095);
+    const int64_t chunk = count < chunk_max ? count : chunk_max;
+    return (size_t)chunk * RB + (((size_t)chunk * 4 + 15) & ~(size_t)15) + (((size_t)chunk + 15) & ~(size_t)15) +
+           sizeof(DivRowsG);
+}
+
+size_t div_scratch_bytes(const grns_ctx *c, int64_t count) {
+#define C_(n) return div_scratch_of<n>(count)
+    switch (c->n) {
+        case 4: C_(4);
+        case 8: C_(8);
+        case 12: C_(12);
+        case 16: C_(16);
+        case 32: C_(32);
+        case 64: C_(64);
+        default: return 0;
+    }
+#undef C_
 }
 
 grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,

@@ -34,6 +34,8 @@ constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/param
 constexpr int kDivB = 48;       // quotient bits per step of the integer division
 constexpr int kScaleB = 52;     // bits per step of the integer power-of-two scaling
 constexpr int kPow2NegRows = 64;  // rows j = 0..63 of the 2^-j mod m_i table
+/* rows a = 0.. of the 2^-(64 a) mod m_i table: every division shift s <= log2M + 64 */
+constexpr int pow2neg64_rows(int log2M) { return (log2M + 64) / 64 + 1; }
 /* binary <-> RNS conversion: integers as 32-bit little-endian limbs, worked
  * on in 26-bit chunks (26 + 30.42 bits per product: up to 158 products, or
  * 64 moduli, sum below 2^64) */
@@ -93,6 +95,8 @@ struct Consts {
     const uint32_t *pow2_inv_sh;// [30 * N]
     const uint32_t *pow2neg;    // [kPow2NegRows * N]  2^-j mod m_i
     const uint32_t *pow2neg_sh; // [kPow2NegRows * N]
+    const uint32_t *pow2neg64;  // [pow2neg64_rows(log2M) * N]  2^-(64 a) mod m_i
+    const uint32_t *pow2neg64_sh;
     /* binary conversion (16-byte aligned rows) */
     const uint32_t *bin_p26;    // [kBinMaxChunks * N]  2^(26 c) mod m_i
     const uint32_t *bin_mi26;   // [bin_chunks * N]     26-bit chunk c of M_i = M / m_i

@@ -728,6 +728,183 @@ GRNS_HD void div_fast(const Consts<N> &C, uint32_t *q, uint32_t *r, const uint32
     flags |= st.f;
 }
 
+/* ---------------- division through prepared rows ----------------
+ *
+ * The plain call's form of the same division.  Pass A leaves, per number, a
+ * row of kRowWords(N) words: the scaled divisor D = d 2^s (N residues at
+ * offset 0), the starting remainder R (N residues at offset kRowPad(N), N
+ * rounded up to a multiple of 4) and a 16-word header with the digit
+ * loop's state (dv_setup's UD, reciprocal, shift and step count, and the
+ * first step's fixed-point value), or -- for a division with no digit step
+ * (invalid input, zero divisor, zero dividend, divisor within E / 2^96 of M,
+ * normalisation cap) -- its final q and r.  Pass B runs the digit steps from
+ * the row alone, in any order, and leaves q and r in the row's first 2N
+ * words, so the numbers can be scheduled longest first across the whole call
+ * while every access to a number's data is one contiguous row.
+ *
+ * The remainder comes from the final R without x and d: after the steps
+ * R = 2^s (x - Q d) with 0 <= R < 4D, so for c = floor(R / D)
+ *     q = Q + c,   r = x - q d = (R - c D) 2^-s,
+ * and 2^-s mod m_i exists for the odd moduli (2^-s = 2^-(s mod 64) 2^-(64 floor(s / 64)),
+ * two table rows; s <= log2M + 49).
+ */
+constexpr int kRowHdr = 16;  // header words of a row
+template <int N>
+constexpr int kRowPad() {  // residue block of a row: N words rounded up to a multiple of 4
+    return (N + 3) & ~3;
+}
+template <int N>
+constexpr int kRowWords() {  // D (or q) at 0, R (or r) at kRowPad, the header at 2 kRowPad: 16-byte vectors
+    return 2 * kRowPad<N>() + kRowHdr;
+}
+/* header word offsets (after the 2N residues) */
+enum : int { kHdrUD = 0, kHdrU = 4, kHdrRm = 8, kHdrS = 10, kHdrSd = 11, kHdrB = 12, kHdrLeft = 13, kHdrFlags = 14 };
+
+GRNS_HD void u128_put(uint32_t *w, u128 v) {
+    w[0] = (uint32_t)v;
+    w[1] = (uint32_t)(v >> 32);
+    w[2] = (uint32_t)(v >> 64);
+    w[3] = (uint32_t)(v >> 96);
+}
+GRNS_HD u128 u128_get(const uint32_t *w) {
+    return (u128)w[0] | ((u128)w[1] << 32) | ((u128)w[2] << 64) | ((u128)w[3] << 96);
+}
+
+/* header of a division with digit steps (st after dv_setup, U the first step's value) */
+GRNS_HD void div_hdr_put(uint32_t *h, const DivSt &st, u128 U, int s) {
+    u128_put(h + kHdrUD, st.UD);
+    u128_put(h + kHdrU, U);
+    h[kHdrRm] = (uint32_t)st.Rm;
+    h[kHdrRm + 1] = (uint32_t)(st.Rm >> 32);
+    h[kHdrS] = (uint32_t)s;
+    h[kHdrSd] = (uint32_t)st.sd;
+    h[kHdrB] = (uint32_t)st.b;
+    h[kHdrLeft] = (uint32_t)st.left;
+    h[kHdrFlags] = 0;
+    h[kHdrFlags + 1] = 0;
+}
+GRNS_HD void div_hdr_get(const uint32_t *h, DivSt &st, u128 &U, int &s) {
+    st.UD = u128_get(h + kHdrUD);
+    U = u128_get(h + kHdrU);
+    st.Rm = (uint64_t)h[kHdrRm] | ((uint64_t)h[kHdrRm + 1] << 32);
+    s = (int)h[kHdrS];
+    st.sd = (int)h[kHdrSd];
+    st.b = (int)h[kHdrB];
+    st.left = (int)h[kHdrLeft];
+    st.f = 0;
+}
+
+/* pass A's row of one division from its record (dv_record) and the operands
+ * (x, d canonical; getters xg(i), dg(i)); returns the digit steps (0: the
+ * row already holds q and r, flags set) */
+template <int N, class GX, class GD>
+GRNS_HD int div_row_setup(const Consts<N> &C, uint2 rec, GX xg, GD dg, uint32_t *row, uint32_t &flags) {
+    const uint32_t status = rec.x >> 16;
+    bool xz = true;
+    for (int i = 0; i < N; i++) xz &= xg(i) == 0;
+    if (status != kDnOk || xz) {  // q = 0, r = x unless stated below
+        bool one = false;
+        if (status == kDnBad) flags |= 1u;  // INVALID_INPUT: q = r = 0
+        else if (status == kDnZero) flags |= 1u << 1;  // division by zero
+        else if (status == kDnCap) flags |= kFxIterCap;
+        else if (status == kDnNear && !xz) {  // d > M (1 - E / 2^96): the quotient is 0 or 1
+            uint32_t a[N], b[N];
+            for (int i = 0; i < N; i++) {
+                a[i] = xg(i);
+                b[i] = dg(i);
+            }
+            one = dv_cmp_vec<N>(C, a, b) >= 0;
+        }
+        for (int i = 0; i < N; i++) {
+            const uint32_t xv = status == kDnBad ? 0u : xg(i);
+            row[i] = one ? 1u : 0u;
+            row[kRowPad<N>() + i] = one ? submod(xv, dg(i), C.m[i]) : xv;
+        }
+        return 0;
+    }
+    const int s = (int)(rec.x & 0xffffu), e = dv_rec_e(rec);
+    const uint32_t *ps = C.pow2 + (int64_t)s * N, *pss = C.pow2_sh + (int64_t)s * N;
+    const uint32_t *pe = e < 0 ? C.pow2neg + (int64_t)(-e) * N : C.pow2 + (int64_t)e * N;
+    const uint32_t *pes = e < 0 ? C.pow2neg_sh + (int64_t)(-e) * N : C.pow2_sh + (int64_t)e * N;
+    constexpr int P = kRowPad<N>();
+    for (int i = 0; i < N; i++) {
+        row[i] = mulmod_shoup(dg(i), ldg_u32(ps + i), ldg_u32(pss + i), C.m[i]);
+        row[P + i] = mulmod_shoup(xg(i), ldg_u32(pe + i), ldg_u32(pes + i), C.m[i]);
+    }
+    DivSt st;
+    dv_setup(st, fx96w<N>(C, [&](int i) { return row[i]; }), s, e);
+    const u128 U = (rec.y >> 31) ? (((u128)1) << 96)
+                                 : (e < 0 ? fx96w<N>(C, xg) : fx96w<N>(C, [&](int i) { return row[P + i]; }));
+    div_hdr_put(row + 2 * P, st, U, s);
+    return st.left;
+}
+
+/* q and r of a division whose digit steps are done: R (the remainder rows),
+ * D, Q residues, U = fx96w(R), st its state, s its shift; c from the
+ * fixed-point values, exact comparisons when too close to call */
+template <int N>
+GRNS_HD void div_row_final(const Consts<N> &C, const uint32_t *R, const uint32_t *D, const uint32_t *Q, u128 U,
+                           const DivSt &st, int s, uint32_t *q, uint32_t *r) {
+    int c = dv_final_fx(st, U, C.E);
+    if (c < 0) c = dv_final_exact<N>(C, R, D);
+    const uint32_t *pa = C.pow2neg + (int64_t)(s & 63) * N, *pas = C.pow2neg_sh + (int64_t)(s & 63) * N;
+    const uint32_t *pb = C.pow2neg64 + (int64_t)(s >> 6) * N, *pbs = C.pow2neg64_sh + (int64_t)(s >> 6) * N;
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = C.m[i], cm = (uint32_t)c % m;  // c <= 3, m >= 3
+        const uint32_t cd = mulmod_barrett(cm, D[i], m, C.mu[i], C.b[i]);
+        const uint32_t v = mulmod_shoup(submod(R[i], cd, m), ldg_u32(pa + i), ldg_u32(pas + i), m);
+        q[i] = addmod(Q[i], cm, m);
+        r[i] = mulmod_shoup(v, ldg_u32(pb + i), ldg_u32(pbs + i), m);
+    }
+}
+
+/* the digit steps of one row (host form of pass B, for checks): q and r
+ * replace the row's first 2N words */
+template <int N>
+GRNS_HD void div_row_run(const Consts<N> &C, uint32_t *row, uint32_t &flags) {
+    constexpr int P = kRowPad<N>();
+    DivSt st;
+    u128 U;
+    int s;
+    div_hdr_get(row + 2 * P, st, U, s);
+    uint32_t R[N], D[N], Q[N];
+    for (int i = 0; i < N; i++) {
+        D[i] = row[i];
+        R[i] = row[P + i];
+        Q[i] = 0;
+    }
+    for (; st.left > 0; st.left--) {
+        const uint64_t qd = dv_digit(st, U, C.E, st.f);
+        for (int i = 0; i < N; i++) {
+            const uint32_t m = C.m[i];
+            const uint32_t qi = reduce53<N>(C, i, qd);
+            R[i] = submod(mulmod_shoup(R[i], C.b48[i], C.b48_sh[i], m), mulmod_barrett(qi, D[i], m, C.mu[i], C.b[i]), m);
+            Q[i] = addmod(mulmod_shoup(Q[i], C.b48[i], C.b48_sh[i], m), qi, m);
+        }
+        U = fx96w<N>(C, [&](int i) { return R[i]; });
+        st.b = kDivB;
+    }
+    div_row_final<N>(C, R, D, Q, U, st, s, row, row + P);
+    flags |= st.f;
+}
+
+/* q, r of one division through a row (the plain call's three passes for one
+ * number; checked against div_fast and exact arithmetic on the CPU) */
+template <int N>
+GRNS_HD void div_rows(const Consts<N> &C, uint32_t *q, uint32_t *r, const uint32_t *x, const uint32_t *d,
+                      uint32_t &flags) {
+    uint32_t row[kRowWords<N>()];
+    bool bad = false;
+    for (int i = 0; i < N; i++) bad |= x[i] >= C.m[i] || d[i] >= C.m[i];
+    const uint2 rec = bad ? dv_pack(kDnBad, 0, 0, false) : dv_record<N>(C, x, d);
+    if (div_row_setup<N>(C, rec, [&](int i) { return x[i]; }, [&](int i) { return d[i]; }, row, flags) > 0)
+        div_row_run<N>(C, row, flags);
+    for (int i = 0; i < N; i++) {
+        q[i] = row[i];
+        r[i] = row[kRowPad<N>() + i];
+    }
+}
+
 /* ---------------- power-of-two scaling (results of rns_scale2pow, src/rnsscal.cuh:93) ---------------- */
 
 /* k with X = sum_i M_i c_i - k M (rns_rank_compute, :134); `small` when X < M/2^30 is known */

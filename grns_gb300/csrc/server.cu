@@ -193,10 +193,11 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
     switch (q.r.op) {
         case GRNS_OP_EVAL: return sizeof(interval_t) * k;
         case GRNS_OP_CMP: return 4 * (size_t)k;
-        case GRNS_OP_DIV: return (2 * 4 * (size_t)n + 12) * k;
+        case GRNS_OP_DIV: return 2 * 4 * (size_t)n * k + (12 * (size_t)k);  // + the batched kernel's records
         case GRNS_OP_SCALE2POW: return (4 * (size_t)n + 12) * k;
         case GRNS_OP_MAX: return ((4 * (size_t)n + 7) / 8) * 8 + 8;
-        case GRNS_OP_MPINT_DIV: return (GRNS_MPINT_BYTES(n) + 16 * (size_t)n + 25) * k;  // + digit columns, division scratch
+        case GRNS_OP_MPINT_DIV:  // + digit columns, the division's scratch
+            return (GRNS_MPINT_BYTES(n) + 16 * (size_t)n + 1) * k + grns::div_scratch_bytes(c, k);
         default: return GRNS_MPINT_BYTES(n) * (size_t)k;
     }
 }

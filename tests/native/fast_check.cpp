@@ -57,6 +57,16 @@ int fc_div(void *p, const uint32_t *x, const uint32_t *d, long cnt, uint32_t *q,
     return 0;
 }
 
+/* the same divisions through prepared rows (the plain call's pass A / pass B split) */
+int fc_div_rows(void *p, const uint32_t *x, const uint32_t *d, long cnt, uint32_t *q, uint32_t *r, uint32_t *flags) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) { uint32_t f = 0; div_rows<N>(K<N>(b), q + k * N, r + k * N, x + k * N, \
+                                                                           d + k * N, f); flags[k] = f; }
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
 int fc_scale(void *p, const uint32_t *x, const uint32_t *D, long cnt, uint32_t *out) {
     Box *b = (Box *)p;
 #define C_(N) for (long k = 0; k < cnt; k++) scale_fast<N>(K<N>(b), out + k * N, x + k * N, D[k])

@@ -32,7 +32,7 @@ def fc(tmp_path_factory):
     L.fc_binary_limbs.argtypes = [ctypes.c_void_p]
     L.fc_table.restype = ctypes.c_long
     L.fc_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_long]
-    for f in ("fc_cmp", "fc_div", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary",
+    for f in ("fc_cmp", "fc_div", "fc_div_rows", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary",
               "fc_eval_fast"):
         getattr(L, f).argtypes = None
     return L
@@ -68,6 +68,10 @@ class FC:
         q, r = np.zeros_like(x), np.zeros_like(x)
         fl = np.zeros(len(X), np.uint32)
         self.L.fc_div(self.h, self.P(x), self.P(d), ctypes.c_long(len(X)), self.P(q), self.P(r), self.P(fl))
+        # the prepared-row form (pass A row, pass B digit steps, r from the final remainder) agrees
+        q2, r2, fl2 = np.zeros_like(x), np.zeros_like(x), np.zeros(len(X), np.uint32)
+        self.L.fc_div_rows(self.h, self.P(x), self.P(d), ctypes.c_long(len(X)), self.P(q2), self.P(r2), self.P(fl2))
+        assert np.array_equal(q, q2) and np.array_equal(r, r2) and np.array_equal(fl, fl2)
         return self.ints(q), self.ints(r), fl
 
     def scale(self, X, S):

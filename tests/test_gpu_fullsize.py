@@ -106,7 +106,7 @@ def exact_sample(ctx, d_log2_upper, seed=7):
         seg = np.arange(b0, min(COUNT, b0 + SEGMENT))
         longest = seg[np.argsort(d_log2_upper[seg], kind="stable")[:16]]
         idx.append(longest)
-        idx.append(rng.choice(seg, 48, replace=False))
+        idx.append(rng.choice(np.setdiff1d(seg, longest), 48, replace=False))
     return np.unique(np.concatenate(idx))
 
 
@@ -141,8 +141,9 @@ def test_scale2pow_full_size_exact_sample(env):
     idx = []
     for b0 in range(0, COUNT, SEGMENT):
         seg = np.arange(b0, min(COUNT, b0 + SEGMENT))
-        idx.append(seg[np.argsort(-Dh[seg], kind="stable")[:8]])
-        idx.append(rng.choice(seg, 56, replace=False))
+        top = seg[np.argsort(-Dh[seg], kind="stable")[:8]]
+        idx.append(top)
+        idx.append(rng.choice(np.setdiff1d(seg, top), 56, replace=False))
     idx = np.unique(np.concatenate(idx))
     assert len(idx) >= 4096
     ex = Exact(mods)
