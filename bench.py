@@ -535,11 +535,11 @@ def bench_batched(ctx_for, L, dev, stream, sp, P, seed, steps, flush):
     sets = (("mixed", (native.OP_CMP, native.OP_DIV, native.OP_SCALE2POW, native.OP_MAX)),
             ("eval_cmp_only", (native.OP_CMP,)), ("div_only", (native.OP_DIV,)))
     for k, (name, ops) in enumerate(sets):
-        out[name] = batched_job_set(c, L, dev, stream, sp, seed + k, steps, flush, ops)
+        out[name] = batched_job_set(c, L, dev, stream, sp, P, seed + k, steps, flush, ops)
     return out
 
 
-def batched_job_set(c, L, dev, stream, sp, seed, steps, flush, op_choices):
+def batched_job_set(c, L, dev, stream, sp, P, seed, steps, flush, op_choices):
     import random
     import ctypes
     import torch
@@ -910,7 +910,7 @@ def main():
                    "streams": "the division and the scaling of a step on two streams at once (independent); "
                               "kernels_ms are each one's span on its stream while they share the GPU",
                    "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "k_div_a<32> + k_div_sort + k_div_b<32> (one division call)",
+        "roofline": {"bound": "hbm", "kernel": "k_div_a<32> + k_div_place + k_div_b<32> + k_div_out<32> (one division call)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": DIV_TRAFFIC_BYTES,
@@ -924,7 +924,7 @@ def main():
         "e2e": {"value": e2e, "unit": "Mnum/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "grns_div_host + grns_scale2pow_host (pinned host arrays, chunked copy/compute "
                        "overlap), the two on two streams", "matches_device_results": e2e_ok},
-        "gpu_launches": 4 * args.steps,  # per step: k_div_a, k_div_sort, k_div_b, k_scale_warp
+        "gpu_launches": 5 * args.steps,  # per step: k_div_a, k_div_place, k_div_b, k_div_out, k_scale_warp
         "extra": extra,
         "workloads": workloads,
     }
