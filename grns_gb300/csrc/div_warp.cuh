@@ -111,6 +111,22 @@ struct Fx96 {
 
 constexpr int kDivUnroll = 4;
 
+/* c = floor(R / D) when the fixed-point comparison was too close to call:
+ * R = j D exactly (dv_final_tie, from the residues in the shared-memory
+ * columns), else the exact comparisons */
+template <int N>
+__device__ __forceinline__ int div_final_tie(const DivK *K, const Consts<N> &C, const uint32_t *Rc, const uint32_t *Dc,
+                                             int stride, u128 UD) {
+    const int j = dv_final_tie<N>(C, UD, [&](int i) { return Rc[i * stride]; }, [&](int i) { return Dc[i * stride]; });
+    if (j) return j;
+    uint32_t a[N], b[N];
+    for (int i = 0; i < N; i++) {
+        a[i] = Rc[i * stride];
+        b[i] = Dc[i * stride];
+    }
+    return dv_final_exact<N>(C, a, b);
+}
+
 /* pass A over the numbers claim() hands out below end: rec[k] = record of
  * number k.  Column rows: the working value in rows [0, N), the dividend in
  * rows [N, 2N). */
@@ -266,14 +282,7 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
         if (lv == 0 || __popc(wt) >= kDivRefill) {
             if (ph == Final) {  // q = Q + c, r = x - q d
                 int c = dv_final_fx(st, U, C.E);
-                if (c < 0) {
-                    uint32_t a[N], b[N];
-                    for (int i = 0; i < N; i++) {
-                        a[i] = Rc[i * stride];
-                        b[i] = Dc[i * stride];
-                    }
-                    c = dv_final_exact<N>(C, a, b);
-                }
+                if (c < 0) c = div_final_tie<N>(K, C, Rc, Dc, stride, st.UD);
 #pragma unroll 4
                 for (int i = 0; i < N; i++) {
                     const DivK k = K[i];
@@ -526,14 +535,7 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
         if (lv == 0 || __popc(wt) >= kDivRefill) {
             if (ph == Final) {  // q = Q + c, r = (R - c D) 2^-s, into the row
                 int c = dv_final_fx(st, U, C.E);
-                if (c < 0) {
-                    uint32_t a[N], b[N];
-                    for (int i = 0; i < N; i++) {
-                        a[i] = Rc[i * stride];
-                        b[i] = Dc[i * stride];
-                    }
-                    c = dv_final_exact<N>(C, a, b);
-                }
+                if (c < 0) c = div_final_tie<N>(K, C, Rc, Dc, stride, st.UD);
                 const uint32_t *pa = C.pow2neg + (int64_t)(s & 63) * N, *pas = C.pow2neg_sh + (int64_t)(s & 63) * N;
                 const uint32_t *pb = C.pow2neg64 + (int64_t)(s >> 6) * N;
                 const uint32_t *pbs = C.pow2neg64_sh + (int64_t)(s >> 6) * N;

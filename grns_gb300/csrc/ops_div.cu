@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
         if (hist[i]) atomicAdd(&G->hist[i], hist[i]);
 }
 
-constexpr int kDivPlaceChunk = 8192;  // numbers per block step of the placement
+constexpr int kDivPlaceChunk = 2048;  // numbers per block step of the placement
 
 /* order: the numbers by decreasing step count over the whole call (a
  * counting sort: positions of step count b start after every number with
@@ -149,21 +149,27 @@ __global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
                     cols + threadIdx.x, blockDim.x);
 }
 
-constexpr int kDivOutTile = 32;  // numbers per tile of the output kernel
+constexpr int kDivOutTile = 64;  // numbers per tile of the output kernel
 
 /* q and r from the rows into the caller's layout: a tile of rows read with
- * coalesced loads into shared memory, written residue-major (SoA) or
- * number-major (AoS) */
+ * coalesced 16-byte loads into shared memory, written residue-major (SoA)
+ * or number-major (AoS) */
 template <int N>
 __global__ void __launch_bounds__(256) k_div_out(const uint32_t *__restrict__ rows, int64_t count, Output<N> q,
                                                  Output<N> r) {
     constexpr int P = kRowPad<N>(), RW = kRowWords<N>(), W = 2 * P + 1;  // tile row: q, r, one word of padding
+    constexpr int V = 2 * P / 4;                                         // 16-byte words of q and r per row
     __shared__ uint32_t tile[kDivOutTile * W];
     for (int64_t k0 = (int64_t)blockIdx.x * kDivOutTile; k0 < count; k0 += (int64_t)gridDim.x * kDivOutTile) {
         const int nk = count - k0 < kDivOutTile ? (int)(count - k0) : kDivOutTile;
-        for (int t = threadIdx.x; t < nk * 2 * P; t += blockDim.x) {
-            const int k = t / (2 * P), w = t - k * (2 * P);
-            tile[k * W + w] = rows[(k0 + k) * RW + w];
+        for (int t = threadIdx.x; t < nk * V; t += blockDim.x) {
+            const int k = t / V, w = t - k * V;
+            const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(rows + (k0 + k) * RW) + w);
+            uint32_t *dst = tile + k * W + 4 * w;
+            dst[0] = v.x;
+            dst[1] = v.y;
+            dst[2] = v.z;
+            dst[3] = v.w;
         }
         __syncthreads();
         if (q.ld) {  // residue-major: a warp writes 32 consecutive numbers of one residue
@@ -281,7 +287,7 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
-            k_div_place<<<grid_for(c, (n + kDivPlaceChunk - 1) / kDivPlaceChunk, 1, 4), 256, 0, s>>>(steps, G, order,
+            k_div_place<<<grid_for(c, (n + kDivPlaceChunk - 1) / kDivPlaceChunk, 1, 8), 256, 0, s>>>(steps, G, order,
                                                                                                    n);
             e = cudaGetLastError();
         }

@@ -650,6 +650,25 @@ GRNS_HD int dv_final_fx(const DivSt &st, u128 UR, uint64_t Eu) {
     return c;
 }
 
+/* R = j D for some j in 1..3, read from the residues; valid when 3D < M
+ * (then equal residues mean equal values), i.e. for UD < 2^94 (D < M / 4).
+ * Returns j, or 0.  This is the usual way the fixed-point comparisons end
+ * too close to call: after the steps R = 2^s (x - Q d), so R - j D is a
+ * multiple of 2^s, which the fixed-point band (width ~ 2^-60 M) can only
+ * contain as 0 when d < 2^48 -- a divisor that divides the dividend. */
+template <int N, class GR, class GD>
+GRNS_HD int dv_final_tie(const Consts<N> &C, u128 UD, GR rg, GD dg) {
+    if (UD >= (((u128)1) << 94)) return 0;
+    bool e1 = true, e2 = true, e3 = true;
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = C.m[i], r = rg(i), d1 = dg(i), d2 = addmod(d1, d1, m);
+        e1 &= r == d1;
+        e2 &= r == d2;
+        e3 &= r == addmod(d2, d1, m);
+    }
+    return e1 ? 1 : (e2 ? 2 : (e3 ? 3 : 0));
+}
+
 /* exact c = floor(R / D) (R < 4D): repeated exact comparison and subtraction */
 template <int N>
 GRNS_HD_RARE int dv_final_exact(const Consts<N> &C, const uint32_t *R, const uint32_t *D) {
@@ -719,7 +738,10 @@ GRNS_HD void div_fast(const Consts<N> &C, uint32_t *q, uint32_t *r, const uint32
         st.b = kDivB;
     }
     int c = dv_final_fx(st, U, C.E);
-    if (c < 0) c = dv_final_exact<N>(C, R, D);
+    if (c < 0) {
+        c = dv_final_tie<N>(C, st.UD, [&](int i) { return R[i]; }, [&](int i) { return D[i]; });
+        if (c == 0) c = dv_final_exact<N>(C, R, D);
+    }
     for (int i = 0; i < N; i++) {
         const uint32_t m = C.m[i];
         q[i] = addmod(Q[i], (uint32_t)c % m, m);
@@ -846,7 +868,10 @@ template <int N>
 GRNS_HD void div_row_final(const Consts<N> &C, const uint32_t *R, const uint32_t *D, const uint32_t *Q, u128 U,
                            const DivSt &st, int s, uint32_t *q, uint32_t *r) {
     int c = dv_final_fx(st, U, C.E);
-    if (c < 0) c = dv_final_exact<N>(C, R, D);
+    if (c < 0) {
+        c = dv_final_tie<N>(C, st.UD, [&](int i) { return R[i]; }, [&](int i) { return D[i]; });
+        if (c == 0) c = dv_final_exact<N>(C, R, D);
+    }
     const uint32_t *pa = C.pow2neg + (int64_t)(s & 63) * N, *pas = C.pow2neg_sh + (int64_t)(s & 63) * N;
     const uint32_t *pb = C.pow2neg64 + (int64_t)(s >> 6) * N, *pbs = C.pow2neg64_sh + (int64_t)(s >> 6) * N;
     for (int i = 0; i < N; i++) {
