@@ -38,7 +38,10 @@ struct HostTables {
     uint64_t acc_lo = 0, acc_hi = 0;             // ceil(acc * 2^100)
     std::vector<uint32_t> c128w;                 // n x 4 words: ceil(2^128 w_i / m_i) mod 2^128
     std::vector<uint32_t> pow2neg, pow2neg_sh;   // kPow2NegRows x n: 2^-j mod m_i
-    std::vector<uint32_t> pow2neg64, pow2neg64_sh;  // pow2neg64_rows(log2M) x n: 2^-(64 a) mod m_i
+    /* division, residue-major (a lane's row lookups for one residue stay within a few cache
+     * lines): pairs (2^j mod m_i, Shoup companion), [i * 64 + j] for j < 64 and
+     * [i * pow2_hi_rows + a] for 2^(64 a); the same for 2^-j and 2^-(64 a) */
+    std::vector<uint32_t> p2lo, p2hi, p2nlo, p2nhi;
     std::vector<uint64_t> mi64;                  // M_i mod 2^64
     uint64_t m64 = 0;                            // M mod 2^64
     uint64_t E = 0;  // sum_i (m_i - 1)
@@ -262,19 +265,32 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
             u = (u * half) % m[i];
         }
     }
-    /* division: 2^-(64 a) mod m_i, so 2^-s = pow2neg[s % 64] pow2neg64[s / 64] for every shift s <= log2M + 64 */
-    const int rows64 = pow2neg64_rows(T.log2M);
-    T.pow2neg64.resize((size_t)rows64 * n);
-    T.pow2neg64_sh.resize(T.pow2neg64.size());
+    /* division: 2^s = 2^(s mod 64) 2^(64 floor(s / 64)) and 2^-s likewise, for every shift s < 64 rows */
+    const int rows = pow2_hi_rows(T.log2M);
+    T.p2lo.assign((size_t)n * 64 * 2, 0);
+    T.p2nlo.assign((size_t)n * 64 * 2, 0);
+    T.p2hi.assign((size_t)n * rows * 2, 0);
+    T.p2nhi.assign((size_t)n * rows * 2, 0);
     for (int i = 0; i < n; i++) {
-        const uint64_t half = (m[i] + 1) / 2;
-        uint64_t step = 1;  // 2^-64 mod m_i
-        for (int j = 0; j < 64; j++) step = (step * half) % m[i];
-        uint64_t u = 1;
-        for (int a = 0; a < rows64; a++) {
-            T.pow2neg64[(size_t)a * n + i] = (uint32_t)u;
-            T.pow2neg64_sh[(size_t)a * n + i] = shoup((uint32_t)u, m[i]);
-            u = (u * step) % m[i];
+        const uint64_t half = (m[i] + 1) / 2;  // 2^-1 mod m_i
+        uint64_t up = 1, dn = 1;
+        for (int j = 0; j < 64; j++) {
+            T.p2lo[((size_t)i * 64 + j) * 2] = (uint32_t)up;
+            T.p2lo[((size_t)i * 64 + j) * 2 + 1] = shoup((uint32_t)up, m[i]);
+            T.p2nlo[((size_t)i * 64 + j) * 2] = (uint32_t)dn;
+            T.p2nlo[((size_t)i * 64 + j) * 2 + 1] = shoup((uint32_t)dn, m[i]);
+            up = (up * 2) % m[i];
+            dn = (dn * half) % m[i];
+        }
+        const uint64_t up64 = up, dn64 = dn;  // 2^64 and 2^-64 mod m_i
+        up = dn = 1;
+        for (int a = 0; a < rows; a++) {
+            T.p2hi[((size_t)i * rows + a) * 2] = (uint32_t)up;
+            T.p2hi[((size_t)i * rows + a) * 2 + 1] = shoup((uint32_t)up, m[i]);
+            T.p2nhi[((size_t)i * rows + a) * 2] = (uint32_t)dn;
+            T.p2nhi[((size_t)i * rows + a) * 2 + 1] = shoup((uint32_t)dn, m[i]);
+            up = (up * up64) % m[i];
+            dn = (dn * dn64) % m[i];
         }
     }
     /* scaling: M_i mod 2^64 and M mod 2^64 */
@@ -391,8 +407,10 @@ inline std::vector<uint32_t> table_blob(const HostTables &T) {
     std::vector<uint32_t> blob(T.c96k);  /* first: 16-byte aligned rows (every size below the
                                             conversion tables is a multiple of 4 words) */
     for (const auto *v : {&T.bin_p26, &T.bin_mi26, &T.bin_m26, &T.pow2, &T.pow2_sh, &T.mrc_inv, &T.mrc_inv_sh, &T.mi_pow2, &T.m_pow2, &T.pow2_inv,
-                          &T.pow2_inv_sh, &T.pow2neg, &T.pow2neg_sh, &T.pow2neg64, &T.pow2neg64_sh})
+                          &T.pow2_inv_sh, &T.pow2neg, &T.pow2neg_sh})
         blob.insert(blob.end(), v->begin(), v->end());
+    blob.resize((blob.size() + 3) & ~(size_t)3, 0u);  // the pair tables start 16-byte aligned
+    for (const auto *v : {&T.p2lo, &T.p2hi, &T.p2nlo, &T.p2nhi}) blob.insert(blob.end(), v->begin(), v->end());
     return blob;
 }
 
@@ -459,8 +477,12 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     C.pow2_inv_sh = blob + off; off += T.pow2_inv_sh.size();
     C.pow2neg = blob + off;     off += T.pow2neg.size();
     C.pow2neg_sh = blob + off;  off += T.pow2neg_sh.size();
-    C.pow2neg64 = blob + off;   off += T.pow2neg64.size();
-    C.pow2neg64_sh = blob + off;
+    off = (off + 3) & ~(size_t)3;
+    C.p2lo = reinterpret_cast<const uint2 *>(blob + off);   off += T.p2lo.size();
+    C.p2hi = reinterpret_cast<const uint2 *>(blob + off);   off += T.p2hi.size();
+    C.p2nlo = reinterpret_cast<const uint2 *>(blob + off);  off += T.p2nlo.size();
+    C.p2nhi = reinterpret_cast<const uint2 *>(blob + off);
+    C.p2rows = pow2_hi_rows(T.log2M);
 }
 
 }  // namespace grns

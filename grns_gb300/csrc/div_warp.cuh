@@ -15,7 +15,7 @@
  * coalesced batch of loads instead of one divergent load per finishing lane).
  * The batched kernel runs the two passes over one warp's job chunk
  * (div_range); the plain call runs them over the whole call through
- * prepared rows, longest divisions first (divprep / divrow_range below).
+ * prepared rows, longest divisions first (div_row_build / divrow_range below).
  *
  * Memory layout: each thread owns a column of 3N words of shared memory
  * (R, D, Q rows, [row][stride], conflict-free), and the block holds one DivK
@@ -413,9 +413,10 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
 /* ---------------- the plain call's division through prepared rows ----------------
  * (rns_fast.cuh: div_row_setup / div_row_final are the one-number forms)
  *
- * Pass A (divprep) runs divnorm_range_f and, as each number's normalisation
- * ends, writes its row: the digit steps' starting state, or q and r at once.
- * A global counting sort by step count (k_div_place, ops_div.cu) orders all
+ * Pass A (divnorm_range) writes each number's 8-byte record; a kernel over
+ * the numbers in index order (div_row_build, every lane busy) turns records
+ * and operands into rows: the digit steps' starting state, or q and r at
+ * once.  A global counting sort by step count (k_div_place, ops_div.cu) orders all
  * numbers longest first; pass B (divrow_range) takes positions of that order
  * from a grid-wide counter, reads each row with 16-byte loads, runs the
  * steps and writes q and r back into the row; a last kernel moves them to
@@ -425,19 +426,18 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
 
 constexpr int kDivRowBins = 256;  // step counts 0..255 (a division takes at most (log2M + 49) / 48 + 1)
 
-/* pass A's row of one division (the device form of div_row_setup).  Xc: the
- * dividend's residues in this lane's shared-memory column (stride `stride`);
- * the divisor is read again from d; row: the number's row in global memory.
- * Returns the digit steps (0: q and r written, flags set in f). */
-template <int N>
-__device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, uint2 rec, const uint32_t *Xc,
-                                             int stride, const Operand<N> &d, int64_t idx, uint32_t *row,
-                                             uint32_t &f) {
+/* the row of one division from its pass-A record (the device form of
+ * div_row_setup; getters xg(i), dg(i) read the operands; row: the number's
+ * row in global memory, written with 16-byte stores).  Returns the digit
+ * steps (0: q and r written, flags set in f). */
+template <int N, class GX, class GD>
+__device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, uint2 rec, GX xg, GD dg,
+                                             uint32_t *row, uint32_t &f) {
     constexpr int P = kRowPad<N>();
     const uint32_t status = rec.x >> 16;
     uint32_t xnz = 0;
 #pragma unroll 8
-    for (int i = 0; i < N; i++) xnz |= Xc[i * stride];
+    for (int i = 0; i < N; i++) xnz |= xg(i);
     if (status != kDnOk || !xnz) {  // no digit step: q = 0, r = x unless stated below
         bool one = false;
         if (status == kDnBad) f |= kFlagInvalidInput;  // q = r = 0
@@ -446,8 +446,8 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
         else if (status == kDnNear && xnz) {  // d > M (1 - E / 2^96): the quotient is 0 or 1
             uint32_t a[N], b[N];
             for (int i = 0; i < N; i++) {
-                a[i] = Xc[i * stride];
-                b[i] = d.load(idx, i);
+                a[i] = xg(i);
+                b[i] = dg(i);
             }
             one = dv_cmp_vec<N>(C, a, b) >= 0;
         }
@@ -459,9 +459,9 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
                 const int i = i0 + j;
                 qv[j] = rv[j] = 0;
                 if (N % 4 == 0 || i < N) {
-                    const uint32_t xv = status == kDnBad ? 0u : Xc[i * stride];
+                    const uint32_t xv = status == kDnBad ? 0u : xg(i);
                     qv[j] = one ? 1u : 0u;
-                    rv[j] = one ? submod(xv, d.load(idx, i), K[i].a.x) : xv;
+                    rv[j] = one ? submod(xv, dg(i), K[i].a.x) : xv;
                 }
             }
             *reinterpret_cast<uint4 *>(row + i0) = make_uint4(qv[0], qv[1], qv[2], qv[3]);
@@ -470,9 +470,6 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
         return 0;
     }
     const int s = (int)(rec.x & 0xffffu), e = dv_rec_e(rec);
-    const uint32_t *ps = C.pow2 + (int64_t)s * N, *pss = C.pow2_sh + (int64_t)s * N;
-    const uint32_t *pe = e < 0 ? C.pow2neg + (int64_t)(-e) * N : C.pow2 + (int64_t)e * N;
-    const uint32_t *pes = e < 0 ? C.pow2neg_sh + (int64_t)(-e) * N : C.pow2_sh + (int64_t)e * N;
     Fx96 fd, fxx, fr;
 #pragma unroll 1
     for (int i0 = 0; i0 < P; i0 += 4) {
@@ -483,9 +480,9 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
             dv[j] = rv[j] = 0;
             if (N % 4 == 0 || i < N) {
                 const DivK k = K[i];
-                const uint32_t xv = Xc[i * stride];
-                dv[j] = mulmod_shoup(d.load(idx, i), __ldg(ps + i), __ldg(pss + i), k.a.x);
-                rv[j] = mulmod_shoup(xv, __ldg(pe + i), __ldg(pes + i), k.a.x);
+                const uint32_t xv = xg(i);
+                dv[j] = mul_pow2<N>(C, i, dg(i), s);
+                rv[j] = e < 0 ? mul_pow2neg<N>(C, i, xv, -e) : mul_pow2<N>(C, i, xv, e);
                 fd.add(dv[j], k);
                 fxx.add(xv, k);
                 fr.add(rv[j], k);
@@ -536,9 +533,6 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
             if (ph == Final) {  // q = Q + c, r = (R - c D) 2^-s, into the row
                 int c = dv_final_fx(st, U, C.E);
                 if (c < 0) c = div_final_tie<N>(K, C, Rc, Dc, stride, st.UD);
-                const uint32_t *pa = C.pow2neg + (int64_t)(s & 63) * N, *pas = C.pow2neg_sh + (int64_t)(s & 63) * N;
-                const uint32_t *pb = C.pow2neg64 + (int64_t)(s >> 6) * N;
-                const uint32_t *pbs = C.pow2neg64_sh + (int64_t)(s >> 6) * N;
 #pragma unroll 1
                 for (int i0 = 0; i0 < P; i0 += 4) {
                     uint32_t qv[4], rv[4];
@@ -551,8 +545,7 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
                             const uint32_t m = k.a.x, cm = (uint32_t)c % m;
                             const uint32_t v = submod(Rc[i * stride], kmulmod(cm, Dc[i * stride], k), m);
                             qv[j] = addmod(Qc[i * stride], cm, m);
-                            rv[j] = mulmod_shoup(mulmod_shoup(v, __ldg(pa + i), __ldg(pas + i), m), __ldg(pb + i),
-                                                 __ldg(pbs + i), m);
+                            rv[j] = mul_pow2neg<N>(C, i, v, s);
                         }
                     }
                     *reinterpret_cast<uint4 *>(row + i0) = make_uint4(qv[0], qv[1], qv[2], qv[3]);
@@ -644,11 +637,10 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
     }
 }
 
-/* shared memory of pass A with rows: the DivK table, the block's step-count
- * histogram, then two column rows per residue */
+/* shared memory of pass A: the DivK table, then two column rows per residue */
 template <int N>
 constexpr size_t divprep_smem_bytes(int threads) {
-    return sizeof(DivK) * N + (size_t)kDivRowBins * 4 + (size_t)2 * N * 4 * threads;
+    return sizeof(DivK) * N + (size_t)2 * N * 4 * threads;
 }
 /* shared memory of pass B with rows: the DivK table, then the columns */
 template <int N>

@@ -2,9 +2,10 @@
  * grns_gb300 -- division and power-of-two scaling kernels.
  *   k_div      : q = floor(X/D), r = X - qD (reference src/rnsdiv.cuh:128),
  *                reference-faithful FP64 form, one thread per number
- *   k_div_a, k_div_place, k_div_b, k_div_out : the same results on the
- *                integer fast path (div_warp.cuh): pass A writing one row
- *                per number, a counting sort of all numbers by step count,
+ *   k_div_a, k_div_rows, k_div_place, k_div_b, k_div_out : the same
+ *                results on the integer fast path (div_warp.cuh): pass A
+ *                writing one record per number, one row per number, a
+ *                counting sort of all numbers by step count,
  *                pass B over the rows longest first (numbers claimed from
  *                grid-wide counters), the rows to the caller's layout
  *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
@@ -70,33 +71,45 @@ struct DivRowsG {
     uint32_t cursor[kDivRowBins];     // positions handed out per step count
 };
 
-/* pass A: numbers claimed from G->ctr_a in index order; per number its row,
- * its step count and (no digit step) its flags; the step-count histogram */
+/* pass A: numbers claimed from G->ctr_a in index order; per number its
+ * 8-byte record (div_warp.cuh, divnorm_range) */
 template <int N>
 __global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
-    k_div_a(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint32_t *__restrict__ rows,
-            uint8_t *__restrict__ steps, uint8_t *__restrict__ flags, DivRowsG *__restrict__ G, int64_t count) {
+    k_div_a(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
+            DivRowsG *__restrict__ G, int64_t count) {
     extern __shared__ uint4 div_smem[];
     DivK *K = reinterpret_cast<DivK *>(div_smem);
-    uint32_t *hist = reinterpret_cast<uint32_t *>(K + N);
-    uint32_t *cols = hist + kDivRowBins;  // layout of divprep_smem_bytes
+    uint32_t *cols = reinterpret_cast<uint32_t *>(K + N);  // layout of divprep_smem_bytes
     divk_fill<N>(C, K);
-    for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x) hist[i] = 0;
     __syncthreads();
     /* prefetch distance: one number per lane of the grid ahead, about what the
      * grid claims while a number is normalised */
     const int64_t lanes = (int64_t)gridDim.x * blockDim.x;
-    const int stride = blockDim.x;
-    divnorm_range_f<N>(
-        K, C, x, d,
-        [&](int64_t idx, uint2 rec, const uint32_t *Xc) {
-            uint32_t f = 0;
-            const int st = div_row_build<N>(K, C, rec, Xc, stride, d, idx, rows + idx * kRowWords<N>(), f);
-            steps[idx] = (uint8_t)st;
-            atomicAdd(&hist[st], 1u);
-            if (flags && st == 0) flags[idx] = (uint8_t)f;
-        },
-        count, [&](int c) { return warp_claim(&G->ctr_a, c); }, lanes, cols + threadIdx.x, stride);
+    divnorm_range<N>(K, C, x, d, rec, count, [&](int c) { return warp_claim(&G->ctr_a, c); }, lanes,
+                     cols + threadIdx.x, blockDim.x);
+}
+
+/* rows: one thread per number in index order (coalesced operand loads, every
+ * lane busy); per number its row, its step count and (no digit step) its
+ * flags; the step-count histogram */
+template <int N>
+__global__ void __launch_bounds__(256) k_div_rows(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d,
+                                                  const uint2 *__restrict__ rec, uint32_t *__restrict__ rows,
+                                                  uint8_t *__restrict__ steps, uint8_t *__restrict__ flags,
+                                                  DivRowsG *__restrict__ G, int64_t count) {
+    __shared__ DivK K[N];
+    __shared__ uint32_t hist[kDivRowBins];
+    divk_fill<N>(C, K);
+    for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t f = 0;
+        const int st = div_row_build<N>(K, C, rec[k], [&](int i) { return x.load(k, i); },
+                                        [&](int i) { return d.load(k, i); }, rows + k * kRowWords<N>(), f);
+        steps[k] = (uint8_t)st;
+        atomicAdd(&hist[st], 1u);
+        if (flags && st == 0) flags[k] = (uint8_t)f;
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x)
         if (hist[i]) atomicAdd(&G->hist[i], hist[i]);
@@ -245,7 +258,7 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
                                                                count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
         return cuda_status(cudaGetLastError());
     }
-    /* fast path (div_warp.cuh): pass A writing rows, the longest-first order
+    /* fast path (div_warp.cuh): pass A writing records, the rows, the longest-first order
      * over the whole call, pass B over the rows, the rows to the caller's
      * layout -- in chunks whose scratch stays below kDivScratchBytes */
     constexpr size_t RB = (size_t)kRowWords<N>() * 4;
@@ -253,7 +266,7 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
     static std::atomic<int> occ_a[kOccDevices], occ_b[kOccDevices];  // resident blocks per SM, per device
     const int occ[2] = {resident_blocks(occ_a, c, k_div_a<N>, kDivBlock, smem_a),
                         resident_blocks(occ_b, c, k_div_b<N>, kDivBlock, smem_b)};
-    const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 5)) & ~(size_t)4095);
+    const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 13)) & ~(size_t)4095);
     const int64_t chunk = count < chunk_max ? count : chunk_max;
     /* warps: every resident one, fewer when a warp would get under min_per_warp
      * numbers (or one per lane's worth) */
@@ -266,16 +279,19 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
         if (warps < 1) warps = 1;
         return (unsigned)((warps * 32 + kDivBlock - 1) / kDivBlock);
     };
-    /* scratch: rows, the order, the step counts, the grid-wide state */
-    const size_t rows_bytes = (size_t)chunk * RB, ord_bytes = ((size_t)chunk * 4 + 15) & ~(size_t)15;
+    /* scratch: rows, records, the order, the step counts, the grid-wide state */
+    const size_t rows_bytes = (size_t)chunk * RB, rec_bytes = (size_t)chunk * 8;
+    const size_t ord_bytes = ((size_t)chunk * 4 + 15) & ~(size_t)15;
     const size_t steps_bytes = ((size_t)chunk + 15) & ~(size_t)15;  // every part 16-byte aligned
     void *scratch = nullptr;
-    cudaError_t e = scratch_alloc(c, &scratch, rows_bytes + ord_bytes + steps_bytes + sizeof(DivRowsG), s);
+    cudaError_t e =
+        scratch_alloc(c, &scratch, rows_bytes + rec_bytes + ord_bytes + steps_bytes + sizeof(DivRowsG), s);
     if (e != cudaSuccess) return cuda_status(e);
     uint32_t *rows = (uint32_t *)scratch;
-    int32_t *order = (int32_t *)((char *)scratch + rows_bytes);
-    uint8_t *steps = (uint8_t *)scratch + rows_bytes + ord_bytes;
-    DivRowsG *G = (DivRowsG *)((char *)scratch + rows_bytes + ord_bytes + steps_bytes);
+    uint2 *rec = (uint2 *)((char *)scratch + rows_bytes);
+    int32_t *order = (int32_t *)((char *)scratch + rows_bytes + rec_bytes);
+    uint8_t *steps = (uint8_t *)scratch + rows_bytes + rec_bytes + ord_bytes;
+    DivRowsG *G = (DivRowsG *)((char *)scratch + rows_bytes + rec_bytes + ord_bytes + steps_bytes);
     for (int64_t c0 = 0; c0 < count && e == cudaSuccess; c0 += chunk) {
         const int64_t n = count - c0 < chunk ? count - c0 : chunk;
         const int64_t off = ld ? c0 : c0 * N;  // first number of the chunk (SoA columns keep the leading dimension)
@@ -283,7 +299,11 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
         uint8_t *fl = flags ? flags + c0 : nullptr;
         e = cudaMemsetAsync(G, 0, sizeof(DivRowsG), s);
         if (e == cudaSuccess) {
-            k_div_a<N><<<grid_of(occ[0], n), kDivBlock, smem_a, s>>>(consts_of<N>(c), X, Dv, rows, steps, fl, G, n);
+            k_div_a<N><<<grid_of(occ[0], n), kDivBlock, smem_a, s>>>(consts_of<N>(c), X, Dv, rec, G, n);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            k_div_rows<N><<<grid_for(c, n, 256, 4), 256, 0, s>>>(consts_of<N>(c), X, Dv, rec, rows, steps, fl, G, n);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
@@ -340,9 +360,9 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
 template <int N>
 static size_t div_scratch_of(int64_t count) {
     constexpr size_t RB = (size_t)kRowWords<N>() * 4;
-    const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 5)) & ~(size_t)4095);
+    const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 13)) & ~(size_t)4095);
     const int64_t chunk = count < chunk_max ? count : chunk_max;
-    return (size_t)chunk * RB + (((size_t)chunk * 4 + 15) & ~(size_t)15) + (((size_t)chunk + 15) & ~(size_t)15) +
+    return (size_t)chunk * (RB + 8) + (((size_t)chunk * 4 + 15) & ~(size_t)15) + (((size_t)chunk + 15) & ~(size_t)15) +
            sizeof(DivRowsG);
 }
 

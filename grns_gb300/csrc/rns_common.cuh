@@ -34,8 +34,8 @@ constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/param
 constexpr int kDivB = 48;       // quotient bits per step of the integer division
 constexpr int kScaleB = 52;     // bits per step of the integer power-of-two scaling
 constexpr int kPow2NegRows = 64;  // rows j = 0..63 of the 2^-j mod m_i table
-/* rows a = 0.. of the 2^-(64 a) mod m_i table: every division shift s <= log2M + 64 */
-constexpr int pow2neg64_rows(int log2M) { return (log2M + 64) / 64 + 1; }
+/* rows a = 0.. of the 2^(64 a) and 2^-(64 a) mod m_i tables: every division shift s <= log2M + 64 */
+constexpr int pow2_hi_rows(int log2M) { return (log2M + 64) / 64 + 1; }
 /* binary <-> RNS conversion: integers as 32-bit little-endian limbs, worked
  * on in 26-bit chunks (26 + 30.42 bits per product: up to 158 products, or
  * 64 moduli, sum below 2^64) */
@@ -95,8 +95,10 @@ struct Consts {
     const uint32_t *pow2_inv_sh;// [30 * N]
     const uint32_t *pow2neg;    // [kPow2NegRows * N]  2^-j mod m_i
     const uint32_t *pow2neg_sh; // [kPow2NegRows * N]
-    const uint32_t *pow2neg64;  // [pow2neg64_rows(log2M) * N]  2^-(64 a) mod m_i
-    const uint32_t *pow2neg64_sh;
+    /* division: (value, Shoup companion) pairs, residue-major -- [i * 64 + j]: 2^j (p2lo),
+     * 2^-j (p2nlo); [i * p2rows + a]: 2^(64 a) (p2hi), 2^-(64 a) (p2nhi) mod m_i */
+    const uint2 *p2lo, *p2hi, *p2nlo, *p2nhi;
+    int p2rows;
     /* binary conversion (16-byte aligned rows) */
     const uint32_t *bin_p26;    // [kBinMaxChunks * N]  2^(26 c) mod m_i
     const uint32_t *bin_mi26;   // [bin_chunks * N]     26-bit chunk c of M_i = M / m_i

@@ -37,6 +37,29 @@ GRNS_HD uint32_t ldg_u32(const uint32_t *p) {
     return *p;
 #endif
 }
+GRNS_HD uint2 ldg_u2(const uint2 *p) {
+#ifdef __CUDA_ARCH__
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
+/* v 2^s mod m_i and v 2^-s mod m_i for 0 <= s < 64 p2rows: two Shoup products
+ * with (value, companion) pairs of the residue-major tables, so the lanes of a
+ * warp looking up different shifts for one residue read a few cache lines */
+template <int N>
+GRNS_HD uint32_t mul_pow2(const Consts<N> &C, int i, uint32_t v, int s) {
+    const uint32_t m = C.m[i];
+    const uint2 a = ldg_u2(C.p2lo + i * 64 + (s & 63)), b = ldg_u2(C.p2hi + (int64_t)i * C.p2rows + (s >> 6));
+    return mulmod_shoup(mulmod_shoup(v, a.x, a.y, m), b.x, b.y, m);
+}
+template <int N>
+GRNS_HD uint32_t mul_pow2neg(const Consts<N> &C, int i, uint32_t v, int s) {
+    const uint32_t m = C.m[i];
+    const uint2 a = ldg_u2(C.p2nlo + i * 64 + (s & 63)), b = ldg_u2(C.p2nhi + (int64_t)i * C.p2rows + (s >> 6));
+    return mulmod_shoup(mulmod_shoup(v, a.x, a.y, m), b.x, b.y, m);
+}
 
 GRNS_HD int clz32(uint32_t x) {
 #ifdef __CUDA_ARCH__
@@ -845,13 +868,10 @@ GRNS_HD int div_row_setup(const Consts<N> &C, uint2 rec, GX xg, GD dg, uint32_t 
         return 0;
     }
     const int s = (int)(rec.x & 0xffffu), e = dv_rec_e(rec);
-    const uint32_t *ps = C.pow2 + (int64_t)s * N, *pss = C.pow2_sh + (int64_t)s * N;
-    const uint32_t *pe = e < 0 ? C.pow2neg + (int64_t)(-e) * N : C.pow2 + (int64_t)e * N;
-    const uint32_t *pes = e < 0 ? C.pow2neg_sh + (int64_t)(-e) * N : C.pow2_sh + (int64_t)e * N;
     constexpr int P = kRowPad<N>();
     for (int i = 0; i < N; i++) {
-        row[i] = mulmod_shoup(dg(i), ldg_u32(ps + i), ldg_u32(pss + i), C.m[i]);
-        row[P + i] = mulmod_shoup(xg(i), ldg_u32(pe + i), ldg_u32(pes + i), C.m[i]);
+        row[i] = mul_pow2<N>(C, i, dg(i), s);
+        row[P + i] = e < 0 ? mul_pow2neg<N>(C, i, xg(i), -e) : mul_pow2<N>(C, i, xg(i), e);
     }
     DivSt st;
     dv_setup(st, fx96w<N>(C, [&](int i) { return row[i]; }), s, e);
@@ -872,14 +892,11 @@ GRNS_HD void div_row_final(const Consts<N> &C, const uint32_t *R, const uint32_t
         c = dv_final_tie<N>(C, st.UD, [&](int i) { return R[i]; }, [&](int i) { return D[i]; });
         if (c == 0) c = dv_final_exact<N>(C, R, D);
     }
-    const uint32_t *pa = C.pow2neg + (int64_t)(s & 63) * N, *pas = C.pow2neg_sh + (int64_t)(s & 63) * N;
-    const uint32_t *pb = C.pow2neg64 + (int64_t)(s >> 6) * N, *pbs = C.pow2neg64_sh + (int64_t)(s >> 6) * N;
     for (int i = 0; i < N; i++) {
         const uint32_t m = C.m[i], cm = (uint32_t)c % m;  // c <= 3, m >= 3
         const uint32_t cd = mulmod_barrett(cm, D[i], m, C.mu[i], C.b[i]);
-        const uint32_t v = mulmod_shoup(submod(R[i], cd, m), ldg_u32(pa + i), ldg_u32(pas + i), m);
         q[i] = addmod(Q[i], cm, m);
-        r[i] = mulmod_shoup(v, ldg_u32(pb + i), ldg_u32(pbs + i), m);
+        r[i] = mul_pow2neg<N>(C, i, submod(R[i], cd, m), s);
     }
 }
 
