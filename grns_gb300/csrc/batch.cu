@@ -45,6 +45,7 @@ struct JobDev {
     int32_t *order;             // div, scale with per-number exponents: longest-first order
     uint32_t D_uniform;
     int32_t coop;
+    int32_t vec;  // AoS operands 16-byte aligned, n a multiple of 4: a number's residues as 16-byte loads
     int64_t chunk_begin;   // first global chunk of this job
     int64_t partial_base;  // max jobs: first partial slot
     int32_t chunk_elems;
@@ -132,6 +133,36 @@ __device__ __forceinline__ uint64_t fx64_coop(const Consts<N> &C, const Operand<
     return a;
 }
 
+/* a number's residues from an AoS array as 16-byte loads (N a multiple of 4,
+ * the array 16-byte aligned) */
+template <int N>
+__device__ __forceinline__ void load_aos4(const uint32_t *base, int64_t k, uint32_t *v) {
+    if constexpr (N % 4 == 0) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(base + k * N);
+#pragma unroll
+        for (int q = 0; q < N / 4; q++) {
+            const uint4 w = __ldcs(p + q);
+            v[4 * q] = w.x;
+            v[4 * q + 1] = w.y;
+            v[4 * q + 2] = w.z;
+            v[4 * q + 3] = w.w;
+        }
+    }
+}
+
+/* the 64-bit fixed-point value of a number given as an array of residues */
+template <int N>
+__device__ __forceinline__ uint64_t fx64_arr(const Consts<N> &C, const uint32_t *v, uint32_t &bad) {
+    uint64_t a = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        bad |= (uint32_t)(v[i] >= C.m[i]);
+        a += (uint64_t)v[i] * C.c64l[i];
+        a += (uint64_t)(uint32_t)(v[i] * C.c64h[i]) << 32;
+    }
+    return a;
+}
+
 template <int N>
 __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, int j, int64_t c, int lane,
                                           unsigned *done, Part *partials, uint32_t *smem) {
@@ -145,7 +176,13 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
             for (int64_t k = start + lane; k < end; k += 32) {
                 uint32_t f = 0;
                 Er lo, up;
-                eval<N>(C, [&](int i) { return x.load_cs(k, i); }, lo, up, f);
+                if (J.vec) {
+                    uint32_t v[N];
+                    load_aos4<N>(J.a, k, v);
+                    eval<N>(C, [&](int i) { return v[i]; }, lo, up, f);
+                } else {
+                    eval<N>(C, [&](int i) { return x.load_cs(k, i); }, lo, up, f);
+                }
                 ((Er *)J.out0)[2 * k] = lo;
                 ((Er *)J.out0)[2 * k + 1] = up;
                 if (J.flags) J.flags[k] = (uint8_t)f;
@@ -182,14 +219,22 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
                     }
                     uint64_t a = 0, b = 0;
                     uint32_t bad = 0;
+                    if (J.vec) {
+                        uint32_t v[N];
+                        load_aos4<N>(J.a, k, v);
+                        a = fx64_arr<N>(C, v, bad);
+                        load_aos4<N>(J.b, k, v);
+                        b = fx64_arr<N>(C, v, bad);
+                    } else {
 #pragma unroll
-                    for (int i = 0; i < N; i++) {
-                        const uint32_t xi = x.load_cs(k, i), yi = y.load_cs(k, i);
-                        bad |= (uint32_t)(xi >= C.m[i]) | (uint32_t)(yi >= C.m[i]);
-                        a += (uint64_t)xi * C.c64l[i];
-                        a += (uint64_t)(uint32_t)(xi * C.c64h[i]) << 32;
-                        b += (uint64_t)yi * C.c64l[i];
-                        b += (uint64_t)(uint32_t)(yi * C.c64h[i]) << 32;
+                        for (int i = 0; i < N; i++) {
+                            const uint32_t xi = x.load_cs(k, i), yi = y.load_cs(k, i);
+                            bad |= (uint32_t)(xi >= C.m[i]) | (uint32_t)(yi >= C.m[i]);
+                            a += (uint64_t)xi * C.c64l[i];
+                            a += (uint64_t)(uint32_t)(xi * C.c64h[i]) << 32;
+                            b += (uint64_t)yi * C.c64l[i];
+                            b += (uint64_t)(uint32_t)(yi * C.c64h[i]) << 32;
+                        }
                     }
                     int r = fx64_order(a, b, C.E);
                     if (r == 2 && !bad) r = batch_tie<N>(C, x, k, y, k);
@@ -232,7 +277,15 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
                 }
             } else {
                 for (int64_t k = start + lane; k < end; k += 32) {
-                    Part p{fx64<N>(C, [&](int i) { return x.load_cs(k, i); }), k};
+                    uint64_t a;
+                    if (J.vec) {
+                        uint32_t v[N], bad = 0;
+                        load_aos4<N>(J.a, k, v);
+                        a = fx64_arr<N>(C, v, bad);
+                    } else {
+                        a = fx64<N>(C, [&](int i) { return x.load_cs(k, i); });
+                    }
+                    Part p{a, k};
                     if (part_better<N>(C, x, p, best)) best = p;
                 }
             }
@@ -435,6 +488,8 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
         const int op = u.op;
         const Sched &sc = c->sched[op];
         J.coop = (op == GRNS_OP_CMP || op == GRNS_OP_MAX) ? sc.coop : 0;
+        J.vec = u.layout == GRNS_LAYOUT_AOS && c->n % 4 == 0 && ((uintptr_t)u.a & 15) == 0 &&
+                ((uintptr_t)u.b & 15) == 0;
         J.chunk_elems = sc.chunk > 0 ? sc.chunk : 256;
         J.nchunks = (int32_t)((u.count + J.chunk_elems - 1) / J.chunk_elems);
         if (op == GRNS_OP_MAX && u.count == 0) J.nchunks = 0;

@@ -470,7 +470,7 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
         return 0;
     }
     const int s = (int)(rec.x & 0xffffu), e = dv_rec_e(rec);
-    Fx96 fd, fxx, fr;
+    Fx96 fd, fu;  // the divisor's value; the first step's (x itself when e < 0, else R = x 2^e)
 #pragma unroll 1
     for (int i0 = 0; i0 < P; i0 += 4) {
         uint32_t dv[4], rv[4];
@@ -482,10 +482,14 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
                 const DivK k = K[i];
                 const uint32_t xv = xg(i);
                 dv[j] = mul_pow2<N>(C, i, dg(i), s);
-                rv[j] = e < 0 ? mul_pow2neg<N>(C, i, xv, -e) : mul_pow2<N>(C, i, xv, e);
+                if (e < 0) {  // -e <= 48: one factor, 2^e = 2^-(-e)
+                    const uint2 p = __ldg(C.p2nlo + i * 64 - e);
+                    rv[j] = mulmod_shoup(xv, p.x, p.y, k.a.x);
+                } else {
+                    rv[j] = mul_pow2<N>(C, i, xv, e);
+                }
                 fd.add(dv[j], k);
-                fxx.add(xv, k);
-                fr.add(rv[j], k);
+                fu.add(e < 0 ? xv : rv[j], k);
             }
         }
         *reinterpret_cast<uint4 *>(row + i0) = make_uint4(dv[0], dv[1], dv[2], dv[3]);
@@ -493,7 +497,7 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
     }
     DivSt st;
     dv_setup(st, fd.value(), s, e);
-    const u128 U = (rec.y >> 31) ? (((u128)1) << 96) : (e < 0 ? fxx.value() : fr.value());
+    const u128 U = (rec.y >> 31) ? (((u128)1) << 96) : fu.value();
     uint32_t h[kRowHdr];
     div_hdr_put(h, st, U, s);
     uint4 *hp = reinterpret_cast<uint4 *>(row + 2 * P);

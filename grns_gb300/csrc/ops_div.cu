@@ -263,9 +263,10 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
      * layout -- in chunks whose scratch stays below kDivScratchBytes */
     constexpr size_t RB = (size_t)kRowWords<N>() * 4;
     const size_t smem_a = divprep_smem_bytes<N>(kDivBlock), smem_b = divrow_smem_bytes<N>(kDivBlock);
-    static std::atomic<int> occ_a[kOccDevices], occ_b[kOccDevices];  // resident blocks per SM, per device
-    const int occ[2] = {resident_blocks(occ_a, c, k_div_a<N>, kDivBlock, smem_a),
-                        resident_blocks(occ_b, c, k_div_b<N>, kDivBlock, smem_b)};
+    static std::atomic<int> occ_a[kOccDevices], occ_b[kOccDevices], occ_r[kOccDevices];  // resident blocks per SM
+    const int occ[3] = {resident_blocks(occ_a, c, k_div_a<N>, kDivBlock, smem_a),
+                        resident_blocks(occ_b, c, k_div_b<N>, kDivBlock, smem_b),
+                        resident_blocks(occ_r, c, k_div_rows<N>, 256, 0)};
     const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 13)) & ~(size_t)4095);
     const int64_t chunk = count < chunk_max ? count : chunk_max;
     /* warps: every resident one, fewer when a warp would get under min_per_warp
@@ -303,7 +304,8 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
-            k_div_rows<N><<<grid_for(c, n, 256, 4), 256, 0, s>>>(consts_of<N>(c), X, Dv, rec, rows, steps, fl, G, n);
+            k_div_rows<N><<<grid_for(c, n, 256, occ[2]), 256, 0, s>>>(consts_of<N>(c), X, Dv, rec, rows, steps, fl, G,
+                                                                     n);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
