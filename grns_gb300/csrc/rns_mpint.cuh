@@ -22,37 +22,57 @@ static_assert(sizeof(MpInt<8>) == 72 && sizeof(MpInt<32>) == 168 && sizeof(MpInt
 
 __device__ __forceinline__ double neg_if(double v, bool neg) { return neg ? -v : v; }
 
+/* the sign and evaluation of an mp_int (the part of the record besides the digits) */
+struct MpIntHead {
+    int32_t sign;
+    Er eval[2];
+};
 template <int N>
-__device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, const MpInt<N> &x, const MpInt<N> &y,
-                                             bool sub, uint32_t &flags) {
+__device__ __forceinline__ MpIntHead head_of(const MpInt<N> &x) {
+    return MpIntHead{x.sign, {x.eval[0], x.eval[1]}};
+}
+
+/* the interval of x + y (sub: x - y) by interval addition of the signed
+ * evaluations, and whether the result is negative (both bounds below 0, the
+ * reference's rule, src/mpint.cuh:381); lo / up are the result's bounds
+ * after the sign is taken out */
+__device__ __forceinline__ bool mpint_addsub_eval(const MpIntHead &x, const MpIntHead &y, bool sub, Er &lo, Er &up) {
     const int sx = x.sign, sy = sub ? (y.sign ^ 1) : y.sign;
     Er evx[2] = {x.eval[0], x.eval[1]}, evy[2] = {y.eval[0], y.eval[1]};
-    uint32_t dig[N];
-#pragma unroll
-    for (int i = 0; i < N; i++) {
-        const uint32_t m = C.m[i], a = x.digits[i], b = y.digits[i];
-        flags |= (a >= m || b >= m) ? kFlagInvalidInput : 0u;
-        uint32_t sa = sx ? submod(0u, a, m) : a;
-        uint32_t sb = sy ? submod(0u, b, m) : b;
-        dig[i] = addmod(sa, sb, m);
-    }
     evx[0].frac = neg_if(evx[0].frac, sx);
     evx[1].frac = neg_if(evx[1].frac, sx);
     evy[0].frac = neg_if(evy[0].frac, sy);
     evy[1].frac = neg_if(evy[1].frac, sy);
-    Er lo = er_add_dir<false>(evx[sx], evy[sy]);
-    Er up = er_add_dir<true>(evx[1 - sx], evy[1 - sy]);
+    lo = er_add_dir<false>(evx[sx], evy[sy]);
+    up = er_add_dir<true>(evx[1 - sx], evy[1 - sy]);
     const bool minus = lo.frac < 0 && up.frac < 0;
-    res.sign = minus;
     if (minus) {
-#pragma unroll
-        for (int i = 0; i < N; i++) dig[i] = dig[i] ? C.m[i] - dig[i] : 0u;
-        Er t = lo;
+        const Er t = lo;
         lo = Er{-up.frac, up.exp};
         up = Er{-t.frac, t.exp};
     }
+    return minus;
+}
+
+/* digit i of x + y (sub: x - y) for a result of sign `minus` */
+__device__ __forceinline__ uint32_t mpint_addsub_digit(uint32_t a, uint32_t b, uint32_t m, int sx, int sy, bool minus,
+                                                       uint32_t &flags) {
+    flags |= (a >= m || b >= m) ? kFlagInvalidInput : 0u;
+    const uint32_t sa = sx ? submod(0u, a, m) : a;
+    const uint32_t sb = sy ? submod(0u, b, m) : b;
+    const uint32_t d = addmod(sa, sb, m);
+    return minus ? (d ? m - d : 0u) : d;
+}
+
+template <int N>
+__device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, const MpInt<N> &x, const MpInt<N> &y,
+                                             bool sub, uint32_t &flags) {
+    Er lo, up;
+    const bool minus = mpint_addsub_eval(head_of(x), head_of(y), sub, lo, up);
+    const int sx = x.sign, sy = sub ? (y.sign ^ 1) : y.sign;
 #pragma unroll
-    for (int i = 0; i < N; i++) res.digits[i] = dig[i];
+    for (int i = 0; i < N; i++) res.digits[i] = mpint_addsub_digit(x.digits[i], y.digits[i], C.m[i], sx, sy, minus, flags);
+    res.sign = minus;
     res.eval[0] = lo;
     res.eval[1] = up;
     flags |= overflow_flags<N>(C, lo, up);
