@@ -276,6 +276,8 @@ def run_only(args):
     n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32, "mpint64": 64,
          "mpdiv32": 32, "tobin32": 32, "frombin32": 32, "tobin64": 64, "mrc32": 32}[args.only]
     ctx = G.RNSContext(greedy(n))
+    if args.eval_split is not None:
+        native.check(L.grns_ctx_set_eval_split(ctx.handle, args.eval_split))
     P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     cnt = args.pairs
@@ -344,6 +346,7 @@ def run_only(args):
         times.append(e0.elapsed_time(e1))
     ms = statistics.median(times) if times else 0.0
     print(json.dumps({"only": args.only, "count": cnt, "flush": bool(args.flush), "calls": args.warmup + args.steps,
+                      "eval_split": L.grns_ctx_get_eval_split(ctx.handle),
                       "ms_median": ms,
                       "Mnum_s": cnt / (ms * 1e-3) / 1e6 if ms else None}))
 
@@ -765,6 +768,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
+    ap.add_argument("--eval-split", type=int, default=None,
+                    help="profiling: eighths of the evaluation's warps on the FP64 pipe (grns_ctx_set_eval_split)")
     ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "evtight32", "mpint64",
                                            "mpdiv32", "tobin32", "frombin32", "tobin64", "mrc32"], default=None,
                     help="profiling: run just this op --warmup + --steps times on --pairs numbers, no JSON line")

@@ -257,6 +257,14 @@ grns_status grns_ctx_get_table(const grns_ctx *c, int which, void *dst, size_t b
     return GRNS_OK;
 }
 
+grns_status grns_ctx_set_eval_split(grns_ctx *c, int fp64_eighths) {
+    if (!c || fp64_eighths < 0 || fp64_eighths > 8) return GRNS_ERR_INVALID_ARGUMENT;
+    c->eval_fp64_eighths = fp64_eighths;
+    return GRNS_OK;
+}
+
+int grns_ctx_get_eval_split(const grns_ctx *c) { return c ? c->eval_fp64_eighths : -1; }
+
 grns_status grns_ctx_set_path(grns_ctx *c, int path) {
     if (!c || (path != GRNS_PATH_FAST && path != GRNS_PATH_REFERENCE)) return GRNS_ERR_INVALID_ARGUMENT;
     c->path = path;

@@ -11,14 +11,38 @@
 
 namespace grns {
 
+/* warps whose index mod 8 is below fp_eighths evaluate on the FP64 pipe
+ * (eval_fp64), the others on the integer pipe (eval_int): the same bits */
+__device__ __forceinline__ bool warp_on_fp64(int fp_eighths) {
+    return (int)((((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) & 7) < fp_eighths;
+}
+
+/* one number's common-path evaluation on the chosen pipe, then the rare
+ * branches (eval_full re-reads the residues through getm) */
+template <int N, bool FAST, class Get, class GetM>
+__device__ __forceinline__ void eval_split(const Consts<N> &C, bool fp, Get get, GetM getm, Er &lo, Er &up,
+                                           uint32_t &f) {
+    uint32_t bad = 0;
+    const int st = fp ? eval_fp64<N, Get, FAST>(C, get, lo, up, bad) : eval_int<N, Get, FAST>(C, get, lo, up, bad);
+    if (bad) {
+        f = kFlagInvalidInput;
+        lo = up = Er{0.0, 0};
+    } else if (st == kEvalZero) {
+        lo = up = Er{0.0, 0};
+    } else if (st == kEvalRare) {
+        eval_full<N, GetM, FAST>(C, getm, lo, up, f);
+    }
+}
+
 template <int N, bool FAST = false>
 __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
-                                              Er *__restrict__ out, uint8_t *__restrict__ flags) {
+                                              Er *__restrict__ out, uint8_t *__restrict__ flags, int fp_eighths) {
+    const bool fp = warp_on_fp64(fp_eighths);
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = 0;
         Er lo, up;
         auto get = [&](int i) { return x.load(k, i); };
-        eval<N, decltype(get), FAST>(C, get, lo, up, f);
+        eval_split<N, FAST>(C, fp, get, get, lo, up, f);
         out[2 * k] = lo;
         out[2 * k + 1] = up;
         if (flags) flags[k] = (uint8_t)f;
@@ -31,7 +55,8 @@ __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> 
 template <int N, bool FAST = false>
 __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Consts<N> C, Operand<N> x,
                                                       int64_t count, Er *__restrict__ out,
-                                                      uint8_t *__restrict__ flags) {
+                                                      uint8_t *__restrict__ flags, int fp_eighths) {
+    const bool fp = warp_on_fp64(fp_eighths);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t cur[N];
@@ -46,20 +71,12 @@ __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Co
 #pragma unroll
             for (int i = 0; i < N; i++) nxt[i] = x.load(kn, i);
         }
-        uint32_t f = 0, bad = 0;
+        uint32_t f = 0;
         Er lo, up;
         auto getc = [&](int i) { return cur[i]; };
-        const int st = eval_int<N, decltype(getc), FAST>(C, getc, lo, up, bad);
-        if (bad) {
-            f = kFlagInvalidInput;
-            lo = up = Er{0.0, 0};
-        } else if (st == kEvalZero) {
-            lo = up = Er{0.0, 0};
-        } else if (st == kEvalRare) {
-            const int64_t kk = k;
-            auto getm = [&](int i) { return x.load(kk, i); };
-            eval_full<N, decltype(getm), FAST>(C, getm, lo, up, f);
-        }
+        const int64_t kk = k;
+        auto getm = [&](int i) { return x.load(kk, i); };
+        eval_split<N, FAST>(C, fp, getc, getm, lo, up, f);
         out[2 * k] = lo;
         out[2 * k + 1] = up;
         if (flags) flags[k] = (uint8_t)f;
@@ -268,10 +285,10 @@ static grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, in
     const int B = 256;
     if (N <= 32)
         k_eval_pipe<N, FAST><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
-                                                                   (Er *)out, flags);
+                                                                   (Er *)out, flags, c->eval_fp64_eighths);
     else
         k_eval<N, FAST><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
-                                                           flags);
+                                                           flags, c->eval_fp64_eighths);
     return cuda_status(cudaGetLastError());
 }
 

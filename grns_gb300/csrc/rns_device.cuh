@@ -182,6 +182,37 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
     upp.exp -= K;
 }
 
+/* Common path on the FP64 pipe: the reference's own directed-rounding
+ * products and pairwise sums (src/rnseval.cuh:194-215), with eval_int's
+ * outcomes -- kEvalOk (low / upp set), kEvalZero, or kEvalRare for an
+ * ambiguous integer part or a fraction below RNS_EVAL_ACCURACY (eval_full
+ * decides those).  The same doubles as eval_int, which emulates exactly
+ * these operations on the integer pipe; a kernel can give some of its warps
+ * this form so the FP64 and integer pipes work at once. */
+template <int N, class Get, bool FAST = false>
+__device__ __forceinline__ int eval_fp64(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
+    PTree<N, false> tl;
+    PTree<N, true> tu;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t xi = get(i);
+        bad |= (uint32_t)(xi >= C.m[i]);
+        const double d = u32_to_double(mulmod_shoup(xi, C.w[i], C.w_sh[i], C.m[i]));
+        tl.push(i, __dmul_rd(d, C.rrd[i]));
+        tu.push(i, __dmul_ru(d, C.rru[i]));
+    }
+    double suml = tl.total(), sumu = tu.total();
+    if (suml == 0 && sumu == 0) return kEvalZero;
+    const unsigned whl = __double2uint_rz(suml), whu = __double2uint_rz(sumu);
+    if (!FAST && whl != whu) return kEvalRare;
+    suml = __dsub_rd(suml, u32_to_double(whl));
+    sumu = __dsub_ru(sumu, u32_to_double(whu));
+    if (sumu < C.acc) return kEvalRare;
+    low = er_from_double(suml);
+    upp = er_from_double(sumu);
+    return kEvalOk;
+}
+
 /* Common path on the integer pipe (eval_int, rns_fast.cuh: the same doubles as
  * the FP64 directed-rounding trees, computed exactly); falls back to eval_full
  * for ambiguous integer parts or small values (rare for uniform X). */

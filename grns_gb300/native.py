@@ -25,6 +25,8 @@ SIGNATURES = {
     "grns_ctx_log2": (c_int, [c_void_p]),
     "grns_ctx_get_table": (c_int, [c_void_p, c_int, c_void_p, c_size_t]),
     "grns_ctx_set_path": (c_int, [c_void_p, c_int]),
+    "grns_ctx_set_eval_split": (c_int, [c_void_p, c_int]),
+    "grns_ctx_get_eval_split": (c_int, [c_void_p]),
     "grns_device_ceil_log2": (c_int, [c_void_p, c_void_p, c_int64, c_void_p]),
     "grns_eval": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),
     "grns_eval_tight": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p]),

@@ -109,6 +109,15 @@ grns_status grns_ctx_get_table(const grns_ctx *ctx, int which, void *host_dst, s
 enum { GRNS_PATH_FAST = 0, GRNS_PATH_REFERENCE = 1 };
 grns_status grns_ctx_set_path(grns_ctx *ctx, int path);
 
+/* Share of grns_eval / grns_eval_fast work computed on the FP64 pipe, in
+ * eighths of the kernel's warps (0..8): those warps run the reference's own
+ * directed-rounding products and sums, the others the exact integer-pipe
+ * emulation of the same operations, so both pipes work at once and the
+ * intervals are the same bits for any setting.  No counterpart in the
+ * reference (a tuning knob of this implementation); default 3. */
+grns_status grns_ctx_set_eval_split(grns_ctx *ctx, int fp64_eighths);
+int grns_ctx_get_eval_split(const grns_ctx *ctx);
+
 /* ceil(log2(x)) as the device computes it inside the evaluation's refinement
  * loop (src/rnseval.cuh:236 calls CUDA's log2, which is not exact at every
  * power of two).  Diagnostics for checking; x, out are device arrays. */

@@ -91,7 +91,7 @@ _NOT_HANDLE_FIRST = {"grns_status_string", "grns_version", "grns_ctx_create", "g
                      "grns_ctx_create_from_params", "grns_server_create", "grns_device_ceil_log2", "grns_gen_shifts"}
 # queries that answer with a value rather than a status
 _QUERIES = {"grns_ctx_n": 0, "grns_ctx_log2": 0, "grns_ctx_binary_limbs": 0, "grns_batch_chunks": -1,
-            "grns_batch_grid": -1}
+            "grns_batch_grid": -1, "grns_ctx_get_eval_split": -1}
 
 
 def test_null_handle_rejected_by_every_entry(lib):

@@ -98,6 +98,30 @@ def test_eval_golden(case, layout):
         assert out.cpu().numpy().tobytes() == g["eval_dev"].tobytes()
 
 
+@pytest.mark.parametrize("split", [0, 5, 8])
+def test_eval_pipe_split_same_bits(case, split):
+    """grns_eval with 0, 5 and 8 eighths of its warps on the FP64 pipe (the
+    rest on the integer pipe): the oracle's bits every time, the golden
+    vectors and fresh uniform numbers, the full and the fast form"""
+    from grns_gb300 import native
+    tag, ctx, orc, g = case
+    L = native.lib()
+    native.check(L.grns_ctx_set_eval_split(ctx.handle, split))
+    try:
+        assert L.grns_ctx_get_eval_split(ctx.handle) == split
+        x = np.concatenate([g["x"], W.uniform_residues(orc.moduli, 20000, seed=77, stream=W.S_X, layout="aos")])
+        got = ctx.rns_eval_compute(to_dev(x, "soa")).cpu().numpy()
+        assert got.tobytes() == oracle_eval_device(ctx, orc, x).tobytes()
+        P = O.PATH_DEVICE_FAST
+        xs = orc.log2_inputs(g["xf"], path=P)
+        want = orc.eval_with_device_log2(g["xf"], xs, ctx.device_ceil_log2(xs) if len(xs) else np.zeros(0, np.int32),
+                                         path=P)
+        assert ctx.rns_eval_compute_fast(to_dev(g["xf"], "soa")).cpu().numpy().tobytes() == want.tobytes()
+    finally:
+        native.check(L.grns_ctx_set_eval_split(ctx.handle, 3))
+    assert L.grns_ctx_set_eval_split(ctx.handle, 9) == 1  # out of range
+
+
 @pytest.mark.parametrize("layout", ["soa", "aos"])
 def test_eval_fast(case, layout):
     """cuda::rns_eval_compute_fast (src/rnseval.cuh:266) on numbers below M/2"""
