@@ -31,7 +31,7 @@ struct grns_ctx {
     int path = 0;  // 0: integer fast path, 1: reference-faithful FP64 kernels (GRNS_PATH_*)
     /* eighths of the bit-identical evaluation's warps that compute on the FP64 pipe (the rest on
      * the integer pipe; the same bits either way) */
-    int eval_fp64_eighths = 3;
+    int eval_fp64_eighths = 4;
     grns::HostTables T;  // host copies of all tables
     void *d_tables = nullptr;  // one device allocation holding the table blob
     /* stream-ordered pool for per-call scratch (division records, scaling and

@@ -114,7 +114,8 @@ grns_status grns_ctx_set_path(grns_ctx *ctx, int path);
  * directed-rounding products and sums, the others the exact integer-pipe
  * emulation of the same operations, so both pipes work at once and the
  * intervals are the same bits for any setting.  No counterpart in the
- * reference (a tuning knob of this implementation); default 3. */
+ * reference (a tuning knob of this implementation); default 4, which gives
+ * each SM scheduler one warp of each kind. */
 grns_status grns_ctx_set_eval_split(grns_ctx *ctx, int fp64_eighths);
 int grns_ctx_get_eval_split(const grns_ctx *ctx);
 

@@ -118,7 +118,7 @@ def test_eval_pipe_split_same_bits(case, split):
                                          path=P)
         assert ctx.rns_eval_compute_fast(to_dev(g["xf"], "soa")).cpu().numpy().tobytes() == want.tobytes()
     finally:
-        native.check(L.grns_ctx_set_eval_split(ctx.handle, 3))
+        native.check(L.grns_ctx_set_eval_split(ctx.handle, 4))
     assert L.grns_ctx_set_eval_split(ctx.handle, 9) == 1  # out of range
 
 
