@@ -43,6 +43,8 @@ struct JobDev {
     const Er *eval_a, *eval_b;  // cmp: optional cached evaluations (2 Er per number)
     uint2 *rec;                 // div: pass-A records (one per number; also reserved for scale jobs)
     int32_t *order;             // div, scale with per-number exponents: longest-first order
+    uint32_t *rdig;             // mp_int div: remainder digits, N per number
+    uint8_t *mflags;            // mp_int div: the division's flags per number
     uint32_t D_uniform;
     int32_t coop;
     int32_t vec;  // AoS operands 16-byte aligned, n a multiple of 4: a number's residues as 16-byte loads
@@ -252,6 +254,27 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
                          cols + threadIdx.x, blockDim.x, hist + (threadIdx.x / 32) * kDivBins);
         }
             break;
+        case GRNS_OP_MPINT_DIV: {  // mpint_div (src/mpint.cuh:511): the division of the digit fields in place,
+                                   // then the Euclidean step, evaluation and sign of each number of the chunk
+            uint32_t *hist = smem + BatchCfg<N>::kTables / 4;
+            uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
+            const MpInt<N> *px = (const MpInt<N> *)J.a, *py = (const MpInt<N> *)J.b;
+            MpInt<N> *po = (MpInt<N> *)J.out0;
+            div_range<N>(reinterpret_cast<const DivK *>(smem), C, MpDigitsIn<N>{J.a}, MpDigitsIn<N>{J.b}, J.rec,
+                         J.order, MpDigitsOut<N>{(uint32_t *)J.out0}, Output<N>{J.rdig, 0}, J.mflags, start, end,
+                         cols + threadIdx.x, blockDim.x, hist + (threadIdx.x / 32) * kDivBins);
+            __syncwarp();  // the chunk's quotients and remainders, written by every lane
+            for (int64_t k = start + lane; k < end; k += 32) {
+                uint32_t f = J.mflags[k];
+                const uint32_t *qd = po[k].digits, *rd = J.rdig + k * N;
+                MpInt<N> res;
+                mpint_div_finish<N>(C, __ldg(&px[k].sign), __ldg(&py[k].sign), [&](int i) { return qd[i]; },
+                                    [&](int i) { return rd[i]; }, f, res);
+                po[k] = res;
+                if (J.flags) J.flags[k] = (uint8_t)f;
+            }
+            break;
+        }
         case GRNS_OP_SCALE2POW: {
             uint32_t *hist = smem + BatchCfg<N>::kTables / 4;
             uint32_t *cols = hist + (blockDim.x / 32) * kDivBins;
@@ -362,6 +385,7 @@ struct grns_batch {
     int64_t total_chunks = 0;
     int64_t nparts = 0;
     int64_t nrec = 0;                // division records
+    int64_t nmp = 0;                 // numbers of mp_int division jobs (remainder digits and flags)
     uint2 *d_rec = nullptr;
     std::vector<JobDev> host_jobs;   // execution order
     std::vector<int> order;          // host_jobs[t] = user job order[t]
@@ -382,7 +406,8 @@ namespace {
 
 double op_cost(int op, int n) {
     switch (op) {
-        case GRNS_OP_DIV: return 400.0 * n;
+        case GRNS_OP_DIV:
+        case GRNS_OP_MPINT_DIV: return 400.0 * n;
         case GRNS_OP_SCALE2POW: return 60.0 * n;
         case GRNS_OP_EVAL: return 8.0 * n;
         case GRNS_OP_MPINT_ADD:
@@ -392,8 +417,13 @@ double op_cost(int op, int n) {
     }
 }
 
+/* bytes of the division scratch: records and orders, mp_int remainder digits and flags */
+size_t batch_rec_bytes(const grns_batch *b) {
+    return kDivScratchPerNumber * (size_t)b->nrec + (4 * (size_t)b->ctx->n + 1) * (size_t)b->nmp;
+}
+
 bool job_ok(const grns_ctx *c, const grns_job &jb) {
-    if (jb.op < GRNS_OP_EVAL || jb.op > GRNS_OP_MPINT_MUL || jb.count < 0) return false;
+    if (jb.op < GRNS_OP_EVAL || jb.op > GRNS_OP_MPINT_DIV || jb.count < 0) return false;
     if (jb.ld != 0 && jb.ld < jb.count) return false;
     if (jb.layout != GRNS_LAYOUT_SOA && jb.layout != GRNS_LAYOUT_AOS) return false;
     if (jb.count == 0) return jb.op != GRNS_OP_MAX || jb.out0;
@@ -402,7 +432,8 @@ bool job_ok(const grns_ctx *c, const grns_job &jb) {
         case GRNS_OP_CMP:
         case GRNS_OP_MPINT_ADD:
         case GRNS_OP_MPINT_SUB:
-        case GRNS_OP_MPINT_MUL: return jb.b != nullptr;
+        case GRNS_OP_MPINT_MUL:
+        case GRNS_OP_MPINT_DIV: return jb.b != nullptr;
         case GRNS_OP_DIV: return jb.b && jb.out1;
         default: return true;
     }
@@ -441,7 +472,7 @@ int occupancy_blocks(size_t smem) {
 void batch_shape(grns_batch *b) {
     bool has_div = false;
     for (const JobDev &J : b->host_jobs)
-        has_div |= (J.op == GRNS_OP_DIV || J.op == GRNS_OP_SCALE2POW) && J.count > 0;
+        has_div |= (J.op == GRNS_OP_DIV || J.op == GRNS_OP_MPINT_DIV || J.op == GRNS_OP_SCALE2POW) && J.count > 0;
     int per_sm = 1;
 #define C_(n)                                                  \
     b->smem = has_div ? BatchCfg<n>::kHeavySmem : 0;           \
@@ -463,7 +494,7 @@ void batch_shape(grns_batch *b) {
 /* fill the device-side descriptors from user jobs (fixed order) */
 grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
     const grns_ctx *c = b->ctx;
-    int64_t chunk = 0, parts = 0, recs = 0;
+    int64_t chunk = 0, parts = 0, recs = 0, mps = 0;
     for (int t = 0; t < b->njobs; t++) {
         const grns_job &u = jobs[b->order[t]];
         JobDev &J = b->host_jobs[t];
@@ -481,9 +512,15 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
         J.D_uniform = u.D_uniform;
         J.rec = nullptr;
         J.order = nullptr;
-        if (u.op == GRNS_OP_DIV || (u.op == GRNS_OP_SCALE2POW && u.b)) {
+        J.rdig = nullptr;
+        J.mflags = nullptr;
+        if (u.op == GRNS_OP_DIV || u.op == GRNS_OP_MPINT_DIV || (u.op == GRNS_OP_SCALE2POW && u.b)) {
             J.rec = b->d_rec ? b->d_rec + recs : nullptr;
             recs += u.count;
+        }
+        if (u.op == GRNS_OP_MPINT_DIV) {  // placed below, after the records and orders
+            J.rdig = (uint32_t *)(uintptr_t)mps;
+            mps += u.count;
         }
         const int op = u.op;
         const Sched &sc = c->sched[op];
@@ -501,12 +538,21 @@ grns_status fill_jobs(grns_batch *b, const grns_job *jobs) {
     b->total_chunks = chunk;
     b->nparts = parts;
     b->nrec = recs;
-    /* the orders follow the records in the same allocation */
-    if (b->d_rec) {
+    b->nmp = mps;
+    /* one allocation: the records, the orders, then the mp_int divisions'
+     * remainder digits and flags */
+    for (int t = 0; t < b->njobs; t++) {
+        JobDev &J = b->host_jobs[t];
+        const int64_t mp_first = (int64_t)(uintptr_t)J.rdig;
+        J.rdig = nullptr;
+        if (!b->d_rec) continue;
         int32_t *ord = (int32_t *)(b->d_rec + recs);
-        for (int t = 0; t < b->njobs; t++) {
-            JobDev &J = b->host_jobs[t];
-            if (J.rec) J.order = ord + (J.rec - b->d_rec);
+        uint32_t *rd = (uint32_t *)(ord + recs);
+        uint8_t *mf = (uint8_t *)(rd + (size_t)c->n * mps);
+        if (J.rec) J.order = ord + (J.rec - b->d_rec);
+        if (J.op == GRNS_OP_MPINT_DIV) {
+            J.rdig = rd + (size_t)c->n * mp_first;
+            J.mflags = mf + mp_first;
         }
     }
     b->empty_max_index.clear();
@@ -543,7 +589,7 @@ grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *
     b.counters_bytes = sizeof(unsigned long long) + sizeof(unsigned) * (size_t)(njobs > 0 ? njobs : 1);
     cudaError_t e = cudaSuccess;
     if (b.nrec) {
-        e = scratch_alloc(c, (void **)&b.d_rec, kDivScratchPerNumber * b.nrec, s);
+        e = scratch_alloc(c, (void **)&b.d_rec, batch_rec_bytes(&b), s);
         if (e != cudaSuccess) return cuda_status(e);
         fill_jobs(&b, jobs);
     }
@@ -610,7 +656,7 @@ grns_status grns_batch_create(grns_ctx *c, const grns_job *jobs, int njobs, int 
     if (e == cudaSuccess && njobs) e = cudaMalloc(&b->d_jobs, sizeof(JobDev) * njobs);
     if (e == cudaSuccess && b->nparts) e = cudaMalloc(&b->d_parts, sizeof(Part) * b->nparts);
     if (e == cudaSuccess && b->nrec) {
-        e = cudaMalloc(&b->d_rec, kDivScratchPerNumber * b->nrec);
+        e = cudaMalloc(&b->d_rec, batch_rec_bytes(b));
         if (e == cudaSuccess) fill_jobs(b, jobs);
     }
     if (e == cudaSuccess && njobs)

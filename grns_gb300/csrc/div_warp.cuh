@@ -130,10 +130,10 @@ __device__ __forceinline__ int div_final_tie(const DivK *K, const Consts<N> &C, 
 /* pass A over the numbers claim() hands out below end: rec[k] = record of
  * number k.  Column rows: the working value in rows [0, N), the dividend in
  * rows [N, 2N). */
-template <int N, class Claim, class Finish>
-__device__ __forceinline__ void divnorm_range_f(const DivK *K, const Consts<N> &C, const Operand<N> &x,
-                                                const Operand<N> &d, Finish finish, int64_t end, Claim claim,
-                                                int64_t prefetch, uint32_t *col, int stride) {
+template <int N, class Claim, class Finish, class Op>
+__device__ __forceinline__ void divnorm_range_f(const DivK *K, const Consts<N> &C, const Op &x, const Op &d,
+                                                Finish finish, int64_t end, Claim claim, int64_t prefetch,
+                                                uint32_t *col, int stride) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -243,10 +243,9 @@ __device__ __forceinline__ void divnorm_range_f(const DivK *K, const Consts<N> &
 }
 
 /* pass A writing records rec[k] (the batched kernel's per-warp form) */
-template <int N, class Claim>
-__device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
-                                              const Operand<N> &d, uint2 *rec, int64_t end, Claim claim,
-                                              int64_t prefetch, uint32_t *col, int stride) {
+template <int N, class Claim, class Op>
+__device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C, const Op &x, const Op &d, uint2 *rec,
+                                              int64_t end, Claim claim, int64_t prefetch, uint32_t *col, int stride) {
     divnorm_range_f<N>(K, C, x, d, [&](int64_t idx, uint2 r, const uint32_t *) { rec[idx] = r; }, end, claim,
                        prefetch, col, stride);
 }
@@ -254,12 +253,11 @@ __device__ __forceinline__ void divnorm_range(const DivK *K, const Consts<N> &C,
 /* pass B over [begin, end) with the records of pass A, numbers taken in the
  * order of div_order.  Column rows: R in [0, N), the scaled divisor D in
  * [N, 2N), the quotient Q in [2N, 3N). */
-template <int N, class Claim>
-__device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
-                                              const Operand<N> &d, const uint2 *rec, const int32_t *order,
-                                              const Output<N> &qo, const Output<N> &ro, uint8_t *flags,
-                                              int64_t begin, int64_t end, Claim claim, uint32_t *col,
-                                              int stride) {
+template <int N, class Claim, class Op, class OutQ, class OutR>
+__device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C, const Op &x, const Op &d,
+                                              const uint2 *rec, const int32_t *order, const OutQ &qo,
+                                              const OutR &ro, uint8_t *flags, int64_t begin, int64_t end, Claim claim,
+                                              uint32_t *col, int stride) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -708,11 +706,10 @@ __device__ __forceinline__ void div_order(const uint2 *rec, int32_t *order, int6
  * the range's index space (index k in [begin, end)); col: this thread's
  * 3N-word shared-memory column (row stride `stride` words); hist: this
  * warp's kDivBins shared counters */
-template <int N>
-__device__ __forceinline__ void div_range(const DivK *K, const Consts<N> &C, const Operand<N> &x,
-                                          const Operand<N> &d, uint2 *rec, int32_t *order, const Output<N> &qo,
-                                          const Output<N> &ro, uint8_t *flags, int64_t begin, int64_t end,
-                                          uint32_t *col, int stride, uint32_t *hist) {
+template <int N, class Op, class OutQ, class OutR>
+__device__ __forceinline__ void div_range(const DivK *K, const Consts<N> &C, const Op &x, const Op &d, uint2 *rec,
+                                          int32_t *order, const OutQ &qo, const OutR &ro, uint8_t *flags,
+                                          int64_t begin, int64_t end, uint32_t *col, int stride, uint32_t *hist) {
     int64_t next = begin;
     divnorm_range<N>(K, C, x, d, rec, end, [&](int c) { const int64_t b = next; next += c; return b; }, kDivPrefetch,
                      col, stride);

@@ -266,24 +266,10 @@ __global__ void __launch_bounds__(128) k_mpint_div_finish(const __grid_constant_
                                                           MpInt<N> *__restrict__ out, uint8_t *__restrict__ flags) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = flags[k];
-        const bool bad = (f & (kFlagInvalidInput | kFlagDivByZero)) != 0;
-        bool rz = true;
-#pragma unroll 8
-        for (int i = 0; i < N; i++) rz &= __ldg(r + (int64_t)i * count + k) == 0;
-        const int xs = __ldg(&x[k].sign), ys = __ldg(&y[k].sign);
-        const bool inc = xs == 1 && !rz && !bad;
         MpInt<N> res;
-        bool qz = true;
-#pragma unroll 8
-        for (int i = 0; i < N; i++) {
-            uint32_t v = bad ? 0u : __ldg(q + (int64_t)i * count + k);
-            if (inc) v = addmod(v, 1u, C.m[i]);
-            res.digits[i] = v;
-            qz &= v == 0;
-        }
-        eval<N>(C, [&](int i) { return res.digits[i]; }, res.eval[0], res.eval[1], f);
-        res.sign = qz ? 0 : (xs ^ ys);
-        res.pad = 0;
+        mpint_div_finish<N>(C, __ldg(&x[k].sign), __ldg(&y[k].sign),
+                            [&](int i) { return __ldg(q + (int64_t)i * count + k); },
+                            [&](int i) { return __ldg(r + (int64_t)i * count + k); }, f, res);
         out[k] = res;
         flags[k] = (uint8_t)f;
     }

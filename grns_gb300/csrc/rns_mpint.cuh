@@ -22,6 +22,51 @@ static_assert(sizeof(MpInt<8>) == 72 && sizeof(MpInt<32>) == 168 && sizeof(MpInt
 
 __device__ __forceinline__ double neg_if(double v, bool neg) { return neg ? -v : v; }
 
+/* the digits of an array of mp_int_t records as an operand / output of the
+ * warp division driver (digit i of record k) */
+template <int N>
+struct MpDigitsIn {
+    const uint32_t *base;  // record 0
+    static constexpr int RW = (int)(sizeof(MpInt<N>) / 4);
+    __device__ __forceinline__ uint32_t load(int64_t k, int i) const { return __ldg(base + k * RW + i); }
+    __device__ __forceinline__ void prefetch_l2(int64_t k) const {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + k * RW));
+    }
+};
+template <int N>
+struct MpDigitsOut {
+    uint32_t *base;
+    static constexpr int RW = (int)(sizeof(MpInt<N>) / 4);
+    __device__ __forceinline__ void store(int64_t k, int i, uint32_t v) const { base[k * RW + i] = v; }
+};
+
+/* mpint_div's last step (reference src/mpint.cuh:511): from the division of
+ * the magnitudes (quotient digits q(i), remainder digits r(i), its flags f),
+ * the Euclidean quotient -- one more when the dividend is negative and the
+ * remainder nonzero, so that x = q y + r with 0 <= r < |y| -- its
+ * evaluation and sign; an invalid digit or a zero divisor gives the zero
+ * record.  res: digits, sign, evaluation and padding written. */
+template <int N, class GQ, class GR>
+__device__ __forceinline__ void mpint_div_finish(const Consts<N> &C, int xs, int ys, GQ q, GR r, uint32_t &f,
+                                                 MpInt<N> &res) {
+    const bool bad = (f & (kFlagInvalidInput | kFlagDivByZero)) != 0;
+    bool rz = true;
+#pragma unroll 8
+    for (int i = 0; i < N; i++) rz &= r(i) == 0;
+    const bool inc = xs == 1 && !rz && !bad;
+    bool qz = true;
+#pragma unroll 8
+    for (int i = 0; i < N; i++) {
+        uint32_t v = bad ? 0u : q(i);
+        if (inc) v = addmod(v, 1u, C.m[i]);
+        res.digits[i] = v;
+        qz &= v == 0;
+    }
+    eval<N>(C, [&](int i) { return res.digits[i]; }, res.eval[0], res.eval[1], f);
+    res.sign = qz ? 0 : (xs ^ ys);
+    res.pad = 0;
+}
+
 /* the sign and evaluation of an mp_int (the part of the record besides the digits) */
 struct MpIntHead {
     int32_t sign;

@@ -196,8 +196,8 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
         case GRNS_OP_DIV: return 2 * 4 * (size_t)n * k + (12 * (size_t)k);  // + the batched kernel's records
         case GRNS_OP_SCALE2POW: return (4 * (size_t)n + 12) * k;
         case GRNS_OP_MAX: return ((4 * (size_t)n + 7) / 8) * 8 + 8;
-        case GRNS_OP_MPINT_DIV:  // + digit columns, the division's scratch
-            return (GRNS_MPINT_BYTES(n) + 16 * (size_t)n + 1) * k + grns::div_scratch_bytes(c, k);
+        case GRNS_OP_MPINT_DIV:  // + the batched kernel's records, remainder digits and flags
+            return (GRNS_MPINT_BYTES(n) + 12 + 4 * (size_t)n + 1) * k;
         default: return GRNS_MPINT_BYTES(n) * (size_t)k;
     }
 }
@@ -242,9 +242,8 @@ void schedule_locked(grns_server *sv) {
     for (Slot *sl : sv->slots) {
         if (sl->busy || sv->pending.empty()) continue;
         int ctx = -1;  // the moduli set of this launch: that of the oldest request admitted
-        std::vector<grns_job> jobs, divs;
-        for (auto it = sv->pending.begin();
-             it != sv->pending.end() && (int)(jobs.size() + divs.size()) < sv->opt.max_jobs_per_launch;) {
+        std::vector<grns_job> jobs;
+        for (auto it = sv->pending.begin(); it != sv->pending.end() && (int)jobs.size() < sv->opt.max_jobs_per_launch;) {
             const uint64_t id = *it;
             Req &q = sv->reqs.at(id);
             if (ctx >= 0 && q.r.ctx_index != ctx) {
@@ -342,16 +341,11 @@ void schedule_locked(grns_server *sv) {
             if (q.r.op == GRNS_OP_EVAL && q.count == A.count) sv->arrays[q.r.a].eval = q.out0;
             q.state = 1;
             sl->reqs.push_back(id);
-            if (q.r.op == GRNS_OP_MPINT_DIV) divs.push_back(j);  // its own launches (grns_mpint_div)
-            else jobs.push_back(j);
+            jobs.push_back(j);
         }
-        if (jobs.empty() && divs.empty()) continue;
+        if (jobs.empty()) continue;
         grns::NvtxRange range("grns_server launch");
-        grns_status st = GRNS_OK;
-        if (!jobs.empty())
-            st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
-        for (size_t t = 0; st == GRNS_OK && t < divs.size(); t++)
-            st = grns::launch_mpint(sv->ctxs[ctx], 3, divs[t].a, divs[t].b, divs[t].count, divs[t].out0, nullptr, sl->s);
+        grns_status st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
         if (st == GRNS_OK) st = grns::cuda_status(cudaLaunchHostFunc(sl->s, on_launch_done, sl));
         if (st != GRNS_OK) {
             for (uint64_t id : sl->reqs) finish(sv, id, sv->reqs.at(id), st, now_us());
@@ -360,7 +354,7 @@ void schedule_locked(grns_server *sv) {
         }
         sl->busy = true;
         sv->launches++;
-        sv->jobs_launched += jobs.size() + divs.size();
+        sv->jobs_launched += jobs.size();
     }
 }
 

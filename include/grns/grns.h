@@ -291,8 +291,8 @@ typedef enum {
     GRNS_OP_MPINT_ADD = 5,  /* a, b, out0: mp_int_t arrays */
     GRNS_OP_MPINT_SUB = 6,
     GRNS_OP_MPINT_MUL = 7,
-    GRNS_OP_MPINT_DIV = 8   /* a, b, out0: mp_int_t arrays; served only (its own launches, as grns_mpint_div),
-                               not a job type of grns_batch */
+    GRNS_OP_MPINT_DIV = 8   /* a, b, out0: mp_int_t arrays; the Euclidean quotient of grns_mpint_div
+                               (cuda::mpint_div, src/mpint.cuh:511), the division fused in the batched kernel */
 } grns_op;
 
 typedef struct {

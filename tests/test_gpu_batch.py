@@ -35,8 +35,8 @@ def make_jobs(ctx, n, rng, njobs, stream):
     L = native.lib()
     jobs, bufs = [], []
     for t in range(njobs):
-        op = rng.choice([0, 1, 2, 3, 4, 5, 6, 7])
-        count = rng.choice([0, 1, 3, 31, 100, 1000, 5000, 20000 if op not in (2, 3) else 2000])
+        op = rng.choice([0, 1, 2, 3, 4, 5, 6, 7, 8])
+        count = rng.choice([0, 1, 3, 31, 100, 1000, 5000, 20000 if op not in (2, 3, 8) else 2000])
         layout = rng.choice([0, 1]) if op < 5 else 0
         j = native.Job()
         j.op, j.layout, j.count = op, layout, count
@@ -44,10 +44,12 @@ def make_jobs(ctx, n, rng, njobs, stream):
             nb = mpint_bytes(n)
             a = torch.zeros(max(1, count) * nb, dtype=torch.uint8, device="cuda")
             b = torch.zeros_like(a)
-            if count:  # signed operands whose products stay below M, evaluations from the device path
-                bits = L.grns_ctx_log2(ctx) // 2 - 10
-                native.check(L.grns_gen_mpint(ctx, 70 + t, count, bits, P(a), stream))
-                native.check(L.grns_gen_mpint(ctx, 170 + t, count, bits, P(b), stream))
+            if count:  # signed operands whose products stay below M, evaluations from the device path;
+                # division: dividends of nearly the full range, divisors of half of it
+                lg = L.grns_ctx_log2(ctx)
+                bits_a, bits_b = (lg - 8, lg // 2) if op == 8 else (lg // 2 - 10, lg // 2 - 10)
+                native.check(L.grns_gen_mpint(ctx, 70 + t, count, bits_a, P(a), stream))
+                native.check(L.grns_gen_mpint(ctx, 170 + t, count, bits_b, P(b), stream))
             o0 = torch.zeros_like(a)
             j.a, j.b, j.out0 = a.data_ptr(), b.data_ptr(), o0.data_ptr()
             bufs.append((op, count, layout, a, b, o0, None))
@@ -108,7 +110,7 @@ def reference_outputs(L, ctx, n, bufs, stream):
             elif op == 4:
                 native.check(L.grns_max(ctx, P(a), count, layout, P(r0), P(r1), None, 0, stream))
             else:
-                fn = {5: L.grns_mpint_add, 6: L.grns_mpint_sub, 7: L.grns_mpint_mul}[op]
+                fn = {5: L.grns_mpint_add, 6: L.grns_mpint_sub, 7: L.grns_mpint_mul, 8: L.grns_mpint_div}[op]
                 native.check(fn(ctx, P(a), P(b), count, P(r0), None, stream))
         elif op == 4:
             r1.fill_(-1)
