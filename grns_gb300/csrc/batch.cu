@@ -432,8 +432,14 @@ bool job_ok(const grns_ctx *c, const grns_job &jb) {
         case GRNS_OP_CMP:
         case GRNS_OP_MPINT_ADD:
         case GRNS_OP_MPINT_SUB:
-        case GRNS_OP_MPINT_MUL:
-        case GRNS_OP_MPINT_DIV: return jb.b != nullptr;
+        case GRNS_OP_MPINT_MUL: return jb.b != nullptr;
+        case GRNS_OP_MPINT_DIV: {  // the quotient digits are written while the operands are still read
+            const size_t bytes = (size_t)GRNS_MPINT_BYTES(c->n) * (size_t)jb.count;
+            auto overlap = [&](const void *p) {
+                return (const char *)p < (const char *)jb.out0 + bytes && (const char *)jb.out0 < (const char *)p + bytes;
+            };
+            return jb.b != nullptr && !overlap(jb.a) && !overlap(jb.b);
+        }
         case GRNS_OP_DIV: return jb.b && jb.out1;
         default: return true;
     }

@@ -292,7 +292,8 @@ typedef enum {
     GRNS_OP_MPINT_SUB = 6,
     GRNS_OP_MPINT_MUL = 7,
     GRNS_OP_MPINT_DIV = 8   /* a, b, out0: mp_int_t arrays; the Euclidean quotient of grns_mpint_div
-                               (cuda::mpint_div, src/mpint.cuh:511), the division fused in the batched kernel */
+                               (cuda::mpint_div, src/mpint.cuh:511), the division fused in the batched kernel;
+                               out0 must not overlap a or b */
 } grns_op;
 
 typedef struct {
