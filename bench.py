@@ -306,6 +306,9 @@ def run_only(args):
     if args.only == "mpdiv32":  # signed dividends below 2^900, divisors below 2^450
         native.check(L.grns_gen_mpint(ctx.handle, SEED, cnt, 900, P(ma), sp))
         native.check(L.grns_gen_mpint(ctx.handle, SEED + 1, cnt, 450, P(mc), sp))
+    if args.only == "mpint64":  # the workload's operands: random signs, magnitudes below 2^950
+        native.check(L.grns_gen_mpint(ctx.handle, SEED, cnt, MP_BITS, P(ma), sp))
+        native.check(L.grns_gen_mpint(ctx.handle, SEED + 1, cnt, MP_BITS, P(mc), sp))
     def call():
         if args.only == "div":
             native.check(L.grns_div(ctx.handle, P(x), P(y), cnt, 0, P(a), P(b), None, sp))
@@ -320,7 +323,7 @@ def run_only(args):
         elif args.only == "evtight32":
             native.check(L.grns_eval_tight(ctx.handle, P(x), cnt, 0, P(out), None, sp))
         elif args.only == "mpint64":
-            native.check(L.grns_mpint_mul(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
+            native.check(getattr(L, f"grns_mpint_{args.mp_op}")(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
         elif args.only == "mpdiv32":
             native.check(L.grns_mpint_div(ctx.handle, P(ma), P(mc), cnt, P(mo), None, sp))
         elif args.only in ("tobin32", "tobin64"):
@@ -768,6 +771,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
+    ap.add_argument("--mp-op", default="mul", choices=["add", "sub", "mul"], help="profiling: the mpint64 operation")
     ap.add_argument("--eval-split", type=int, default=None,
                     help="profiling: eighths of the evaluation's warps on the FP64 pipe (grns_ctx_set_eval_split)")
     ap.add_argument("--only", choices=["div", "scale", "cmp32", "cmp8", "max64", "eval32", "evtight32", "mpint64",

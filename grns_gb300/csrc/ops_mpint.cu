@@ -144,7 +144,7 @@ __device__ __forceinline__ void mp_chunk(const Consts<N> &C, const uint4 *K, int
         a.pad = 0;
         a.eval[0] = lo;
         a.eval[1] = up;
-        f |= overflow_flags<N>(C, lo, up);
+        f |= overflow_flags_i<N>(C, lo, up);
         if (flags) flags[k0 + t] = (uint8_t)f;
     }
     __syncwarp();

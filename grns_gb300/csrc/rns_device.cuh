@@ -412,6 +412,80 @@ __device__ __forceinline__ Er er_add_dir(Er x, Er y) {
     return r;
 }
 
+/* ---- the same operations with the bit handling on the integer pipe ----
+ * Sign tests, sign flips, the exponent renormalisation of er_adjust and
+ * scalbn of a normal result are exact bit operations on the IEEE encoding;
+ * on GB300 the FP64 pipe (a few operations per clock per SM) would otherwise
+ * bound the mp_int kernels.  Only the directed-rounding addition itself stays
+ * an FP64 instruction.  Results are bit-identical to the FP64 forms above. */
+__device__ __forceinline__ bool dneg_i(double v) {  // v < 0 (false for -0)
+    const uint64_t u = dbits(v);
+    return (u >> 63) && (u << 1);
+}
+__device__ __forceinline__ bool dnz_i(double v) { return (dbits(v) << 1) != 0; }  // v != 0
+__device__ __forceinline__ double dflip_i(double v, bool neg) {                   // neg ? -v : v
+    return bitsd(dbits(v) ^ ((uint64_t)neg << 63));
+}
+/* scalbn(v, -d) for d >= 0: exact exponent arithmetic while the result stays
+ * normal, the library call otherwise (a subnormal or zero result) */
+__device__ __forceinline__ double scalbn_down_i(double v, int d) {
+    const uint64_t u = dbits(v);
+    const int e = (int)((u >> 52) & 0x7ff);
+    if (e == 0x7ff || (e == 0 && !(u << 1))) return v;  // infinities, NaN, +-0 are unchanged
+    if (e - d >= 1) return bitsd(u - ((uint64_t)d << 52));
+    return scalbn(v, -d);  // a subnormal argument or result
+}
+/* er_adjust (src/extrange.cuh:366) on the integer pipe: the frac of a zero
+ * keeps its sign, as the reference's multiplication by 0.0 does */
+__device__ __forceinline__ void er_adjust_i(Er &x) {
+    const uint64_t u = dbits(x.frac);
+    if (u << 1) {
+        x.exp = x.exp + (int64_t)((u & 0x7fffffffffffffffull) >> 52) - 1023;
+        x.frac = bitsd((u & 0x800fffffffffffffull) | 0x3ff0000000000000ull);
+    } else {
+        x.exp = 0;
+        x.frac = bitsd(u & 0x8000000000000000ull);
+    }
+}
+template <bool UP>
+__device__ __forceinline__ Er er_add_dir_i(Er x, Er y) {
+    const bool xz = !dnz_i(x.frac), yz = !dnz_i(y.frac);
+    if (xz) x.exp = 0;
+    if (yz) y.exp = 0;
+    const int dexp = (xz || yz) ? 0 : (int)(x.exp - y.exp);
+    Er r;
+    double a, b;
+    if (dexp > 0) {
+        r.exp = x.exp; a = x.frac; b = scalbn_down_i(y.frac, dexp);
+    } else if (dexp < 0) {
+        r.exp = y.exp; a = y.frac; b = scalbn_down_i(x.frac, -dexp);
+    } else {
+        r.exp = (x.exp == 0) ? y.exp : x.exp; a = x.frac; b = y.frac;
+    }
+    r.frac = UP ? __dadd_ru(a, b) : __dadd_rd(a, b);
+    er_adjust_i(r);
+    return r;
+}
+/* total order of doubles (not NaN) as unsigned keys */
+__device__ __forceinline__ uint64_t dkey_i(double v) {
+    const uint64_t u = dbits(v);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+/* er_ucmp (src/extrange.cuh:597) with the double comparisons as key comparisons
+ * (-0 and +0 compare equal there, as in the FP64 form) */
+__device__ __forceinline__ int er_ucmp_i(const Er &x, const Er &y) {
+    const uint64_t kx = dnz_i(x.frac) ? dkey_i(x.frac) : dkey_i(0.0), ky = dnz_i(y.frac) ? dkey_i(y.frac) : dkey_i(0.0);
+    const int diff = (int)(x.exp - y.exp);
+    if (diff == 0) return kx == ky ? 0 : (kx > ky ? 1 : -1);
+    return (dnz_i(x.frac) && (diff > 0 || (diff < 0 && !dnz_i(y.frac)))) ? 1 : -1;
+}
+template <int N>
+__device__ __forceinline__ uint32_t overflow_flags_i(const Consts<N> &C, const Er &low, const Er &upp) {
+    if (upp.exp < -1 || er_ucmp_i(upp, C.inv_unit_low) <= 0) return 0;
+    if (er_ucmp_i(low, C.inv_unit_upp) == 1) return kFlagOverflow;
+    return kFlagMayOverflow;
+}
+
 /* er_md_rd / er_md_ru (src/extrange.cuh:557/:566) */
 template <bool UP>
 __device__ __forceinline__ Er er_md(const Er &x, const Er &y, const Er &z) {

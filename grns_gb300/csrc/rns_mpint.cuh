@@ -84,17 +84,17 @@ __device__ __forceinline__ MpIntHead head_of(const MpInt<N> &x) {
 __device__ __forceinline__ bool mpint_addsub_eval(const MpIntHead &x, const MpIntHead &y, bool sub, Er &lo, Er &up) {
     const int sx = x.sign, sy = sub ? (y.sign ^ 1) : y.sign;
     Er evx[2] = {x.eval[0], x.eval[1]}, evy[2] = {y.eval[0], y.eval[1]};
-    evx[0].frac = neg_if(evx[0].frac, sx);
-    evx[1].frac = neg_if(evx[1].frac, sx);
-    evy[0].frac = neg_if(evy[0].frac, sy);
-    evy[1].frac = neg_if(evy[1].frac, sy);
-    lo = er_add_dir<false>(evx[sx], evy[sy]);
-    up = er_add_dir<true>(evx[1 - sx], evy[1 - sy]);
-    const bool minus = lo.frac < 0 && up.frac < 0;
+    evx[0].frac = dflip_i(evx[0].frac, sx);
+    evx[1].frac = dflip_i(evx[1].frac, sx);
+    evy[0].frac = dflip_i(evy[0].frac, sy);
+    evy[1].frac = dflip_i(evy[1].frac, sy);
+    lo = er_add_dir_i<false>(evx[sx], evy[sy]);
+    up = er_add_dir_i<true>(evx[1 - sx], evy[1 - sy]);
+    const bool minus = dneg_i(lo.frac) && dneg_i(up.frac);
     if (minus) {
         const Er t = lo;
-        lo = Er{-up.frac, up.exp};
-        up = Er{-t.frac, t.exp};
+        lo = Er{dflip_i(up.frac, true), up.exp};
+        up = Er{dflip_i(t.frac, true), t.exp};
     }
     return minus;
 }
@@ -120,7 +120,7 @@ __device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, 
     res.sign = minus;
     res.eval[0] = lo;
     res.eval[1] = up;
-    flags |= overflow_flags<N>(C, lo, up);
+    flags |= overflow_flags_i<N>(C, lo, up);
 }
 
 template <int N>
@@ -138,7 +138,7 @@ __device__ __forceinline__ void mpint_mul(const Consts<N> &C, MpInt<N> &res, con
         zero &= v == 0;
     }
     res.sign = zero ? 0 : (x.sign ^ y.sign);
-    flags |= overflow_flags<N>(C, res.eval[0], res.eval[1]);
+    flags |= overflow_flags_i<N>(C, res.eval[0], res.eval[1]);
 }
 
 }  // namespace grns

@@ -258,6 +258,30 @@ def test_mpint(case, op):
     assert [(-v if s else v) for v, s in zip(mags, got["sign"])] == [exact(p, q) for p, q in zip(vals_a, vals_b)]
 
 
+@pytest.mark.parametrize("op", ["add", "sub", "mul"])
+def test_mpint_extreme_magnitudes(case, op):
+    """operands of very different sizes (at n = 64 the exponent gaps exceed
+    1022, so the shifted bound of the interval addition is subnormal or
+    zero), zeros, +-1, powers of two and exact cancellations: the oracle's
+    digits, signs and evaluations bit for bit"""
+    tag, ctx, orc, g = case
+    top = orc.log2M // 2 - 2 if op == "mul" else orc.log2M - 2
+    rng = random.Random(23)
+    vals = [0, 1, -1, 2, -3] + [rng.choice((1, -1)) << j for j in range(0, top, max(1, top // 25))]
+    vals += [rng.choice((1, -1)) * rng.randrange(1 << top) for _ in range(60)]
+    a = [rng.choice(vals) for _ in range(800)]
+    b = [rng.choice(vals) for _ in range(800)]
+    b[:60] = [-v for v in a[:60]]       # x + y = 0 exactly
+    b[60:120] = list(a[60:120])         # x - y = 0 exactly
+    ma, mb = orc.mpint_from_ints(a), orc.mpint_from_ints(b)
+    fn = getattr(ctx, f"mpint_{op}")
+    got = fn(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda()).cpu().numpy()
+    got = got.view(mpint_dtype(orc.n))
+    want, _ = orc.mpint(op, ma, mb, path=O.PATH_DEVICE)
+    for f in ("digits", "sign", "eval"):
+        assert got[f].tobytes() == want[f].tobytes(), f
+
+
 def _signed(orc, m):
     return [(-v if s else v) for v, s in zip(orc.exact.from_rns(m["digits"]), m["sign"])]
 
