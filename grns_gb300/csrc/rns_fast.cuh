@@ -296,6 +296,55 @@ GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &ba
     return kEvalOk;
 }
 
+/* ---------------- directed-rounding product and quotient on the integer pipe ----------------
+ * out = (a * b) / c with both operations rounded down (up = false) or up,
+ * as __ddiv_rd(__dmul_rd(a, b), c) / __ddiv_ru(__dmul_ru(a, b), c): the
+ * 53-bit mantissas multiplied exactly (106 bits) and rounded, then an exact
+ * 128 / 64-bit division rounded.  Returns false -- the caller then uses the
+ * FP64 instructions -- unless a and b are normal or zero, c is normal, and
+ * both results are normal or zero. */
+GRNS_HD bool dmuldiv_dir_i(double a, double b, double c, bool up, double &out) {
+    const uint64_t ua = dbits(a), ub = dbits(b), uc = dbits(c);
+    const int ea = (int)((ua >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff), ec = (int)((uc >> 52) & 0x7ff);
+    const uint64_t fm = (((uint64_t)1) << 52) - 1;
+    const bool za = !(ua << 1), zb = !(ub << 1);
+    if ((ea == 0 && !za) || (eb == 0 && !zb) || ea == 0x7ff || eb == 0x7ff || ec == 0 || ec == 0x7ff) return false;
+    const uint64_t sp = (ua ^ ub) >> 63, sq = sp ^ (uc >> 63);  // signs of the product and the quotient
+    if (za || zb) {  // (+-0) / c
+        out = bitsd(sq << 63);
+        return true;
+    }
+    /* the product, rounded to 53 bits toward -inf (down) or +inf (up) */
+    const u128 P = (u128)((ua & fm) | (fm + 1)) * (u128)((ub & fm) | (fm + 1));
+    int sh = bitlen128(P) - 53;  // 52 or 53
+    uint64_t pm = (uint64_t)(P >> sh);
+    if ((P & ((((u128)1) << sh) - 1)) != 0 && (up != (sp != 0))) {  // inexact, magnitude rounded away from 0
+        if (++pm == (((uint64_t)1) << 53)) {
+            pm >>= 1;
+            sh++;
+        }
+    }
+    const int ep = ea + eb - 1023 + (sh - 52);  // biased exponent of the rounded product
+    if (ep < 1 || ep > 2046) return false;
+    /* the quotient pm 2^64 / mc, rounded the same way */
+    const uint64_t mc = (uc & fm) | (fm + 1);
+    const u128 N = ((u128)pm) << 64;
+    const u128 Q = N / mc;
+    const bool rem = (N - Q * mc) != 0;
+    const int qs = bitlen128(Q) - 53;  // 11 or 12
+    uint64_t qm = (uint64_t)(Q >> qs);
+    if ((rem || (Q & ((((u128)1) << qs) - 1)) != 0) && (up != (sq != 0))) {
+        if (++qm == (((uint64_t)1) << 53)) {
+            qm >>= 1;
+            return false;  // a carry into the next binade: left to the FP64 form
+        }
+    }
+    const int eq = ep - ec + qs + 1011;  // biased exponent of the quotient: qm 2^(qs - 64) 2^(ep - ec)
+    if (eq < 1 || eq > 2046) return false;
+    out = bitsd((sq << 63) | ((uint64_t)eq << 52) | (qm & fm));
+    return true;
+}
+
 /* ---------------- one-ulp interval evaluation ----------------
  *
  * T = sum_i x_i ceil(2^128 w_i / m_i) mod 2^128 exceeds 2^128 frac(X/M) by

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "rns_device.cuh"
+#include "rns_fast.cuh"
 
 namespace grns {
 
@@ -65,6 +66,21 @@ __device__ __forceinline__ void mpint_div_finish(const Consts<N> &C, int xs, int
     eval<N>(C, [&](int i) { return res.digits[i]; }, res.eval[0], res.eval[1], f);
     res.sign = qz ? 0 : (xs ^ ys);
     res.pad = 0;
+}
+
+/* er_md_rd / er_md_ru (src/extrange.cuh:557/:566) with the product and the
+ * quotient on the integer pipe (dmuldiv_dir_i), the FP64 instructions where
+ * it defers; the same bits as er_md */
+template <bool UP>
+__device__ __forceinline__ Er er_md_i(const Er &x, const Er &y, const Er &z) {
+    Er r;
+    r.exp = x.exp + y.exp - z.exp;
+    double q;
+    if (!dmuldiv_dir_i(x.frac, y.frac, z.frac, UP, q))
+        q = UP ? __ddiv_ru(__dmul_ru(x.frac, y.frac), z.frac) : __ddiv_rd(__dmul_rd(x.frac, y.frac), z.frac);
+    r.frac = q;
+    er_adjust_i(r);
+    return r;
 }
 
 /* the sign and evaluation of an mp_int (the part of the record besides the digits) */
@@ -126,8 +142,8 @@ __device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, 
 template <int N>
 __device__ __forceinline__ void mpint_mul(const Consts<N> &C, MpInt<N> &res, const MpInt<N> &x, const MpInt<N> &y,
                                           uint32_t &flags) {
-    res.eval[0] = er_md<false>(x.eval[0], y.eval[0], C.unit_upp);
-    res.eval[1] = er_md<true>(x.eval[1], y.eval[1], C.unit_low);
+    res.eval[0] = er_md_i<false>(x.eval[0], y.eval[0], C.unit_upp);
+    res.eval[1] = er_md_i<true>(x.eval[1], y.eval[1], C.unit_low);
     bool zero = true;
 #pragma unroll
     for (int i = 0; i < N; i++) {

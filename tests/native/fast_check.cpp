@@ -143,6 +143,16 @@ int fc_to_binary(void *p, const uint32_t *x, long cnt, uint32_t *out, int32_t *o
     return 0;
 }
 
+/* (a b) / c with directed rounding on the integer pipe; ok[k] = 0 where it defers to FP64 */
+int fc_dmuldiv(const double *a, const double *b, const double *c, long cnt, int up, double *out, int32_t *ok) {
+    for (long k = 0; k < cnt; k++) {
+        double r = 0;
+        ok[k] = dmuldiv_dir_i(a[k], b[k], c[k], up != 0, r) ? 1 : 0;
+        out[k] = r;
+    }
+    return 0;
+}
+
 int fc_binary_limbs(void *p) { return ((Box *)p)->T.bin_limbs; }
 
 uint64_t fc_E(void *p) { return ((Box *)p)->T.E; }

@@ -32,7 +32,7 @@ def fc(tmp_path_factory):
     L.fc_binary_limbs.argtypes = [ctypes.c_void_p]
     L.fc_table.restype = ctypes.c_long
     L.fc_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_long]
-    for f in ("fc_cmp", "fc_div", "fc_div_rows", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary",
+    for f in ("fc_cmp", "fc_div", "fc_div_rows", "fc_dmuldiv", "fc_scale", "fc_fx", "fc_eval", "fc_eval_tight", "fc_from_binary", "fc_to_binary",
               "fc_eval_fast"):
         getattr(L, f).argtypes = None
     return L
@@ -466,3 +466,30 @@ def test_differential_fuzz(fc):
         rounds += 1
     for f in ctxs.values():
         fc.fc_destroy(f.h)
+
+
+def test_directed_product_quotient_on_the_integer_pipe(fc):
+    """(a b) / c rounded down and up on the integer pipe (the mp_int product's
+    interval bound) equals the oracle's IEEE directed-rounding product then
+    quotient, wherever it does not defer to the FP64 instructions"""
+    from oracle import oracle as O
+    L = O.lib()
+    rng = np.random.default_rng(8)
+    n = 20000
+    a = rng.uniform(1.0, 2.0, n) * rng.choice([1.0, -1.0], n)
+    b = rng.uniform(1.0, 2.0, n) * rng.choice([1.0, -1.0], n)
+    c = rng.uniform(0.5, 1.0, n)
+    a[:8] = [0.0, -0.0, 1.0, 1.0, 2 - 2 ** -52, 1.5, 1.0, 1.25]
+    b[:8] = [1.5, 1.5, 0.0, 1.0, 2 - 2 ** -52, 1.0 + 2 ** -52, 1.0, 1.75]
+    c[:8] = [0.75, 0.75, 0.5, 1.0, 0.5 + 2 ** -53, 1 - 2 ** -53, 0.5, 0.875]
+    c[8:40] = 0.5 + np.arange(32) * 2.0 ** -53  # divisors with exact and near-exact quotients
+    for up in (0, 1):
+        out = np.zeros(n)
+        ok = np.zeros(n, np.int32)
+        fc.fc_dmuldiv(ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(b.ctypes.data), ctypes.c_void_p(c.ctypes.data),
+                      ctypes.c_long(n), up, ctypes.c_void_p(out.ctypes.data), ctypes.c_void_p(ok.ctypes.data))
+        assert ok.mean() > 0.99
+        mul, div = (3, 5) if up else (2, 4)
+        want = np.array([L.oracle_d_op(div, L.oracle_d_op(mul, x, y), z) for x, y, z in zip(a, b, c)])
+        sel = ok.astype(bool)
+        assert np.array_equal(out[sel].view(np.uint64), want[sel].view(np.uint64))
