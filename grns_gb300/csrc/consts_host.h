@@ -458,6 +458,8 @@ inline void fill_consts(Consts<N> &C, const HostTables &T, const uint32_t *blob)
     C.unit_upp = T.unit_upp;
     C.inv_unit_low = T.inv_unit_low;
     C.inv_unit_upp = T.inv_unit_upp;
+    C.unit_rcp_low = (uint64_t)((((unsigned __int128)1) << 116) / ((dbits(T.unit_low.frac) & ((1ull << 52) - 1)) | (1ull << 52)));
+    C.unit_rcp_upp = (uint64_t)((((unsigned __int128)1) << 116) / ((dbits(T.unit_upp.frac) & ((1ull << 52) - 1)) | (1ull << 52)));
     C.m_pow2_res30 = T.m_pow2[29];
     C.E = T.E;
     C.c96k = reinterpret_cast<const uint4 *>(blob);

@@ -107,8 +107,8 @@ __device__ __forceinline__ void mp_chunk(const Consts<N> &C, const uint4 *K, int
     Er lo{0, 0}, up{0, 0};
     if (act && p == 0) {  // the record's interval, once
         if (op == 2) {
-            lo = er_md_i<false>(a.eval[0], b.eval[0], C.unit_upp);
-            up = er_md_i<true>(a.eval[1], b.eval[1], C.unit_low);
+            lo = er_md_i<false>(a.eval[0], b.eval[0], C.unit_upp, C.unit_rcp_upp);
+            up = er_md_i<true>(a.eval[1], b.eval[1], C.unit_low, C.unit_rcp_low);
         } else {
             minus = mpint_addsub_eval(head_of(a), head_of(b), op == 1, lo, up);
         }

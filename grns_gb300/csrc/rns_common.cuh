@@ -65,6 +65,7 @@ struct Consts {
     int ref_factor;       // RNS_EVAL_REF_FACTOR
     int log2M;            // floor(log2 M), the RNS_MODULI_PRODUCT_LOG2 convention
     Er unit_low, unit_upp, inv_unit_low, inv_unit_upp;  // RNS_EVAL_UNIT, RNS_EVAL_INV_UNIT
+    uint64_t unit_rcp_low, unit_rcp_upp;  // floor(2^116 / mantissa) of unit_low.frac, unit_upp.frac
     uint32_t m_pow2_res30;                // M mod 2^30
     /* integer fast path: fixed-point reciprocals.  "w-folded" constants give
      * frac(x_i w_i / m_i) directly from the residue x_i (frac(x w / m) = s / m). */

@@ -303,7 +303,14 @@ GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &ba
  * 128 / 64-bit division rounded.  Returns false -- the caller then uses the
  * FP64 instructions -- unless a and b are normal or zero, c is normal, and
  * both results are normal or zero. */
-GRNS_HD bool dmuldiv_dir_i(double a, double b, double c, bool up, double &out) {
+/* floor(2^116 / mc) for the 53-bit mantissa mc of a normal c: the quotient
+ * below then needs one multiplication and at most two corrections */
+GRNS_HD uint64_t dmuldiv_recip(double c) {
+    const uint64_t mc = (dbits(c) & ((((uint64_t)1) << 52) - 1)) | (((uint64_t)1) << 52);
+    return (uint64_t)((((u128)1) << 116) / mc);
+}
+
+GRNS_HD bool dmuldiv_dir_i(double a, double b, double c, bool up, double &out, uint64_t rcp = 0) {
     const uint64_t ua = dbits(a), ub = dbits(b), uc = dbits(c);
     const int ea = (int)((ua >> 52) & 0x7ff), eb = (int)((ub >> 52) & 0x7ff), ec = (int)((uc >> 52) & 0x7ff);
     const uint64_t fm = (((uint64_t)1) << 52) - 1;
@@ -329,7 +336,17 @@ GRNS_HD bool dmuldiv_dir_i(double a, double b, double c, bool up, double &out) {
     /* the quotient pm 2^64 / mc, rounded the same way */
     const uint64_t mc = (uc & fm) | (fm + 1);
     const u128 N = ((u128)pm) << 64;
-    const u128 Q = N / mc;
+    u128 Q;
+    if (rcp) {  // rcp = floor(2^116 / mc): Q <= floor(N / mc), short by at most 2
+        Q = ((u128)pm * rcp) >> 52;
+        u128 R = N - Q * mc;
+        while (R >= mc) {
+            R -= mc;
+            Q++;
+        }
+    } else {
+        Q = N / mc;
+    }
     const bool rem = (N - Q * mc) != 0;
     const int qs = bitlen128(Q) - 53;  // 11 or 12
     uint64_t qm = (uint64_t)(Q >> qs);

@@ -69,14 +69,14 @@ __device__ __forceinline__ void mpint_div_finish(const Consts<N> &C, int xs, int
 }
 
 /* er_md_rd / er_md_ru (src/extrange.cuh:557/:566) with the product and the
- * quotient on the integer pipe (dmuldiv_dir_i), the FP64 instructions where
- * it defers; the same bits as er_md */
+ * quotient on the integer pipe (dmuldiv_dir_i; z_rcp = dmuldiv_recip(z.frac)),
+ * the FP64 instructions where it defers; the same bits as er_md */
 template <bool UP>
-__device__ __forceinline__ Er er_md_i(const Er &x, const Er &y, const Er &z) {
+__device__ __forceinline__ Er er_md_i(const Er &x, const Er &y, const Er &z, uint64_t z_rcp) {
     Er r;
     r.exp = x.exp + y.exp - z.exp;
     double q;
-    if (!dmuldiv_dir_i(x.frac, y.frac, z.frac, UP, q))
+    if (!dmuldiv_dir_i(x.frac, y.frac, z.frac, UP, q, z_rcp))
         q = UP ? __ddiv_ru(__dmul_ru(x.frac, y.frac), z.frac) : __ddiv_rd(__dmul_rd(x.frac, y.frac), z.frac);
     r.frac = q;
     er_adjust_i(r);
@@ -142,8 +142,8 @@ __device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, 
 template <int N>
 __device__ __forceinline__ void mpint_mul(const Consts<N> &C, MpInt<N> &res, const MpInt<N> &x, const MpInt<N> &y,
                                           uint32_t &flags) {
-    res.eval[0] = er_md_i<false>(x.eval[0], y.eval[0], C.unit_upp);
-    res.eval[1] = er_md_i<true>(x.eval[1], y.eval[1], C.unit_low);
+    res.eval[0] = er_md_i<false>(x.eval[0], y.eval[0], C.unit_upp, C.unit_rcp_upp);
+    res.eval[1] = er_md_i<true>(x.eval[1], y.eval[1], C.unit_low, C.unit_rcp_low);
     bool zero = true;
 #pragma unroll
     for (int i = 0; i < N; i++) {

@@ -148,6 +148,10 @@ int fc_dmuldiv(const double *a, const double *b, const double *c, long cnt, int 
     for (long k = 0; k < cnt; k++) {
         double r = 0;
         ok[k] = dmuldiv_dir_i(a[k], b[k], c[k], up != 0, r) ? 1 : 0;
+        double r2 = 0;  /* with the precomputed reciprocal: the same answer */
+        if (dmuldiv_dir_i(a[k], b[k], c[k], up != 0, r2, dmuldiv_recip(c[k])) != (ok[k] != 0) ||
+            dbits(r2) != dbits(r))
+            ok[k] = -1;
         out[k] = r;
     }
     return 0;

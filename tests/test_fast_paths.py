@@ -488,6 +488,7 @@ def test_directed_product_quotient_on_the_integer_pipe(fc):
         ok = np.zeros(n, np.int32)
         fc.fc_dmuldiv(ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(b.ctypes.data), ctypes.c_void_p(c.ctypes.data),
                       ctypes.c_long(n), up, ctypes.c_void_p(out.ctypes.data), ctypes.c_void_p(ok.ctypes.data))
+        assert not (ok < 0).any()  # the reciprocal form agrees with the division form
         assert ok.mean() > 0.99
         mul, div = (3, 5) if up else (2, 4)
         want = np.array([L.oracle_d_op(div, L.oracle_d_op(mul, x, y), z) for x, y, z in zip(a, b, c)])
