@@ -1,7 +1,9 @@
 """Build libgrns_gb300.so in-tree with nvcc for sm_103a.
 
 Each translation unit compiles in parallel to an object file under
-grns_gb300/_build/, then nvcc links the shared library.  Nothing is
+grns_gb300/_build/, then nvcc links the shared library.  A source that names
+GRNS_SPLIT_BY_N in its header comment compiles as GRNS_N_PARTS units, one per
+group of moduli counts (-DGRNS_PART=k; the groups are in csrc/internal.h).  Nothing is
 installed; the library is loaded from grns_gb300/_build/ by grns_gb300.native.
 """
 import os
@@ -38,8 +40,28 @@ def headers():
     return hs
 
 
-def _compile(src, extra):
-    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+N_PARTS = 4  # GRNS_N_PARTS in csrc/internal.h
+
+
+def units():
+    """(source, part) for every translation unit; part None = the whole file"""
+    out = []
+    for src in sources():
+        with open(src) as f:
+            head = f.read(2048)
+        if "GRNS_SPLIT_BY_N" in head:
+            out += [(src, k) for k in range(N_PARTS)]
+        else:
+            out.append((src, None))
+    # the longest units first, so that they do not start last
+    return sorted(out, key=lambda u: -os.path.getsize(u[0]))
+
+
+def _compile(unit, extra):
+    src, part = unit
+    tag = "" if part is None else f".p{part}"
+    obj = os.path.join(OUT, os.path.basename(src) + tag + ".o")
+    extra = list(extra) + ([] if part is None else [f"-DGRNS_PART={part}"])
     newest = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in headers()])
     if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
         return obj
@@ -53,9 +75,9 @@ def _compile(src, extra):
 
 def build(verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
-    srcs = sources()
-    with ThreadPoolExecutor(max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
+    us = units()
+    with ThreadPoolExecutor(max(1, min(len(us), os.cpu_count() or 4))) as ex:
+        objs = list(ex.map(lambda u: _compile(u, list(extra)), us))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -16,6 +16,8 @@
  * (one thread per number) or "coop" (n-threaded: the n residues of a number
  * spread over the lanes of a lane group, reduced by shuffles; cmp and max
  * only), and the chunk length.
+ *
+ * GRNS_SPLIT_BY_N: compiled as one unit per group of moduli counts.
  */
 #include <algorithm>
 #include <cstdio>
@@ -340,7 +342,7 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
             MpInt<N> *po = (MpInt<N> *)J.out0;
             for (int64_t k = start + lane; k < end; k += 32) {
                 MpInt<N> a = px[k], b = py[k], r;
-                r.pad = 0;
+                clear_pad(r);
                 uint32_t f = 0;
                 if (J.op == GRNS_OP_MPINT_MUL) mpint_mul<N>(C, r, a, b, f);
                 else mpint_addsub<N>(C, r, a, b, J.op == GRNS_OP_MPINT_SUB, f);
@@ -402,6 +404,38 @@ struct grns_batch {
     cudaStream_t graph_stream = nullptr;
 };
 
+namespace grns {
+
+template <int N>
+grns_status launch_batch_kernel(grns_batch *b, cudaStream_t s) {
+    k_batch<N><<<b->grid, BatchCfg<N>::kBlock, b->smem, s>>>(consts_of<N>(b->ctx), b->d_jobs, b->njobs, b->total_chunks,
+                                              b->d_counter, b->d_done, b->d_parts, b->smem ? 1 : 0);
+    return cuda_status(cudaGetLastError());
+}
+
+template <int N>
+int occupancy_blocks(size_t smem) {
+    if (BatchCfg<N>::kHeavySmem > 48 * 1024)  // per device: set on every shape computation
+        cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BatchCfg<N>::kHeavySmem);
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, BatchCfg<N>::kBlock, smem);
+    return nb > 0 ? nb : 1;
+}
+
+/* the per-count entry points: extern here, instantiated for this unit's counts */
+#define GRNS_BATCH_ROOTS_(n, EXT)                                                   \
+    EXT template grns_status launch_batch_kernel<n>(grns_batch *, cudaStream_t);    \
+    EXT template int occupancy_blocks<n>(size_t);
+#define GRNS_EXTERN_(n) GRNS_BATCH_ROOTS_(n, extern)
+#define GRNS_DEFINE_(n) GRNS_BATCH_ROOTS_(n, )
+GRNS_FOR_EACH_N(GRNS_EXTERN_)
+GRNS_PART_N(GRNS_DEFINE_)
+#undef GRNS_EXTERN_
+#undef GRNS_DEFINE_
+
+}  // namespace grns
+
+#if GRNS_PART_MAIN
 namespace {
 
 double op_cost(int op, int n) {
@@ -445,13 +479,6 @@ bool job_ok(const grns_ctx *c, const grns_job &jb) {
     }
 }
 
-template <int N>
-grns_status launch_batch_kernel(grns_batch *b, cudaStream_t s) {
-    k_batch<N><<<b->grid, BatchCfg<N>::kBlock, b->smem, s>>>(consts_of<N>(b->ctx), b->d_jobs, b->njobs, b->total_chunks,
-                                              b->d_counter, b->d_done, b->d_parts, b->smem ? 1 : 0);
-    return cuda_status(cudaGetLastError());
-}
-
 grns_status enqueue(grns_batch *b, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(b->d_counter, 0, b->counters_bytes, s);
     if (e != cudaSuccess) return cuda_status(e);
@@ -465,15 +492,6 @@ grns_status enqueue(grns_batch *b, cudaStream_t s) {
 #undef C_
 }
 
-template <int N>
-int occupancy_blocks(size_t smem) {
-    if (BatchCfg<N>::kHeavySmem > 48 * 1024)  // per device: set on every shape computation
-        cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BatchCfg<N>::kHeavySmem);
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, BatchCfg<N>::kBlock, smem);
-    return nb > 0 ? nb : 1;
-}
-
 /* launch shape of a batch: grid (SMs x resident blocks) and shared memory */
 void batch_shape(grns_batch *b) {
     bool has_div = false;
@@ -484,15 +502,7 @@ void batch_shape(grns_batch *b) {
     b->smem = has_div ? BatchCfg<n>::kHeavySmem : 0;           \
     per_sm = occupancy_blocks<n>(b->smem);                     \
     break
-    switch (b->ctx->n) {
-        case 4: C_(4);
-        case 8: C_(8);
-        case 12: C_(12);
-        case 16: C_(16);
-        case 32: C_(32);
-        case 64: C_(64);
-        default: break;
-    }
+    GRNS_SWITCH_N(b->ctx->n, break)
 #undef C_
     b->grid = b->ctx->sm_count * per_sm;
 }
@@ -729,3 +739,4 @@ int64_t grns_batch_chunks(const grns_batch *b) { return b ? b->total_chunks : -1
 int grns_batch_grid(const grns_batch *b) { return b ? b->grid : -1; }
 
 }  // extern "C"
+#endif  // GRNS_PART_MAIN

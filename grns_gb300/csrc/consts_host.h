@@ -45,8 +45,8 @@ struct HostTables {
     std::vector<uint64_t> mi64;                  // M_i mod 2^64
     uint64_t m64 = 0;                            // M mod 2^64
     uint64_t E = 0;  // sum_i (m_i - 1)
-    std::vector<uint32_t> bin_p26;               // kBinMaxChunks x n: 2^(26 c) mod m_i
-    std::vector<uint32_t> bin_mi26;              // bin_chunks x n: 26-bit chunks of M_i
+    std::vector<uint32_t> bin_p26;               // kBinMaxChunks x bin_ld(n): 2^(26 c) mod m_i
+    std::vector<uint32_t> bin_mi26;              // bin_chunks x bin_ld(n): 26-bit chunks of M_i
     std::vector<uint32_t> bin_m26;               // bin_chunks, padded to a multiple of 4: chunks of M
     int bin_chunks = 0, bin_limbs = 0;
 };
@@ -326,7 +326,8 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
         T.bin_chunks = (bitlen + kBinChunk - 1) / kBinChunk;
         T.bin_m26.assign((size_t)((T.bin_chunks + 3) / 4) * 4, 0);
         chunks26(M, T.bin_chunks, T.bin_m26.data(), 1);
-        T.bin_mi26.assign((size_t)T.bin_chunks * n, 0);
+        const int ld = bin_ld(n);
+        T.bin_mi26.assign((size_t)T.bin_chunks * ld, 0);
         for (int i = 0; i < n; i++) {
             std::vector<uint32_t> q(M.size(), 0);  // M / m_i by long division
             uint64_t r = 0;
@@ -335,14 +336,14 @@ inline void build_tables(HostTables &T, const uint32_t *mod, int n) {
                 q[j] = (uint32_t)(v / m[i]);
                 r = v % m[i];
             }
-            chunks26(q, T.bin_chunks, &T.bin_mi26[i], (size_t)n);
+            chunks26(q, T.bin_chunks, &T.bin_mi26[i], (size_t)ld);
         }
-        T.bin_p26.assign((size_t)kBinMaxChunks * n, 0);
+        T.bin_p26.assign((size_t)kBinMaxChunks * ld, 0);
         for (int i = 0; i < n; i++) {
             const uint64_t step = (((uint64_t)1) << kBinChunk) % m[i];
             uint64_t v = 1 % m[i];
             for (int c = 0; c < kBinMaxChunks; c++) {
-                T.bin_p26[(size_t)c * n + i] = (uint32_t)v;
+                T.bin_p26[(size_t)c * ld + i] = (uint32_t)v;
                 v = (v * step) % m[i];
             }
         }

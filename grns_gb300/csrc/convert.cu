@@ -32,9 +32,10 @@ __global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constan
     extern __shared__ uint4 conv_smem[];
     const int chunks = (32 * nlimbs + kBinChunk - 1) / kBinChunk;
     const int rs = odd_at_least(nlimbs + 1);  // row stride: limbs, one zero word, odd
-    uint4 *T4 = conv_smem;                    // [chunks][N / 4]
-    uint32_t *rows = reinterpret_cast<uint32_t *>(T4 + chunks * (N / 4));
-    for (int w = threadIdx.x; w < chunks * (N / 4); w += blockDim.x)
+    constexpr int L4 = bin_ld(N) / 4;         // 16-byte words per table row
+    uint4 *T4 = conv_smem;                    // [chunks][L4]
+    uint32_t *rows = reinterpret_cast<uint32_t *>(T4 + chunks * L4);
+    for (int w = threadIdx.x; w < chunks * L4; w += blockDim.x)
         T4[w] = reinterpret_cast<const uint4 *>(C.bin_p26)[w];
     uint32_t *row = rows + threadIdx.x * rs;
     for (int j = nlimbs; j < rs; j++) row[j] = 0;
@@ -62,7 +63,7 @@ __global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constan
             for (int c = 0; c < chunks; c++) {
                 const int bit = kBinChunk * c, j = bit >> 5;
                 const uint32_t ch = __funnelshift_r(row[j], row[j + 1], bit & 31) & kBinMask;
-                const uint4 *t = T4 + c * (N / 4) + g / 4;
+                const uint4 *t = T4 + c * L4 + g / 4;
 #pragma unroll
                 for (int u = 0; u < G; u += 4) {
                     const uint4 v = t[u / 4];
@@ -73,14 +74,16 @@ __global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constan
                 }
             }
 #pragma unroll
-            for (int u = 0; u < G; u++) out[k * ks + (int64_t)(g + u) * is] = bin_mod64<N>(C, g + u, acc[u]);
+            for (int u = 0; u < G; u++)
+                if (N % G == 0 || g + u < N) out[k * ks + (int64_t)(g + u) * is] = bin_mod64<N>(C, g + u, acc[u]);
         }
     }
 }
 
 template <int N>
 constexpr size_t from_binary_smem(int nlimbs) {
-    return (size_t)((32 * nlimbs + kBinChunk - 1) / kBinChunk) * N * 4 + (size_t)kConvBlock * odd_at_least(nlimbs + 1) * 4;
+    return (size_t)((32 * nlimbs + kBinChunk - 1) / kBinChunk) * bin_ld(N) * 4 +
+           (size_t)kConvBlock * odd_at_least(nlimbs + 1) * 4;
 }
 
 /* ---------------- RNS -> binary ---------------- */
@@ -100,10 +103,11 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
     const int chunks = C.bin_chunks;
     const int m4 = (chunks + 3) / 4;
     const int rs = odd_at_least(chunks);
-    uint4 *Mi4 = conv_smem;                 // [chunks][N / 4]
-    uint32_t *M26 = reinterpret_cast<uint32_t *>(Mi4 + chunks * (N / 4));  // [m4 * 4]
+    constexpr int L = bin_ld(N);            // table row: N words and zeros up to a multiple of 4
+    uint4 *Mi4 = conv_smem;                 // [chunks][L / 4]
+    uint32_t *M26 = reinterpret_cast<uint32_t *>(Mi4 + chunks * (L / 4));  // [m4 * 4]
     uint32_t *rows = M26 + m4 * 4;
-    for (int w = threadIdx.x; w < chunks * (N / 4); w += blockDim.x)
+    for (int w = threadIdx.x; w < chunks * (L / 4); w += blockDim.x)
         Mi4[w] = reinterpret_cast<const uint4 *>(C.bin_mi26)[w];
     for (int w = threadIdx.x; w < m4 * 4; w += blockDim.x) M26[w] = C.bin_m26[w];
     uint32_t *row = rows + threadIdx.x * rs;
@@ -112,8 +116,10 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
         __syncthreads();
         if ((int)threadIdx.x < tile) {
             const int64_t k = k0 + threadIdx.x;
-            uint32_t s[N];
+            uint32_t s[L];
             uint32_t bad = 0, any = 0;
+#pragma unroll
+            for (int i = N; i < L; i++) s[i] = 0;
 #pragma unroll
             for (int i = 0; i < N; i++) {
                 const uint32_t v = __ldg(x + k * ks + (int64_t)i * is);
@@ -127,10 +133,10 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
                 const uint32_t kk = bin_rank<N>(C, s);
                 int64_t carry = 0;
                 for (int c = 0; c < chunks; c++) {
-                    const uint4 *t = Mi4 + c * (N / 4);
+                    const uint4 *t = Mi4 + c * (L / 4);
                     uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
-                    for (int i = 0; i < N; i += 4) {
+                    for (int i = 0; i < L; i += 4) {
                         const uint4 v = t[i / 4];
                         a0 += (uint64_t)s[i] * v.x;
                         a1 += (uint64_t)s[i + 1] * v.y;
@@ -165,7 +171,7 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
 
 template <int N>
 size_t to_binary_smem(const Consts<N> &C) {
-    return (size_t)C.bin_chunks * N * 4 + (size_t)((C.bin_chunks + 3) / 4) * 16 +
+    return (size_t)C.bin_chunks * bin_ld(N) * 4 + (size_t)((C.bin_chunks + 3) / 4) * 16 +
            (size_t)kConvBlock * odd_at_least(C.bin_chunks) * 4;
 }
 
@@ -185,7 +191,7 @@ __global__ void __launch_bounds__(128) k_mpint_pack(const __grid_constant__ Cons
         for (int i = 0; i < N; i++) r.digits[i] = __ldg(res + (int64_t)i * count + k);
         eval<N>(C, [&](int i) { return r.digits[i]; }, r.eval[0], r.eval[1], f);
         r.sign = (signs && __ldg(signs + k) != 0 && nonzero[k]) ? 1 : 0;
-        r.pad = 0;
+        clear_pad(r);
         out[k] = r;
     }
 }

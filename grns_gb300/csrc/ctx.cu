@@ -39,16 +39,11 @@ grns_status build(grns_ctx *c, const uint32_t *moduli) {
     e = cudaMemcpy(c->d_tables, blob.data(), blob.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return grns::cuda_status(e);
     const uint32_t *d = (const uint32_t *)c->d_tables;
-    switch (c->n) {
-        case 4: grns::fill_consts<4>(*reinterpret_cast<grns::Consts<4> *>(c->consts), c->T, d); break;
-        case 8: grns::fill_consts<8>(*reinterpret_cast<grns::Consts<8> *>(c->consts), c->T, d); break;
-        case 12: grns::fill_consts<12>(*reinterpret_cast<grns::Consts<12> *>(c->consts), c->T, d); break;
-        case 16: grns::fill_consts<16>(*reinterpret_cast<grns::Consts<16> *>(c->consts), c->T, d); break;
-        case 32: grns::fill_consts<32>(*reinterpret_cast<grns::Consts<32> *>(c->consts), c->T, d); break;
-        case 64: grns::fill_consts<64>(*reinterpret_cast<grns::Consts<64> *>(c->consts), c->T, d); break;
-        default: return GRNS_ERR_UNSUPPORTED;
-    }
-    return GRNS_OK;
+#define C_(n)                                                                        \
+    grns::fill_consts<n>(*reinterpret_cast<grns::Consts<n> *>(c->consts), c->T, d); \
+    return GRNS_OK
+    GRNS_DISPATCH_N(c->n, C_)
+#undef C_
 }
 
 /* ---- the reference's params.h format (src/params.h:11-39, src/params/...) ---- */
@@ -145,7 +140,7 @@ const char *grns_version(void) { return "grns_gb300 0.1 (sm_103a)"; }
 grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out) {
     if (!moduli || !out) return GRNS_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    if (!(n == 4 || n == 8 || n == 12 || n == 16 || n == 32 || n == 64)) return GRNS_ERR_UNSUPPORTED;
+    if (!grns::supported_n(n)) return GRNS_ERR_UNSUPPORTED;
     for (int i = 0; i < n; i++) {
         if (moduli[i] < 3 || moduli[i] > 1431655765 || (moduli[i] & 1) == 0) return GRNS_ERR_UNSUPPORTED;
         for (int j = 0; j < i; j++)

@@ -230,13 +230,18 @@ __device__ __forceinline__ void divnorm_range_f(const DivK *K, const Consts<N> &
                 uint32_t w[4], xv[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    w[j] = W[(i0 + j) * stride];
-                    xv[j] = X[(i0 + j) * stride];
+                    const int i = (N % 4 == 0 || i0 + j < N) ? i0 + j : N - 1;  // past N: the last residue again
+                    w[j] = W[i * stride];
+                    xv[j] = X[i * stride];
                 }
 #pragma unroll
-                for (int j = 0; j < 4; j++) w[j] = tox ? xv[j] : (more ? kmag(w[j], K[i0 + j]) : w[j]);
+                for (int j = 0; j < 4; j++) {
+                    const int i = (N % 4 == 0 || i0 + j < N) ? i0 + j : N - 1;
+                    w[j] = tox ? xv[j] : (more ? kmag(w[j], K[i]) : w[j]);
+                }
 #pragma unroll
-                for (int j = 0; j < 4; j++) W[(i0 + j) * stride] = w[j];
+                for (int j = 0; j < 4; j++)
+                    if (N % 4 == 0 || i0 + j < N) W[(i0 + j) * stride] = w[j];
             }
         }
     }
@@ -374,28 +379,33 @@ __device__ __forceinline__ void divloop_range(const DivK *K, const Consts<N> &C,
         const bool live = ph == Iter;
         const uint64_t qd = live ? dv_digit(st, U, C.E, st.f) : 0;
         Fx96 fx;
-        constexpr int G = N % kDivGroup == 0 ? kDivGroup : 4;  // every supported N is a multiple of 4
+        /* groups of G residues; N not a multiple of G: the slots past N repeat
+         * the last residue and neither store nor enter the evaluation */
+        constexpr int G = N % kDivGroup == 0 ? kDivGroup : 4;
+        constexpr bool ragged = N % G != 0;
 #pragma unroll 1
         for (int i0 = 0; i0 < N; i0 += G) {  // groups: loads, arithmetic, stores
             uint32_t rv[G], dv[G], qv[G];
 #pragma unroll
             for (int j = 0; j < G; j++) {
-                rv[j] = Rc[(i0 + j) * stride];
-                dv[j] = Dc[(i0 + j) * stride];
-                qv[j] = Qc[(i0 + j) * stride];
+                const int i = (!ragged || i0 + j < N) ? i0 + j : N - 1;
+                rv[j] = Rc[i * stride];
+                dv[j] = Dc[i * stride];
+                qv[j] = Qc[i * stride];
             }
 #pragma unroll
             for (int j = 0; j < G; j++) {
-                const DivK k = K[i0 + j];
+                const DivK k = K[(!ragged || i0 + j < N) ? i0 + j : N - 1];
                 const uint32_t m = k.a.x;
                 const uint32_t qi = kred53(qd, k);
                 const uint32_t rn = submod(kmag(rv[j], k), kmulmod(qi, dv[j], k), m);
                 rv[j] = live ? rn : rv[j];
                 qv[j] = addmod(kmag(qv[j], k), qi, m);
-                fx.add(rv[j], k);
+                if (!ragged || i0 + j < N) fx.add(rv[j], k);
             }
 #pragma unroll
             for (int j = 0; j < G; j++) {
+                if (ragged && i0 + j >= N) continue;
                 Rc[(i0 + j) * stride] = rv[j];
                 if (live) Qc[(i0 + j) * stride] = qv[j];
             }

@@ -96,7 +96,7 @@ __global__ void k_gen_mpint(const __grid_constant__ Consts<N> C, uint64_t key_ma
             }
         }
         v.sign = (any && (draw(key_sign, (uint64_t)k) & 1u)) ? 1 : 0;
-        v.pad = 0;
+        clear_pad(v);
         uint32_t f = 0;
         eval<N>(C, [&](int i) { return v.digits[i]; }, v.eval[0], v.eval[1], f);
         out[k] = v;

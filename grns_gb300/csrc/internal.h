@@ -139,13 +139,51 @@ grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *
 
 }  // namespace grns
 
-#define GRNS_DISPATCH_N(n, CALL) \
-    switch (n) {                 \
-        case 4: CALL(4);         \
-        case 8: CALL(8);         \
-        case 12: CALL(12);       \
-        case 16: CALL(16);       \
-        case 32: CALL(32);       \
-        case 64: CALL(64);       \
-        default: return GRNS_ERR_UNSUPPORTED; \
+/* A source that names GRNS_SPLIT_BY_N in its header comment is compiled as
+ * GRNS_N_PARTS units (-DGRNS_PART=0, 1, ...): unit k holds the explicit
+ * instantiations of the file's per-count templates for the counts
+ * GRNS_PART_N lists; unit 0 (GRNS_PART_MAIN) also holds the file's other
+ * code, whose dispatch sees the templates through extern declarations.
+ * Without GRNS_PART one unit holds everything.  The groups balance compile
+ * time (n = 32 and n = 64 cost about as much as n = 4..16 together). */
+#define GRNS_N_PARTS 4
+#define GRNS_N_PART0_(X) X(4) X(5) X(6) X(7) X(8) X(9) X(10)
+#define GRNS_N_PART1_(X) X(11) X(12) X(13) X(14) X(15) X(16)
+#define GRNS_N_PART2_(X) X(32)
+#define GRNS_N_PART3_(X) X(64)
+#if !defined(GRNS_PART)
+#define GRNS_PART_MAIN 1
+#define GRNS_PART_N(X) GRNS_FOR_EACH_N(X)
+#elif GRNS_PART == 0
+#define GRNS_PART_MAIN 1
+#define GRNS_PART_N(X) GRNS_N_PART0_(X)
+#elif GRNS_PART == 1
+#define GRNS_PART_MAIN 0
+#define GRNS_PART_N(X) GRNS_N_PART1_(X)
+#elif GRNS_PART == 2
+#define GRNS_PART_MAIN 0
+#define GRNS_PART_N(X) GRNS_N_PART2_(X)
+#elif GRNS_PART == 3
+#define GRNS_PART_MAIN 0
+#define GRNS_PART_N(X) GRNS_N_PART3_(X)
+#else
+#error "GRNS_PART out of range"
+#endif
+
+/* switch (n) over the supported counts; every case expands the caller's
+ * macro C_(n) (which returns; C_NAME names it for the reader), other
+ * counts return GRNS_ERR_UNSUPPORTED */
+#define GRNS_DISPATCH_CASE_(n) \
+    case n:                    \
+        C_(n);
+#define GRNS_DISPATCH_N(n, C_NAME)             \
+    switch (n) {                               \
+        GRNS_FOR_EACH_N(GRNS_DISPATCH_CASE_)   \
+        default: return GRNS_ERR_UNSUPPORTED;  \
+    }
+/* the same with the caller's statement for other counts */
+#define GRNS_SWITCH_N(n, DEFAULT)            \
+    switch (n) {                             \
+        GRNS_FOR_EACH_N(GRNS_DISPATCH_CASE_) \
+        default: DEFAULT;                    \
     }

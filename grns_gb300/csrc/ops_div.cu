@@ -9,6 +9,7 @@
  *                pass B over the rows longest first (numbers claimed from
  *                grid-wide counters), the rows to the caller's layout
  *   k_scale    : floor(X / 2^D)             (reference src/rnsscal.cuh:207)
+ * GRNS_SPLIT_BY_N: compiled as one unit per group of moduli counts.
  */
 #include <algorithm>
 
@@ -120,8 +121,8 @@ constexpr int kDivPlaceChunk = 2048;  // numbers per block step of the placement
 /* order: the numbers by decreasing step count over the whole call (a
  * counting sort: positions of step count b start after every number with
  * more steps; each block reserves its range per count with one atomic) */
-__global__ void __launch_bounds__(256) k_div_place(const uint8_t *__restrict__ steps, DivRowsG *__restrict__ G,
-                                                   int32_t *__restrict__ order, int64_t count) {
+static __global__ void __launch_bounds__(256) k_div_place(const uint8_t *__restrict__ steps, DivRowsG *__restrict__ G,
+                                                          int32_t *__restrict__ order, int64_t count) {
     __shared__ uint32_t loc[kDivRowBins], base[kDivRowBins], tot[kDivRowBins];
     for (int i = threadIdx.x; i < kDivRowBins; i += blockDim.x) tot[i] = G->hist[i];
     for (int64_t b0 = (int64_t)blockIdx.x * kDivPlaceChunk; b0 < count; b0 += (int64_t)gridDim.x * kDivPlaceChunk) {
@@ -250,8 +251,8 @@ __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N>
 }
 
 template <int N>
-static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
-                           uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp) {
+grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count, uint32_t *q,
+                    uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
         k_div<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
@@ -328,8 +329,8 @@ static grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t 
 }
 
 template <int N>
-static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
-                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp) {
+grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld, int64_t count,
+                      uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
         k_scale<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
@@ -360,7 +361,7 @@ static grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_
 }
 
 template <int N>
-static size_t div_scratch_of(int64_t count) {
+size_t div_scratch_of(int64_t count) {
     constexpr size_t RB = (size_t)kRowWords<N>() * 4;
     const int64_t chunk_max = (int64_t)std::max<size_t>(4096, (kDivScratchBytes / (RB + 13)) & ~(size_t)4095);
     const int64_t chunk = count < chunk_max ? count : chunk_max;
@@ -368,17 +369,24 @@ static size_t div_scratch_of(int64_t count) {
            sizeof(DivRowsG);
 }
 
+/* the per-count entry points: extern here, instantiated for this unit's counts */
+#define GRNS_DIV_ROOTS_(n, EXT)                                                                                      \
+    EXT template grns_status run_div<n>(const grns_ctx *, const uint32_t *, const uint32_t *, int64_t, int64_t,        \
+                                        uint32_t *, uint32_t *, uint8_t *, cudaStream_t, int);                       \
+    EXT template grns_status run_scale<n>(const grns_ctx *, const uint32_t *, const uint32_t *, uint32_t, int64_t,     \
+                                          int64_t, uint32_t *, uint8_t *, cudaStream_t, int);                        \
+    EXT template size_t div_scratch_of<n>(int64_t);
+#define GRNS_EXTERN_(n) GRNS_DIV_ROOTS_(n, extern)
+#define GRNS_DEFINE_(n) GRNS_DIV_ROOTS_(n, )
+GRNS_FOR_EACH_N(GRNS_EXTERN_)
+GRNS_PART_N(GRNS_DEFINE_)
+#undef GRNS_EXTERN_
+#undef GRNS_DEFINE_
+
+#if GRNS_PART_MAIN
 size_t div_scratch_bytes(const grns_ctx *c, int64_t count) {
 #define C_(n) return div_scratch_of<n>(count)
-    switch (c->n) {
-        case 4: C_(4);
-        case 8: C_(8);
-        case 12: C_(12);
-        case 16: C_(16);
-        case 32: C_(32);
-        case 64: C_(64);
-        default: return 0;
-    }
+    GRNS_SWITCH_N(c->n, return 0)
 #undef C_
 }
 
@@ -395,5 +403,7 @@ grns_status launch_scale2pow(const grns_ctx *c, const uint32_t *x, const uint32_
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }
+
+#endif  // GRNS_PART_MAIN
 
 }  // namespace grns

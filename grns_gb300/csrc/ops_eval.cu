@@ -4,6 +4,7 @@
  *   k_cmp : out[k] = rns_cmp(X_k, Y_k)       (reference src/rnscmp.cuh:55),
  *           both evaluations fused in registers, never written back.
  * One thread per number, grid-stride, residues read per modulus slice.
+ * GRNS_SPLIT_BY_N: compiled as one unit per group of moduli counts.
  */
 #include "internal.h"
 #include "rns_device.cuh"
@@ -285,8 +286,8 @@ __global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ Con
 }
 
 template <int N, bool FAST>
-static grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
-                            uint8_t *flags, cudaStream_t s) {
+grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
+                     uint8_t *flags, cudaStream_t s) {
     const int B = 256;
     if (N <= 32)
         k_eval_pipe<N, FAST><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
@@ -298,8 +299,8 @@ static grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, in
 }
 
 template <int N>
-static grns_status run_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, int64_t ld, int64_t count,
-                           int32_t *out, uint8_t *flags, cudaStream_t s) {
+grns_status run_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, int64_t ld, int64_t count, int32_t *out,
+                    uint8_t *flags, cudaStream_t s) {
     const int B = 256;
     if (c->path == GRNS_PATH_REFERENCE)
         k_cmp<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{y, ld}, count, out,
@@ -314,8 +315,8 @@ static grns_status run_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t 
 }
 
 template <int N>
-static grns_status run_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
-                                  uint8_t *flags, cudaStream_t s) {
+grns_status run_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
+                           uint8_t *flags, cudaStream_t s) {
     const int B = 256;
     if (ld != 0 && ld % 4 == 0 && ((uintptr_t)x % 16) == 0)
         k_eval_tight_soa4<N><<<grid_for(c, (count + 3) / 4, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld},
@@ -326,6 +327,24 @@ static grns_status run_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t 
     return cuda_status(cudaGetLastError());
 }
 
+/* the per-count entry points: extern here, instantiated for this unit's counts below */
+#define GRNS_EVAL_ROOTS_(n, EXT)                                                                                    \
+    EXT template grns_status run_eval<n, true>(const grns_ctx *, const uint32_t *, int64_t, int64_t, interval_t *,   \
+                                               uint8_t *, cudaStream_t);                                            \
+    EXT template grns_status run_eval<n, false>(const grns_ctx *, const uint32_t *, int64_t, int64_t, interval_t *,  \
+                                                uint8_t *, cudaStream_t);                                           \
+    EXT template grns_status run_cmp<n>(const grns_ctx *, const uint32_t *, const uint32_t *, int64_t, int64_t,      \
+                                        int32_t *, uint8_t *, cudaStream_t);                                        \
+    EXT template grns_status run_eval_tight<n>(const grns_ctx *, const uint32_t *, int64_t, int64_t, interval_t *,   \
+                                               uint8_t *, cudaStream_t);
+#define GRNS_EXTERN_(n) GRNS_EVAL_ROOTS_(n, extern)
+#define GRNS_DEFINE_(n) GRNS_EVAL_ROOTS_(n, )
+GRNS_FOR_EACH_N(GRNS_EXTERN_)
+GRNS_PART_N(GRNS_DEFINE_)
+#undef GRNS_EXTERN_
+#undef GRNS_DEFINE_
+
+#if GRNS_PART_MAIN
 grns_status launch_eval_tight(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                               uint8_t *flags, cudaStream_t s) {
 #define C_(n) return run_eval_tight<n>(c, x, ld, count, out, flags, s)
@@ -346,5 +365,6 @@ grns_status launch_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, 
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }
+#endif  // GRNS_PART_MAIN
 
 }  // namespace grns

@@ -256,15 +256,7 @@ grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count
     }
     grns_status st;
 #define C_(n) st = run_max<n>(c, x, ld, count, out_value, out_index, scratch, s); break
-    switch (c->n) {
-        case 4: C_(4);
-        case 8: C_(8);
-        case 12: C_(12);
-        case 16: C_(16);
-        case 32: C_(32);
-        case 64: C_(64);
-        default: st = GRNS_ERR_UNSUPPORTED;
-    }
+    GRNS_SWITCH_N(c->n, st = GRNS_ERR_UNSUPPORTED)
 #undef C_
     if (owned) {
         cudaError_t e = scratch_free(scratch, s);

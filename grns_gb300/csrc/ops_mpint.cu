@@ -22,7 +22,7 @@ __global__ void __launch_bounds__(256) k_mpint(const __grid_constant__ Consts<N>
                                                int64_t count, MpInt<N> *__restrict__ out, uint8_t *__restrict__ flags) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         MpInt<N> a = x[k], b = y[k], r;
-        r.pad = 0;
+        clear_pad(r);
         uint32_t f = 0;
         if (op == 2) mpint_mul<N>(C, r, a, b, f);
         else mpint_addsub<N>(C, r, a, b, op == 1, f);
@@ -141,7 +141,7 @@ __device__ __forceinline__ void mp_chunk(const Consts<N> &C, const uint4 *K, int
     __syncwarp();  // every lane of the record has read its sign and evaluation
     if (act && p == 0) {
         a.sign = sign;
-        a.pad = 0;
+        clear_pad(a);
         a.eval[0] = lo;
         a.eval[1] = up;
         f |= overflow_flags_i<N>(C, lo, up);

@@ -52,6 +52,15 @@ struct Er {  // er_float_t
 };
 
 /* Constant block of one moduli set, specialised on the moduli count N. */
+/* the moduli counts kernels are built for: every n from 4 to 16 (the
+ * reference's params catalogue up to 16 moduli), 32 and 64 */
+#define GRNS_FOR_EACH_N(X) \
+    X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(32) X(64)
+GRNS_HD constexpr bool supported_n(int n) { return (n >= 4 && n <= 16) || n == 32 || n == 64; }
+
+/* words per row of the binary conversion tables: n rounded up to a multiple of 4 */
+GRNS_HD constexpr int bin_ld(int n) { return (n + 3) / 4 * 4; }
+
 template <int N>
 struct Consts {
     uint32_t m[N];        // moduli
@@ -100,9 +109,9 @@ struct Consts {
      * 2^-j (p2nlo); [i * p2rows + a]: 2^(64 a) (p2hi), 2^-(64 a) (p2nhi) mod m_i */
     const uint2 *p2lo, *p2hi, *p2nlo, *p2nhi;
     int p2rows;
-    /* binary conversion (16-byte aligned rows) */
-    const uint32_t *bin_p26;    // [kBinMaxChunks * N]  2^(26 c) mod m_i
-    const uint32_t *bin_mi26;   // [bin_chunks * N]     26-bit chunk c of M_i = M / m_i
+    /* binary conversion (16-byte aligned rows of bin_ld(N) words, zeros past N) */
+    const uint32_t *bin_p26;    // [kBinMaxChunks * bin_ld(N)]  2^(26 c) mod m_i
+    const uint32_t *bin_mi26;   // [bin_chunks * bin_ld(N)]     26-bit chunk c of M_i = M / m_i
     const uint32_t *bin_m26;    // [bin_chunks]         26-bit chunk c of M
     int bin_chunks;             // ceil(bits(M) / 26)
     int bin_limbs;              // ceil(bits(M) / 32): 32-bit limbs of an integer below M

@@ -49,7 +49,7 @@ GRNS_HD void from_binary(const Consts<N> &C, const uint32_t *row, int nlimbs, ui
     const int chunks = (32 * nlimbs + kBinChunk - 1) / kBinChunk;
     for (int i = 0; i < N; i++) {
         uint64_t acc = 0;
-        for (int c = 0; c < chunks; c++) acc += (uint64_t)bin_chunk(row, nlimbs, c) * C.bin_p26[c * N + i];
+        for (int c = 0; c < chunks; c++) acc += (uint64_t)bin_chunk(row, nlimbs, c) * C.bin_p26[c * bin_ld(N) + i];
         res[i] = bin_mod64<N>(C, i, acc);
     }
 }
@@ -75,7 +75,7 @@ GRNS_HD uint32_t bin_rank(const Consts<N> &C, const uint32_t *s) {
 template <int N>
 GRNS_HD uint32_t bin_crt_chunk(const Consts<N> &C, const uint32_t *s, uint32_t kk, int c, int64_t &carry) {
     uint64_t acc = 0;
-    const uint32_t *row = C.bin_mi26 + (size_t)c * N;
+    const uint32_t *row = C.bin_mi26 + (size_t)c * bin_ld(N);
     for (int i = 0; i < N; i++) acc += (uint64_t)s[i] * row[i];
     const int64_t v = (int64_t)acc - (int64_t)kk * C.bin_m26[c] + carry;
     carry = v >> kBinChunk;  // floor division (arithmetic shift)

@@ -722,9 +722,12 @@ GRNS_HD uint64_t dv_digit(const DivSt &st, u128 U, uint64_t E, uint32_t &flags) 
 }
 
 /* c = floor(R / D) for 0 <= R < 4D from the fixed-point values; -1 when a
- * comparison is too close to call (the exact path decides) */
+ * comparison is too close to call (the exact path decides).  UR < E is
+ * ambiguous once 4D may reach M (1 - E / 2^96): R is then either tiny or
+ * within E M / 2^96 of M, where the evaluation wraps past 2^96 to below E. */
 GRNS_HD int dv_final_fx(const DivSt &st, u128 UR, uint64_t Eu) {
     const u128 E = Eu;
+    if (UR < E && 4 * st.UD + E > (((u128)1) << 96)) return -1;
     int c = 0;
     for (int j = 1; j <= 3; j++) {
         const u128 jD = (u128)j * st.UD, jDl = (u128)j * (st.UD - E);

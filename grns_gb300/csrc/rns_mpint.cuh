@@ -12,14 +12,35 @@
 
 namespace grns {
 
+/* byte layout of the reference mp_int_t for n = N: digits, sign, then the
+ * 8-byte aligned evaluation -- 4 bytes of padding after the sign for even N,
+ * none for odd N */
+template <int N, bool EVEN = (N % 2 == 0)>
+struct MpIntT;
 template <int N>
-struct MpInt {  // byte layout of the reference mp_int_t for n = N (N even: 4 bytes of padding)
+struct MpIntT<N, true> {
     uint32_t digits[N];
     int32_t sign;
     int32_t pad;  // written as 0
     Er eval[2];
 };
-static_assert(sizeof(MpInt<8>) == 72 && sizeof(MpInt<32>) == 168 && sizeof(MpInt<64>) == 296, "mp_int_t layout");
+template <int N>
+struct MpIntT<N, false> {
+    uint32_t digits[N];
+    int32_t sign;
+    Er eval[2];
+};
+template <int N>
+using MpInt = MpIntT<N>;
+template <int N>
+__host__ __device__ __forceinline__ void clear_pad(MpIntT<N, true> &r) {
+    r.pad = 0;
+}
+template <int N>
+__host__ __device__ __forceinline__ void clear_pad(MpIntT<N, false> &) {}
+static_assert(sizeof(MpInt<8>) == 72 && sizeof(MpInt<32>) == 168 && sizeof(MpInt<64>) == 296 &&
+                  sizeof(MpInt<5>) == 56 && sizeof(MpInt<15>) == 96,
+              "mp_int_t layout");
 
 __device__ __forceinline__ double neg_if(double v, bool neg) { return neg ? -v : v; }
 
@@ -65,7 +86,7 @@ __device__ __forceinline__ void mpint_div_finish(const Consts<N> &C, int xs, int
     }
     eval<N>(C, [&](int i) { return res.digits[i]; }, res.eval[0], res.eval[1], f);
     res.sign = qz ? 0 : (xs ^ ys);
-    res.pad = 0;
+    clear_pad(res);
 }
 
 /* er_md_rd / er_md_ru (src/extrange.cuh:557/:566) with the product and the

@@ -24,10 +24,37 @@
 #define ON 4
 #include "grns_oracle_n.h"
 #undef ON
+#define ON 5
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 6
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 7
+#include "grns_oracle_n.h"
+#undef ON
 #define ON 8
 #include "grns_oracle_n.h"
 #undef ON
+#define ON 9
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 10
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 11
+#include "grns_oracle_n.h"
+#undef ON
 #define ON 12
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 13
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 14
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 15
 #include "grns_oracle_n.h"
 #undef ON
 #define ON 16
@@ -40,7 +67,7 @@
 #include "grns_oracle_n.h"
 #undef ON
 
-#define OR_SUPPORTED(n) ((n) == 4 || (n) == 8 || (n) == 12 || (n) == 16 || (n) == 32 || (n) == 64)
+#define OR_SUPPORTED(n) (((n) >= 4 && (n) <= 16) || (n) == 32 || (n) == 64)
 
 /* mod_inverse semantics (src/rnsbase.cuh:121/:156): the inverse in [0, m). */
 static long or_inverse(long x, long m) {
@@ -194,12 +221,21 @@ int oracle_max_threads(void) {
 
 #define OR_DISPATCH(c, CALL)                 \
     switch ((c)->n) {                        \
-        case 4: CALL(4); break;              \
-        case 8: CALL(8); break;              \
-        case 12: CALL(12); break;            \
-        case 16: CALL(16); break;            \
-        case 32: CALL(32); break;            \
-        case 64: CALL(64); break;            \
+        case 4: CALL(4); break;          \
+        case 5: CALL(5); break;          \
+        case 6: CALL(6); break;          \
+        case 7: CALL(7); break;          \
+        case 8: CALL(8); break;          \
+        case 9: CALL(9); break;          \
+        case 10: CALL(10); break;        \
+        case 11: CALL(11); break;        \
+        case 12: CALL(12); break;        \
+        case 13: CALL(13); break;        \
+        case 14: CALL(14); break;        \
+        case 15: CALL(15); break;        \
+        case 16: CALL(16); break;        \
+        case 32: CALL(32); break;        \
+        case 64: CALL(64); break;        \
         default: break;                      \
     }
 

@@ -47,8 +47,9 @@ def floor_log2_product(moduli):
 
 
 # tag -> moduli (None = the reference's shipped src/params.h; a string = a
-# params file of the reference's catalogue, pre-included as it is)
-SETS = {
+# params file of the reference's catalogue, pre-included as it is).  BASE is
+# what build() compiles by default; make_golden.py also builds CATALOGUE.
+BASE = {
     "ref8": None,
     "g8": greedy_moduli(8),
     "g12": greedy_moduli(12),
@@ -58,6 +59,19 @@ SETS = {
     "p32": "src/params/moduli-64-4096-bit/params.32m.512b.h",  # 17-bit moduli
     "p64": "src/params/moduli-100-6400-bit/params.64m.1600b.h",  # 26-bit moduli
 }
+
+# the rest of the catalogue up to 64 moduli: catNN_nK = params.Km.*.h of the
+# family moduli-*-NN-bit (p16 / p32 / p64 above are cat69_n16 / cat4096_n32 /
+# cat6400_n64)
+_FAMILIES = {
+    "69": ("moduli-10-69-bit", {4: 10, 5: 13, 6: 17, 7: 22, 8: 26, 9: 31, 10: 36, 11: 41, 12: 47, 13: 52, 14: 58,
+                                15: 63}),
+    "4096": ("moduli-64-4096-bit", {4: 64, 8: 128, 16: 256, 64: 1024}),
+    "6400": ("moduli-100-6400-bit", {4: 100, 8: 200, 16: 400, 32: 800}),
+}
+CATALOGUE = {f"cat{fam}_n{n}": f"src/params/{d}/params.{n}m.{b}b.h"
+             for fam, (d, sizes) in _FAMILIES.items() for n, b in sizes.items()}
+SETS = {**BASE, **CATALOGUE}
 
 
 def catalogue_moduli(relpath):
@@ -131,8 +145,8 @@ def build(tags=None, quiet=False, ref=None):
             print("oracle/_ref: libgmp.so.10 / libmpfr.so.6 not found; nothing built")
         return {}
     os.makedirs(OUT, exist_ok=True)
-    tags = list(tags or SETS)
-    with ThreadPoolExecutor(len(tags)) as ex:
+    tags = list(tags or BASE)
+    with ThreadPoolExecutor(min(len(tags), os.cpu_count() or 4)) as ex:
         paths = list(ex.map(lambda t: build_one(t, gmp, mpfr), tags))
     return dict(zip(tags, paths))
 

@@ -13,8 +13,8 @@ mp_int division operands with the Euclidean sign cases, binary <-> RNS
 conversions through the reference's GMP routines, and the
 extended-range doubles of tests/test_verify_extrange.cu:115-117.
 
-Run from the repository root:
-    GRNS_REFERENCE=<reference checkout> python tests/golden/make_golden.py
+Run from the repository root (all tags, or the tags named):
+    GRNS_REFERENCE=<reference checkout> python tests/golden/make_golden.py [tag ...]
 (needs the reference checkout and libgmp/libmpfr; the fixtures it writes are
 committed, so the tests themselves never need the reference).
 """
@@ -32,7 +32,7 @@ from oracle.oracle import REFERENCE_DEFAULT_MODULI  # noqa: E402
 from oracle.ref import build_ref  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"]
+TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"] + list(build_ref.CATALOGUE)
 
 
 def special_values(M, log2M):
@@ -51,11 +51,11 @@ def limbs_of(values, limbs):
     return out
 
 
-def main():
-    built = refcheck.build_ref.build(TAGS)
+def main(tags):
+    built = refcheck.build_ref.build(tags)
     if not built:
         raise SystemExit("reference checker libraries unavailable")
-    for tag in TAGS:
+    for tag in tags:
         ref = refcheck.get(tag)
         moduli = build_ref.SETS[tag] or REFERENCE_DEFAULT_MODULI
         if isinstance(moduli, str):  # a params file of the reference's catalogue
@@ -88,7 +88,7 @@ def main():
         xd = res(Xd)
         S = np.array([1 + (k * 37) % 60 for k in range(N)], dtype=np.uint32)
         S[:6] = [29, 30, 31, 60, L, L + 3]
-        half = 1 << (L // 2 - 10)
+        half = 1 << (L // 2 - 10 if L >= 40 else max(1, L // 2 - 1))  # products stay below M
         A = [rng.randrange(-half, half) for _ in range(N)]
         B = [rng.randrange(-half, half) for _ in range(N)]
         A[0], B[0] = -55, 13
@@ -104,11 +104,13 @@ def main():
             fx[f"div_q_{path}"], fx[f"div_r_{path}"] = q, r
             fx[f"scale_{path}"] = ref.scale2pow(x, S, dev=dev)
             fx[f"mrc_{path}"] = ref.mrc(x, dev=dev)
-        fx["eval_fast_host"] = ref.eval(x, dev=False, fast=True).view(np.uint8)
-        # cuda::rns_eval_compute_fast requires a number "not too large" (src/rnseval.cuh:259):
-        # near M the reference reads outside its tables, so only X < M/2 here
+        # rns_eval_compute_fast requires a number "not too large" (src/rnseval.cuh:259;
+        # the host form at :112 likewise): near M both forms' refinement index runs
+        # past RNS_POW2 (the host form crashed on X = 2^47 of params.12m.47b.h), so
+        # only X < M/2 here
         xf = res([v for v in X if v < M // 2])
         fx["xf"] = xf
+        fx["eval_fast_host"] = ref.eval(xf, dev=False, fast=True).view(np.uint8)
         fx["eval_fast_dev"] = ref.eval(xf, dev=True, fast=True).view(np.uint8)
         # mp_int inputs through the reference's own constructor (host eval), then both op paths
         ma = np.concatenate([ref.mpint_from_str(v).view(np.uint8) for v in A])
@@ -169,4 +171,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or TAGS)

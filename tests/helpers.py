@@ -6,9 +6,14 @@ import numpy as np
 from oracle.oracle import REFERENCE_DEFAULT_MODULI, greedy_moduli
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# moduli sets: the reference's shipped default (ref8), greedy 30-bit sets (gN) and
-# three sets of the reference's params catalogue (pN: moduli 3..59, 17-bit, 26-bit)
-TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"]
+# moduli sets: the reference's shipped default (ref8), greedy 30-bit sets (gN),
+# three sets of the reference's params catalogue (pN: moduli 3..59, 17-bit,
+# 26-bit) and the catalogue's other files up to 64 moduli (catFAMILY_nK =
+# src/params/moduli-*-FAMILY-bit/params.Km.*.h)
+BASE_TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"]
+CATALOGUE_TAGS = ["cat69_n%d" % n for n in range(4, 16)] + ["cat4096_n%d" % n for n in (4, 8, 16, 64)] + \
+    ["cat6400_n%d" % n for n in (4, 8, 16, 32)]
+TAGS = BASE_TAGS + CATALOGUE_TAGS
 
 ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
 IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
@@ -17,7 +22,7 @@ IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
 def moduli_for(tag):
     if tag == "ref8":
         return list(REFERENCE_DEFAULT_MODULI)
-    if tag.startswith("p"):  # recorded in the fixture by tests/golden/make_golden.py
+    if tag.startswith(("p", "cat")):  # recorded in the fixture by tests/golden/make_golden.py
         return [int(m) for m in np.load(os.path.join(GOLDEN, f"golden_{tag}.npz"))["moduli"]]
     return greedy_moduli(int(tag[1:]))
 

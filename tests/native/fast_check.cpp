@@ -21,8 +21,8 @@ struct Box {
 template <int N>
 static const Consts<N> &K(const Box *b) { return *reinterpret_cast<const Consts<N> *>(b->consts); }
 
-#define DISPATCH(n, CALL) switch (n) { case 4: CALL(4); break; case 8: CALL(8); break; case 12: CALL(12); break; \
-    case 16: CALL(16); break; case 32: CALL(32); break; case 64: CALL(64); break; default: return -1; }
+#define FC_CASE_(n) case n: C_(n); break;  // C_: the caller's macro
+#define DISPATCH(n, CALL) switch (n) { GRNS_FOR_EACH_N(FC_CASE_) default: return -1; }
 
 extern "C" {
 
@@ -32,8 +32,9 @@ void *fc_create(const uint32_t *m, int n) {
     build_tables(b->T, m, n);
     b->blob = table_blob(b->T);
 #define F_(N) fill_consts<N>(*reinterpret_cast<Consts<N> *>(b->consts), b->T, b->blob.data())
-    switch (n) { case 4: F_(4); break; case 8: F_(8); break; case 12: F_(12); break; case 16: F_(16); break;
-                 case 32: F_(32); break; case 64: F_(64); break; default: delete b; return nullptr; }
+#define FC_FILL_(n) case n: F_(n); break;
+    switch (n) { GRNS_FOR_EACH_N(FC_FILL_) default: delete b; return nullptr; }
+#undef FC_FILL_
 #undef F_
     return b;
 }

@@ -50,8 +50,8 @@ def test_status_strings(lib):
 def test_invalid_arguments_rejected_without_gpu(lib):
     out = ctypes.c_void_p()
     assert lib.grns_ctx_create(None, 8, ctypes.byref(out)) == 1
-    mods = (ctypes.c_int32 * 8)(*([3] * 8))
-    assert lib.grns_ctx_create(mods, 7, ctypes.byref(out)) == 2  # unsupported n
+    mods = (ctypes.c_int32 * 17)(*([3] * 17))
+    assert lib.grns_ctx_create(mods, 17, ctypes.byref(out)) == 2  # unsupported n
     assert lib.grns_eval(None, None, 1, 0, None, None, None) == 1
 
 

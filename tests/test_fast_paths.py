@@ -198,6 +198,20 @@ def test_division_quotient_boundaries(fc, tag):
     assert not fl.any()
 
 
+@pytest.mark.parametrize("tag", TAGS)
+def test_division_remainder_evaluation_wraps(fc, tag):
+    """dividends within a hair of M over divisors just below M (above the
+    near-M band, within 2^-53 M): the final remainder's fixed-point value
+    wraps past 2^96, and the correction must not read it as a small R"""
+    from tests.test_gpu_parity import near_m_division_cases
+    f = FC(fc, moduli_for(tag))
+    X, Dv = near_m_division_cases(f.M)
+    q, r, fl = f.div(X, Dv)
+    assert q == [a // b for a, b in zip(X, Dv)]
+    assert r == [a % b for a, b in zip(X, Dv)]
+    assert not fl.any()
+
+
 @pytest.mark.parametrize("tag", ["ref8", "g8", "g32", "g64", "p16", "p32", "p64"])
 def test_division_short_and_extreme_dividends(fc, tag):
     """dividends of every length (the leading zero digits are skipped), and
@@ -237,7 +251,7 @@ def test_integer_eval_is_bit_exact(fc, tag):
     rng = random.Random(41)
     vals = [rng.randrange(M) for _ in range(3000)]
     vals += [0, 1, 2, M - 1, M - 2, M // 2, M // 3, (M + 1) // 2] + [M >> j for j in range(1, 200, 7)]
-    vals += [rng.randrange(M >> 40) for _ in range(200)]
+    vals += [rng.randrange(max(1, M >> 40)) for _ in range(200)]
     x = f.res(vals)
     st = np.zeros(len(vals), np.int32)
     iv = np.zeros(len(vals), IV)
@@ -284,7 +298,7 @@ def test_one_ulp_evaluation(fc, tag):
     f, orc = FC(fc, mods), O.Oracle(mods)
     M = f.M
     rng = random.Random(43)
-    vals = [rng.randrange(M) for _ in range(1500)] + [rng.randrange(M >> 30) for _ in range(100)]
+    vals = [rng.randrange(M) for _ in range(1500)] + [rng.randrange(max(1, M >> 30)) for _ in range(100)]
     vals += [1, 2, M - 1, M // 2, M // 3, (M + 1) // 2] + [M >> j for j in range(1, 120, 9)]
     x = f.res(vals)
     ok = np.zeros(len(vals), np.int32)

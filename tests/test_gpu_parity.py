@@ -200,6 +200,32 @@ def test_div(case, layout, path):
     assert int(flags.sum()) == 0
 
 
+def near_m_division_cases(M):
+    """dividends within a hair of M over divisors just below M, between the
+    band where a divisor counts as near M and 2^-53 M: the remainder's
+    fixed-point evaluation wraps past 2^96 there"""
+    X, D = [], []
+    for b in (2, 20, 40, 53, 60, 67, 75, 85):
+        d = M - max(1, M >> b)
+        for x in (M - 1, M - 2, M - 1 - (1 << 22), M - (M >> 90 if M >> 90 else 3), d, d + 1, d - 1):
+            if 0 < d < M and 0 <= x < M:
+                X.append(x)
+                D.append(d)
+    return X, D
+
+
+@pytest.mark.parametrize("layout", ["soa", "aos"])
+def test_div_dividend_and_divisor_near_m(case, layout, path):
+    tag, ctx, orc, g = case
+    X, Dv = near_m_division_cases(orc.exact.M)
+    x, d = orc.exact.to_rns(X), orc.exact.to_rns(Dv)
+    flags = flags_buf(len(X))
+    q, r = ctx.rns_div(to_dev(x, layout), to_dev(d, layout), layout=layout, flags=flags)
+    assert orc.exact.from_rns(from_dev(q, layout)) == [a // b for a, b in zip(X, Dv)]
+    assert orc.exact.from_rns(from_dev(r, layout)) == [a % b for a, b in zip(X, Dv)]
+    assert int(flags.sum()) == 0
+
+
 def test_div_by_zero_flag(case, path):
     tag, ctx, orc, g = case
     x = orc.exact.to_rns([12345, 7])

@@ -39,7 +39,7 @@ def test_eval_matches_golden(case, path, code):
 
 def test_eval_fast_host_matches_golden(case):
     tag, orc, g = case
-    assert orc.eval(g["x"], path=O.PATH_HOST_FAST).view(np.uint8).tobytes() == g["eval_fast_host"].tobytes()
+    assert orc.eval(g["xf"], path=O.PATH_HOST_FAST).view(np.uint8).tobytes() == g["eval_fast_host"].tobytes()
 
 
 def test_eval_fast_device_matches_golden(case):
