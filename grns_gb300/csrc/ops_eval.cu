@@ -91,6 +91,65 @@ __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Co
     }
 }
 
+/* the same with the numbers claimed by warps from a counter, kEvalClaim
+ * lanes' worth at a time, so the FP64-pipe and integer-pipe warps each take
+ * work at their own rate until the array runs out (with a fixed grid-stride
+ * share the faster kind idles at the end); the next number's residues load
+ * while the current one is evaluated */
+constexpr int kEvalClaim = 8;  // numbers per lane per claim
+
+template <int N, bool FAST = false>
+__global__ void __launch_bounds__(256, 2) k_eval_claim(const __grid_constant__ Consts<N> C, Operand<N> x,
+                                                       int64_t count, Er *__restrict__ out,
+                                                       uint8_t *__restrict__ flags, int fp_eighths,
+                                                       unsigned long long *__restrict__ ctr) {
+    const bool fp = warp_on_fp64(fp_eighths);
+    const int lane = threadIdx.x & 31;
+    auto claim = [&]() -> int64_t {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(ctr, 32ull * kEvalClaim);
+        return (int64_t)__shfl_sync(0xffffffffu, b, 0);
+    };
+    int64_t base = claim();
+    int j = 0;
+    int64_t k = base + lane;
+    uint32_t cur[N];
+    if (k < count) {
+#pragma unroll
+        for (int i = 0; i < N; i++) cur[i] = x.load(k, i);
+    }
+    while (base < count) {  // warp-uniform
+        int64_t nbase = base;
+        int nj = j + 1;
+        if (nj == kEvalClaim) {
+            nbase = claim();
+            nj = 0;
+        }
+        const int64_t kn = nbase + 32 * nj + lane;
+        uint32_t nxt[N];
+        if (kn < count) {
+#pragma unroll
+            for (int i = 0; i < N; i++) nxt[i] = x.load(kn, i);
+        }
+        if (k < count) {
+            uint32_t f = 0;
+            Er lo, up;
+            auto getc = [&](int i) { return cur[i]; };
+            const int64_t kk = k;
+            auto getm = [&](int i) { return x.load(kk, i); };
+            eval_split<N, FAST>(C, fp, getc, getm, lo, up, f);
+            out[2 * k] = lo;
+            out[2 * k + 1] = up;
+            if (flags) flags[k] = (uint8_t)f;
+        }
+#pragma unroll
+        for (int i = 0; i < N; i++) cur[i] = nxt[i];
+        base = nbase;
+        j = nj;
+        k = kn;
+    }
+}
+
 /* one-ulp enclosure where certified (rns_fast.cuh eval_tight), the
  * bit-exact evaluation otherwise (noinline: rare for uniform X) */
 template <int N>
@@ -285,16 +344,32 @@ __global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ Con
     }
 }
 
+constexpr int64_t kEvalClaimMin = 1 << 16;  // smaller arrays keep the fixed grid-stride share
+
 template <int N, bool FAST>
 grns_status run_eval(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, interval_t *out,
                      uint8_t *flags, cudaStream_t s) {
     const int B = 256;
-    if (N <= 32)
-        k_eval_pipe<N, FAST><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
-                                                                   (Er *)out, flags, c->eval_fp64_eighths);
-    else
+    if constexpr (N > 32) {
         k_eval<N, FAST><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
                                                            flags, c->eval_fp64_eighths);
+        return cuda_status(cudaGetLastError());
+    }
+    if (count >= kEvalClaimMin && c->eval_fp64_eighths > 0 && c->eval_fp64_eighths < 8) {
+        /* both pipes in use: warps claim their numbers (a counter from the pool, zeroed in stream order) */
+        void *ctr = nullptr;
+        cudaError_t e = scratch_alloc(c, &ctr, sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return cuda_status(e);
+        k_eval_claim<N, FAST><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
+                                                                    (Er *)out, flags, c->eval_fp64_eighths,
+                                                                    (unsigned long long *)ctr);
+        e = cudaGetLastError();
+        scratch_free(ctr, s);
+        return cuda_status(e);
+    }
+    k_eval_pipe<N, FAST><<<grid_for(c, count, B, 2), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count, (Er *)out,
+                                                               flags, c->eval_fp64_eighths);
     return cuda_status(cudaGetLastError());
 }
 

@@ -67,7 +67,8 @@ const char *grns_version(void);
  * Replaces rns_const_init() (reference src/rnsbase.cuh:324) and
  * mpint_const_init() (src/mpint.cuh:20), which fill process-global tables;
  * here every moduli set is its own context, so several (e.g. n = 32 and
- * n = 64) can be resident together.  Supported n: 4, 8, 12, 16, 32, 64;
+ * n = 64) can be resident together.  Supported n: every n from 4 to 16, 32
+ * and 64 (the reference's params catalogue up to 64 moduli);
  * moduli odd, pairwise coprime, 3 <= m_i <= 1431655765. */
 grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out);
 grns_status grns_ctx_destroy(grns_ctx *ctx);

@@ -107,12 +107,38 @@ def find_lib(name):
     return None
 
 
-def build_one(tag, gmp, mpfr):
-    src = os.path.join(REF, "src")
-    out = os.path.join(OUT, f"libgrnsref_{tag}.so")
-    drv = os.path.join(HERE, "ref_driver.cpp")
+# the sets whose n-threaded device functions run as one emulated block
+# (oracle/ref/ref_block.cpp: n a multiple of 32, whole warps)
+BLOCK_TAGS = ["g32", "g64", "p32", "p64"]
+
+
+def block_headers():
+    """oracle/_ref/block_src: the reference's src/ headers for the block
+    build, with `static __shared__` written `__shared__` (the shim defines
+    __shared__ as `static` there; CUDA's __shared__ locals are block-wide
+    statics already).  Generated from the checkout, never committed."""
+    src, dst = os.path.join(REF, "src"), os.path.join(OUT, "block_src")
+    os.makedirs(dst, exist_ok=True)
+    for f in os.listdir(src):
+        if f.endswith((".cuh", ".h")):
+            with open(os.path.join(src, f)) as fh:
+                text = fh.read()
+            with open(os.path.join(dst, f), "w") as fh:
+                fh.write(text.replace("static __shared__", "__shared__"))
+    return dst
+
+
+def build_one(tag, gmp, mpfr, block=False):
+    src = block_headers() if block else os.path.join(REF, "src")
+    out = os.path.join(OUT, f"libgrnsref_block_{tag}.so" if block else f"libgrnsref_{tag}.so")
+    drv = os.path.join(HERE, "ref_block.cpp" if block else "ref_driver.cpp")
     cmd = ["g++", "-std=c++14", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-frounding-math",
            "-w", "-include", os.path.join(HERE, "shim", "cuda_host_shim.h")]
+    if block:
+        # -fno-gnu-unique: the block-wide statics of inline functions stay
+        # private to each set's library (as GNU-unique symbols the loader
+        # would merge the n = 32 and n = 64 sets' arrays across libraries)
+        cmd += ["-DORACLE_BLOCK_EMULATION", "-pthread", "-fno-gnu-unique"]
     if isinstance(SETS[tag], str):
         cmd += ["-include", os.path.join(REF, SETS[tag])]
     elif SETS[tag] is not None:
@@ -146,8 +172,10 @@ def build(tags=None, quiet=False, ref=None):
         return {}
     os.makedirs(OUT, exist_ok=True)
     tags = list(tags or BASE)
-    with ThreadPoolExecutor(min(len(tags), os.cpu_count() or 4)) as ex:
+    blocks = [t for t in BLOCK_TAGS if t in tags]
+    with ThreadPoolExecutor(min(len(tags) + len(blocks), os.cpu_count() or 4)) as ex:
         paths = list(ex.map(lambda t: build_one(t, gmp, mpfr), tags))
+        list(ex.map(lambda t: build_one(t, gmp, mpfr, block=True), blocks))
     return dict(zip(tags, paths))
 
 

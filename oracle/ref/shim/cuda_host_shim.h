@@ -16,7 +16,13 @@
  *  - cudaMemcpyToSymbol copies into the (now host) symbol, so the `cuda::`
  *    constant tables are filled exactly as rns_const_init fills them on a GPU.
  *  - Thread-index builtins exist only so the n-threaded variants compile;
- *    the checker never calls those variants.
+ *    the serial checker never calls those variants.  With
+ *    ORACLE_BLOCK_EMULATION defined (oracle/ref/ref_block.cpp) they run for
+ *    real: one host thread per CUDA thread of a block, threadIdx per thread,
+ *    __syncthreads a barrier of the block, __shfl_down_sync an exchange among
+ *    the 32 lanes of a warp, and __shared__ locals block-wide statics (the
+ *    CUDA meaning; the recipe drops the reference's redundant `static`
+ *    before `__shared__` in its build copy of the headers).
  */
 #ifndef ORACLE_CUDA_HOST_SHIM_H
 #define ORACLE_CUDA_HOST_SHIM_H
@@ -32,7 +38,11 @@
 #define __host__
 #define __global__
 #define __constant__
+#ifdef ORACLE_BLOCK_EMULATION
+#define __shared__ static
+#else
 #define __shared__
+#endif
 #define __forceinline__ inline
 
 typedef int cudaError_t;
@@ -47,10 +57,19 @@ inline cudaError_t cudaMemcpyToSymbol(T &symbol, const void *src, size_t bytes) 
 }
 
 struct oracle_shim_dim3 { unsigned x, y, z; };
-extern oracle_shim_dim3 threadIdx, blockIdx, blockDim, gridDim;
 static const int warpSize = 32;
+#ifdef ORACLE_BLOCK_EMULATION
+extern thread_local oracle_shim_dim3 threadIdx;
+extern oracle_shim_dim3 blockIdx, blockDim, gridDim;
+void oracle_block_sync();
+double oracle_warp_shfl_down(double v, int delta);
+inline void __syncthreads() { oracle_block_sync(); }
+inline double __shfl_down_sync(unsigned, double v, int delta) { return oracle_warp_shfl_down(v, delta); }
+#else
+extern oracle_shim_dim3 threadIdx, blockIdx, blockDim, gridDim;
 inline void __syncthreads() {}
 inline double __shfl_down_sync(unsigned, double v, int) { return v; }
+#endif
 
 enum { ORACLE_OP_ADD, ORACLE_OP_SUB, ORACLE_OP_MUL, ORACLE_OP_DIV };
 

@@ -145,3 +145,42 @@ def get(tag):
     if tag not in _cache:
         _cache[tag] = Ref(tag)
     return _cache[tag]
+
+
+def block_available(tag):
+    return os.path.exists(os.path.join(REF_DIR, f"libgrnsref_block_{tag}.so"))
+
+
+class Block:
+    """The reference's n-threaded device functions run as one emulated thread
+    block on the CPU (oracle/ref/ref_block.cpp; sets with n a multiple of 32)."""
+
+    def __init__(self, tag):
+        self.L = ctypes.CDLL(os.path.join(REF_DIR, f"libgrnsref_block_{tag}.so"))
+        self.L.ref_block_init()
+        self.n = self.L.ref_block_n()
+
+    def eval(self, x):
+        x = np.ascontiguousarray(x, np.int32)
+        out = np.zeros(x.shape[0], IV_DTYPE)
+        self.L.ref_block_eval(_p(x), ctypes.c_long(x.shape[0]), _p(out))
+        return out
+
+    def cmp(self, x, y):
+        x, y = np.ascontiguousarray(x, np.int32), np.ascontiguousarray(y, np.int32)
+        out = np.zeros(x.shape[0], np.int32)
+        self.L.ref_block_cmp(_p(x), _p(y), ctypes.c_long(x.shape[0]), _p(out))
+        return out
+
+    def mrc(self, x):
+        x = np.ascontiguousarray(x, np.int32)
+        out = np.zeros_like(x)
+        self.L.ref_block_mrc(_p(x), ctypes.c_long(x.shape[0]), _p(out))
+        return out
+
+
+def block(tag):
+    key = ("block", tag)
+    if key not in _cache:
+        _cache[key] = Block(tag)
+    return _cache[key]

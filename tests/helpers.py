@@ -35,3 +35,9 @@ def mpint_dtype(n):
     off = ((4 * n + 4 + 7) // 8) * 8
     return np.dtype({"names": ["digits", "sign", "eval"], "formats": [("<i4", (n,)), "<i4", (ER_DTYPE, (2,))],
                      "offsets": [0, 4 * n, off], "itemsize": off + 32})
+
+
+def product_safe_bits(log2M):
+    """bit length of mp_int operands whose products stay below M (the
+    catalogue's smallest sets have M of 10 to 36 bits)"""
+    return log2M // 2 - 10 if log2M >= 40 else max(1, log2M // 2 - 1)

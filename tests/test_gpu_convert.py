@@ -102,12 +102,13 @@ def test_round_trip_and_partial_tiles(case):
 
 def test_invalid_residue_flagged(case):
     tag, ctx, orc, g = case
-    x = orc.exact.to_rns([12345, 678])
+    v = 12345 if orc.M > 12345 else orc.M - 3
+    x = orc.exact.to_rns([v, 678 % orc.M])
     x[1, 0] = orc.moduli[0]
     flags = torch.zeros(2, dtype=torch.uint8, device="cuda")
     got = ctx.rns_to_binary(to_dev(x, "aos"), layout="aos", flags=flags).cpu().numpy()
     assert list(flags.cpu().numpy()) == [0, 1]
-    assert G.limbs_to_ints(got) == [12345, 0]
+    assert G.limbs_to_ints(got) == [v, 0]
     with pytest.raises(RuntimeError):
         ctx.rns_to_binary(to_dev(x, "aos"), layout="aos", limbs=ctx.binary_limbs - 1)
 

@@ -9,7 +9,7 @@ import pytest
 
 from grns_gb300 import workload as W
 from oracle import oracle as O
-from tests.helpers import IV_DTYPE, TAGS, golden, moduli_for, mpint_dtype
+from tests.helpers import IV_DTYPE, TAGS, golden, moduli_for, mpint_dtype, product_safe_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -98,18 +98,20 @@ def test_eval_golden(case, layout):
         assert out.cpu().numpy().tobytes() == g["eval_dev"].tobytes()
 
 
-@pytest.mark.parametrize("split", [0, 5, 8])
+@pytest.mark.parametrize("split", [0, 4, 5, 8])
 def test_eval_pipe_split_same_bits(case, split):
-    """grns_eval with 0, 5 and 8 eighths of its warps on the FP64 pipe (the
-    rest on the integer pipe): the oracle's bits every time, the golden
-    vectors and fresh uniform numbers, the full and the fast form"""
+    """grns_eval with 0, 4, 5 and 8 eighths of its warps on the FP64 pipe
+    (the rest on the integer pipe; with both pipes in use and 2^16 numbers or
+    more, warps claim their numbers from a counter): the oracle's bits every
+    time, the golden vectors and fresh uniform numbers, the full and the fast
+    form"""
     from grns_gb300 import native
     tag, ctx, orc, g = case
     L = native.lib()
     native.check(L.grns_ctx_set_eval_split(ctx.handle, split))
     try:
         assert L.grns_ctx_get_eval_split(ctx.handle) == split
-        x = np.concatenate([g["x"], W.uniform_residues(orc.moduli, 20000, seed=77, stream=W.S_X, layout="aos")])
+        x = np.concatenate([g["x"], W.uniform_residues(orc.moduli, 70000, seed=77, stream=W.S_X, layout="aos")])
         got = ctx.rns_eval_compute(to_dev(x, "soa")).cpu().numpy()
         assert got.tobytes() == oracle_eval_device(ctx, orc, x).tobytes()
         P = O.PATH_DEVICE_FAST
@@ -154,7 +156,7 @@ def test_eval_random_bit_exact_and_enclosing(case, layout):
     # sprinkle small values (refinement loop) and values near M (ambiguity branch)
     rng = random.Random(5)
     small = [rng.randrange(1, 1 << rng.randrange(1, orc.log2M)) for _ in range(200)]
-    big = [orc.M - rng.randrange(1, 1 << 40) for _ in range(100)]
+    big = [orc.M - rng.randrange(1, min(1 << 40, orc.M)) for _ in range(100)]
     x = np.concatenate([x, orc.exact.to_rns(small + big)])
     flags = flags_buf(len(x))
     got = ctx.rns_eval_compute(to_dev(x, layout), layout=layout, flags=flags).cpu().numpy().view(IV_DTYPE)
@@ -228,14 +230,15 @@ def test_div_dividend_and_divisor_near_m(case, layout, path):
 
 def test_div_by_zero_flag(case, path):
     tag, ctx, orc, g = case
-    x = orc.exact.to_rns([12345, 7])
+    v = 12345 if orc.M > 12345 else orc.M - 3
+    x = orc.exact.to_rns([v, 7])
     d = orc.exact.to_rns([0, 7])
     flags = flags_buf(2)
     q, r = ctx.rns_div(to_dev(x, "aos"), to_dev(d, "aos"), layout="aos", flags=flags)
     f = flags.cpu().numpy()
     assert f[0] & 2 and f[1] == 0
     assert orc.exact.from_rns(q.cpu().numpy()) == [0, 1]
-    assert orc.exact.from_rns(r.cpu().numpy()) == [12345, 0]
+    assert orc.exact.from_rns(r.cpu().numpy()) == [v, 0]
 
 
 @pytest.mark.parametrize("layout", ["soa", "aos"])
@@ -271,9 +274,9 @@ def test_mpint(case, op):
     flags = flags_buf(len(g["mpint_a"]) // mpint_dtype(orc.n).itemsize)
     out = fn(a, b, flags=flags).cpu().numpy()
     assert out.tobytes() == g[f"mpint_{op}_dev"].tobytes()
-    # fresh operands: magnitudes below 2^(log2M/2 - 10), eval from the device path
-    vals_a = W.mpint_values(600, orc.log2M // 2 - 10, seed=13)
-    vals_b = W.mpint_values(600, orc.log2M // 2 - 10, seed=14)
+    # fresh operands: magnitudes whose products stay below M, eval from the device path
+    vals_a = W.mpint_values(600, product_safe_bits(orc.log2M), seed=13)
+    vals_b = W.mpint_values(600, product_safe_bits(orc.log2M), seed=14)
     ma, mb = orc.mpint_from_ints(vals_a), orc.mpint_from_ints(vals_b)
     out = fn(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda())
     got = out.cpu().numpy().view(mpint_dtype(orc.n))
@@ -396,7 +399,7 @@ def test_mrc(case, layout):
 
 def test_mpint_overflow_flag(case):
     tag, ctx, orc, g = case
-    big = orc.M // 2 + 12345
+    big = orc.M // 2 + min(12345, orc.M // 8)
     ma, mb = orc.mpint_from_ints([big, 3]), orc.mpint_from_ints([big, 4])
     flags = flags_buf(2)
     ctx.mpint_add(torch.from_numpy(ma.view(np.uint8)).cuda(), torch.from_numpy(mb.view(np.uint8)).cuda(), flags=flags)
@@ -480,7 +483,7 @@ def test_eval_tight(case, layout):
     tag, ctx, orc, g = case
     M = orc.exact.M
     rng = random.Random(7)
-    vals = [rng.randrange(M) for _ in range(1500)] + [0, 1, M - 1, M // 2] + [rng.randrange(M >> 40) for _ in range(60)]
+    vals = [rng.randrange(M) for _ in range(1500)] + [0, 1, M - 1, M // 2] + [rng.randrange(max(1, M >> 40)) for _ in range(60)]
     x = to_dev(W.to_residues(vals, moduli_for(tag), layout="aos"), layout)
     tight = ctx.rns_eval_tight(x, layout=layout).cpu().numpy().view(IV_DTYPE)
     ref = ctx.rns_eval_compute(x, layout=layout).cpu().numpy().view(IV_DTYPE)

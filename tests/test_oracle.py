@@ -197,3 +197,23 @@ def test_oracle_vs_reference_build(tag):
     for dev, code in ((True, O.PATH_DEVICE), (False, O.PATH_HOST)):
         assert ref.eval(x, dev=dev).tobytes() == orc.eval(x, path=code).tobytes()
         assert np.array_equal(ref.cmp(x, y, dev=dev), orc.cmp(x, y, path=code))
+
+
+@pytest.mark.parametrize("tag", ["g32", "p32", "g64", "p64"])
+def test_parallel_order_pinned_on_reference_block_code(tag):
+    """rns_eval_compute_parallel (src/rnseval.cuh:332) executed as one thread
+    block of the reference's own code on the CPU (one host thread per CUDA
+    thread, oracle/ref/ref_block.cpp) gives the oracle's n-threaded order
+    (eval_dpar) bit for bit -- the order the device header's
+    rns_eval_compute_parallel follows on the GPU; rns_cmp_parallel and
+    mrc_pipeline give the serial results"""
+    if not refcheck.block_available(tag):
+        pytest.skip("reference block checker not built (no reference checkout)")
+    orc, g, blk = O.Oracle(moduli_for(tag)), golden(tag), refcheck.block(tag)
+    x = g["x"] if orc.n <= 32 else g["x"][:40]  # the special values lead the fixture
+    got = blk.eval(x)
+    assert got.tobytes() == orc.eval(x, path=O.PATH_DEVICE_PARALLEL).tobytes()
+    assert (got != orc.eval(x, path=O.PATH_DEVICE)).any()  # the order differs from the serial tree's
+    k = 8
+    assert list(blk.cmp(x[:k], g["y"][:k])) == list(orc.cmp(x[:k], g["y"][:k], path=O.PATH_DEVICE))
+    assert np.array_equal(blk.mrc(x), orc.mrc(x, path=O.PATH_DEVICE))
