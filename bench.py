@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 N32 = 32
 PAIRS = 1 << 18
-DIV_TRAFFIC_BYTES = 328.2e6  # DRAM bytes of one 2^18-pair division call (ncu, three launches)
+DIV_TRAFFIC_BYTES = 446.3e6  # DRAM bytes of one 2^18-pair division call (ncu, five launches, each cold)
 CONV_COUNT = 1 << 22  # numbers per binary <-> RNS conversion call
 CMP_PAIRS = 1 << 20
 EVAL_COUNT = 1 << 22
@@ -919,12 +919,13 @@ def main():
                    "streams": "the division and the scaling of a step on two streams at once (independent); "
                               "kernels_ms are each one's span on its stream while they share the GPU",
                    "l2": "flushed (256 MiB write) between timed steps", "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "k_div_a<32> + k_div_place + k_div_b<32> + k_div_out<32> (one division call)",
+        "roofline": {"bound": "hbm", "kernel": "k_div_a<32> + k_div_rows<32> + k_div_place + k_div_b<32> + k_div_out<32> "
+                                               "(one division call)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": DIV_TRAFFIC_BYTES,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three launches of "
-                                       "one call, profiles/k_div_n32_262144pairs.md",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the five launches of "
+                                       "one call, each captured cold, profiles/k_div_n32_262144pairs.md",
                      "note": "division is integer-pipe bound (48-bit digit steps); the HBM-bound kernels "
                              "(eval, cmp, max, mp_int) carry their own fractions in extra"},
         "kernels_ms": {"division": div_avg, "k_scale_warp": statistics.mean(scale_ms),
@@ -933,7 +934,7 @@ def main():
         "e2e": {"value": e2e, "unit": "Mnum/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "grns_div_host + grns_scale2pow_host (pinned host arrays, chunked copy/compute "
                        "overlap), the two on two streams", "matches_device_results": e2e_ok},
-        "gpu_launches": 5 * args.steps,  # per step: k_div_a, k_div_place, k_div_b, k_div_out, k_scale_warp
+        "gpu_launches": 6 * args.steps,  # per step: k_div_a, k_div_rows, k_div_place, k_div_b, k_div_out, k_scale_warp
         "extra": extra,
         "workloads": workloads,
     }

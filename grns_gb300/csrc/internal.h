@@ -122,12 +122,14 @@ grns_status launch_cmp(const grns_ctx *c, const uint32_t *x, const uint32_t *y, 
                        int32_t *out, uint8_t *flags, cudaStream_t s);
 /* min_per_warp > 0 launches fewer warps when that gives each warp at least
  * min_per_warp numbers (better balance inside a warp's range; the kernel then
- * leaves SMs free for a concurrent launch) */
+ * leaves SMs free for a concurrent launch); ld_out: the outputs' leading
+ * dimension (SoA; -1: ld, 0 when the inputs are AoS) */
 grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
-                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp = 0);
+                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp = 0,
+                       int64_t ld_out = -1);
 grns_status launch_scale2pow(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t D_uniform,
                              int64_t ld, int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s,
-                             int min_per_warp = 0);
+                             int min_per_warp = 0, int64_t ld_out = -1);
 grns_status launch_mpint(const grns_ctx *c, int op, const void *x, const void *y, int64_t count, void *out,
                          uint8_t *flags, cudaStream_t s);
 grns_status launch_max(grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out_value,

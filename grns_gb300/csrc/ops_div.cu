@@ -224,6 +224,110 @@ __global__ void __launch_bounds__(kDivBlock, N > 32 ? 4 : 6)
                    hist + (threadIdx.x / 32) * kDivBins);
 }
 
+/* floor(X / 2^D) in one pass (scale_bin, rns_fast.cuh) for n <= 32: a warp
+ * takes a contiguous range of numbers, orders it by chunk count (longest
+ * first, so the 32 lanes of a group run similar loops) and scales 32 numbers
+ * at a time, one per lane.  The chunk tables (M_i and 2^(26 c) mod m_i in
+ * 26-bit chunks, rows of bin_ld(N) words) sit in shared memory and are read
+ * as 16-byte broadcasts; the residues' products s_i and the n 64-bit
+ * accumulators stay in registers. */
+constexpr int kScaleBinBlock = 128;
+
+template <int N>
+__device__ __forceinline__ int scale_bin_chunks(const Consts<N> &C, unsigned D) {
+    return D > (unsigned)C.log2M ? 0 : (int)((D + kBinChunk - 1) / kBinChunk);
+}
+
+template <int N>
+size_t scale_bin_smem(const Consts<N> &C) {
+    return (size_t)C.bin_chunks * bin_ld(N) * 4 * 2 + (size_t)((C.bin_chunks + 3) / 4) * 16 +
+           (size_t)(kScaleBinBlock / 32) * kDivBins * 4;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kScaleBinBlock) k_scale_bin(const __grid_constant__ Consts<N> C, Operand<N> x,
+                                                              const uint32_t *__restrict__ Darr, uint32_t D_uniform,
+                                                              int32_t *__restrict__ order, int64_t count,
+                                                              int64_t per_warp, Output<N> out,
+                                                              uint8_t *__restrict__ flags) {
+    extern __shared__ uint4 sb_smem[];
+    constexpr int L4 = bin_ld(N) / 4;
+    const int chunks = C.bin_chunks, m4 = (chunks + 3) / 4;
+    uint4 *MI4 = sb_smem;             // [chunks][L4]  26-bit chunk c of M_i
+    uint4 *P4 = MI4 + chunks * L4;    // [chunks][L4]  2^(26 c) mod m_i
+    uint32_t *M26 = reinterpret_cast<uint32_t *>(P4 + chunks * L4);  // [m4 * 4] chunks of M
+    uint32_t *hist = M26 + m4 * 4;
+    for (int w = threadIdx.x; w < chunks * L4; w += blockDim.x) {
+        MI4[w] = reinterpret_cast<const uint4 *>(C.bin_mi26)[w];
+        P4[w] = reinterpret_cast<const uint4 *>(C.bin_p26)[w];
+    }
+    for (int w = threadIdx.x; w < m4 * 4; w += blockDim.x) M26[w] = C.bin_m26[w];
+    __syncthreads();
+    const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t b = wi * per_warp;
+    if (b >= count) return;  // whole warp
+    const int64_t e = b + per_warp < count ? b + per_warp : count;
+    if (Darr) {
+        lpt_order([&](int64_t k) { return min(kDivBins - 1, scale_bin_chunks<N>(C, __ldg(Darr + k))); }, order, b, e,
+                  hist + (threadIdx.x / 32) * kDivBins);
+    }
+    const int lane = threadIdx.x & 31;
+    for (int64_t p = b + lane; p < e; p += 32) {
+        const int64_t idx = Darr ? b + order[p] : p;
+        const unsigned D = Darr ? __ldg(Darr + idx) : D_uniform;
+        uint32_t s[4 * L4], bad = 0;
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            const uint32_t v = x.load(idx, i);
+            bad |= (uint32_t)(v >= C.m[i]);
+            s[i] = mulmod_shoup(v, C.w[i], C.w_sh[i], C.m[i]);
+        }
+#pragma unroll
+        for (int i = N; i < 4 * L4; i++) s[i] = 0;
+        if (flags) flags[idx] = bad ? (uint8_t)kFlagInvalidInput : (uint8_t)0;
+        if (bad || D > (unsigned)C.log2M || D == 0) {  // invalid or 2^D > X: 0; D = 0: X
+#pragma unroll 4
+            for (int i = 0; i < N; i++) out.store(idx, i, (bad || D) ? 0u : x.load(idx, i));
+            continue;
+        }
+        const uint32_t kk = scale_bin_rank<N>(C, [&](int i) { return s[i]; }, [&](int i) { return x.load(idx, i); });
+        const int nch = (int)((D + kBinChunk - 1) / kBinChunk);
+        const uint32_t top = D % kBinChunk ? (1u << (D % kBinChunk)) - 1u : kBinMask;
+        uint64_t acc[4 * L4];
+#pragma unroll
+        for (int i = 0; i < 4 * L4; i++) acc[i] = 0;
+        int64_t carry = 0;
+#pragma unroll 1
+        for (int c = 0; c < nch; c++) {
+            const uint4 *t = MI4 + c * L4;
+            uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+            for (int q = 0; q < L4; q++) {
+                const uint4 v = t[q];
+                a0 += (uint64_t)s[4 * q] * v.x;
+                a1 += (uint64_t)s[4 * q + 1] * v.y;
+                a2 += (uint64_t)s[4 * q + 2] * v.z;
+                a3 += (uint64_t)s[4 * q + 3] * v.w;
+            }
+            const int64_t v = (int64_t)((a0 + a1) + (a2 + a3)) - (int64_t)kk * M26[c] + carry;
+            carry = v >> kBinChunk;  // floor division (arithmetic shift)
+            const uint32_t r = (uint32_t)v & (c == nch - 1 ? top : kBinMask);
+            const uint4 *pp = P4 + c * L4;
+#pragma unroll
+            for (int q = 0; q < L4; q++) {
+                const uint4 w = pp[q];
+                acc[4 * q] += (uint64_t)r * w.x;
+                acc[4 * q + 1] += (uint64_t)r * w.y;
+                acc[4 * q + 2] += (uint64_t)r * w.z;
+                acc[4 * q + 3] += (uint64_t)r * w.w;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < N; i++)
+            out.store(idx, i, scale_bin_finish<N>(C, i, x.load(idx, i), bin_mod64<N>(C, i, acc[i]), D));
+    }
+}
+
 template <int N, bool FAST>
 __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N> C, Operand<N> x,
                                                const uint32_t *__restrict__ D, uint32_t D_uniform, int64_t count,
@@ -252,11 +356,11 @@ __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N>
 
 template <int N>
 grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count, uint32_t *q,
-                    uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp) {
+                    uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp, int64_t ldo) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
         k_div<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
-                                                               count, Output<N>{q, ld}, Output<N>{r, ld}, flags);
+                                                               count, Output<N>{q, ldo}, Output<N>{r, ldo}, flags);
         return cuda_status(cudaGetLastError());
     }
     /* fast path (div_warp.cuh): pass A writing records, the rows, the longest-first order
@@ -297,6 +401,7 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
     for (int64_t c0 = 0; c0 < count && e == cudaSuccess; c0 += chunk) {
         const int64_t n = count - c0 < chunk ? count - c0 : chunk;
         const int64_t off = ld ? c0 : c0 * N;  // first number of the chunk (SoA columns keep the leading dimension)
+        const int64_t offo = ldo ? c0 : c0 * N;
         const Operand<N> X{x + off, ld}, Dv{d + off, ld};
         uint8_t *fl = flags ? flags + c0 : nullptr;
         e = cudaMemsetAsync(G, 0, sizeof(DivRowsG), s);
@@ -320,7 +425,7 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
         }
         if (e == cudaSuccess) {
             k_div_out<N><<<grid_for(c, (n + kDivOutTile - 1) / kDivOutTile, 1, 8), 256, 0, s>>>(
-                rows, n, Output<N>{q + off, ld}, Output<N>{r + off, ld});
+                rows, n, Output<N>{q + offo, ldo}, Output<N>{r + offo, ldo});
             e = cudaGetLastError();
         }
     }
@@ -329,15 +434,50 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
 }
 
 template <int N>
+grns_status run_scale_steps(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
+                            int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp,
+                            int64_t ldo);
+
+template <int N>
 grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld, int64_t count,
-                      uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp) {
+                      uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp, int64_t ldo) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
         k_scale<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
-                                                                 Output<N>{out, ld}, flags);
+                                                                 Output<N>{out, ldo}, flags);
         return cuda_status(cudaGetLastError());
     }
-    /* fast path: warps over contiguous ranges (scale_warp.cuh) */
+    if constexpr (N <= 32) {  /* one pass over the chunks of X mod 2^D */
+        const size_t smem = scale_bin_smem<N>(consts_of<N>(c));
+        static std::atomic<int> per_sm_bin[kOccDevices];
+        const int occ = resident_blocks(per_sm_bin, c, k_scale_bin<N>, kScaleBinBlock, smem);
+        const int64_t warps_cap = (int64_t)c->sm_count * occ * (kScaleBinBlock / 32);
+        int64_t warps = (count + 63) / 64;  // ranges of 64 numbers or more: two lane groups to order
+        if (min_per_warp > 0 && warps > (count + min_per_warp - 1) / min_per_warp)
+            warps = (count + min_per_warp - 1) / min_per_warp;
+        if (warps > warps_cap) warps = warps_cap;
+        if (warps < 1) warps = 1;
+        const int64_t per_warp = (count + warps - 1) / warps;
+        const unsigned grid = (unsigned)((warps * 32 + kScaleBinBlock - 1) / kScaleBinBlock);
+        int32_t *order = nullptr;
+        cudaError_t e = cudaSuccess;
+        if (D) e = scratch_alloc(c, (void **)&order, (size_t)count * sizeof(int32_t), s);
+        if (e != cudaSuccess) return cuda_status(e);
+        k_scale_bin<N><<<grid, kScaleBinBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, order, count,
+                                                         per_warp > 0 ? per_warp : 1, Output<N>{out, ldo}, flags);
+        e = cudaGetLastError();
+        if (order) scratch_free(order, s);
+        return cuda_status(e);
+    } else {
+        return run_scale_steps<N>(c, x, D, Du, ld, count, out, flags, s, min_per_warp, ldo);
+    }
+}
+
+/* n = 64: exact 52-bit steps, warps over contiguous ranges (scale_warp.cuh) */
+template <int N>
+grns_status run_scale_steps(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
+                            int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp,
+                            int64_t ldo) {
     const size_t smem = scale_smem_bytes<N>(kDivBlock);
     static std::atomic<int> per_sm[kOccDevices];  // resident blocks per SM, per device
     const int occ = resident_blocks(per_sm, c, k_scale_warp<N>, kDivBlock, smem);
@@ -354,7 +494,7 @@ grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, u
     if (D) e = scratch_alloc(c, (void **)&order, (size_t)count * sizeof(int32_t), s);
     if (e != cudaSuccess) return cuda_status(e);
     k_scale_warp<N><<<grid, kDivBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, order, count,
-                                                  per_warp > 0 ? per_warp : 1, Output<N>{out, ld}, flags);
+                                                  per_warp > 0 ? per_warp : 1, Output<N>{out, ldo}, flags);
     e = cudaGetLastError();
     if (order) scratch_free(order, s);
     return cuda_status(e);
@@ -372,9 +512,9 @@ size_t div_scratch_of(int64_t count) {
 /* the per-count entry points: extern here, instantiated for this unit's counts */
 #define GRNS_DIV_ROOTS_(n, EXT)                                                                                      \
     EXT template grns_status run_div<n>(const grns_ctx *, const uint32_t *, const uint32_t *, int64_t, int64_t,        \
-                                        uint32_t *, uint32_t *, uint8_t *, cudaStream_t, int);                       \
+                                        uint32_t *, uint32_t *, uint8_t *, cudaStream_t, int, int64_t);              \
     EXT template grns_status run_scale<n>(const grns_ctx *, const uint32_t *, const uint32_t *, uint32_t, int64_t,     \
-                                          int64_t, uint32_t *, uint8_t *, cudaStream_t, int);                        \
+                                          int64_t, uint32_t *, uint8_t *, cudaStream_t, int, int64_t);               \
     EXT template size_t div_scratch_of<n>(int64_t);
 #define GRNS_EXTERN_(n) GRNS_DIV_ROOTS_(n, extern)
 #define GRNS_DEFINE_(n) GRNS_DIV_ROOTS_(n, )
@@ -391,15 +531,18 @@ size_t div_scratch_bytes(const grns_ctx *c, int64_t count) {
 }
 
 grns_status launch_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int64_t ld, int64_t count,
-                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp) {
-#define C_(n) return run_div<n>(c, x, d, ld, count, q, r, flags, s, min_per_warp)
+                       uint32_t *q, uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp, int64_t ld_out) {
+    const int64_t ldo = ld_out < 0 ? ld : ld_out;
+#define C_(n) return run_div<n>(c, x, d, ld, count, q, r, flags, s, min_per_warp, ldo)
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }
 
 grns_status launch_scale2pow(const grns_ctx *c, const uint32_t *x, const uint32_t *D, uint32_t Du, int64_t ld,
-                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp) {
-#define C_(n) return run_scale<n>(c, x, D, Du, ld, count, out, flags, s, min_per_warp)
+                             int64_t count, uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp,
+                             int64_t ld_out) {
+    const int64_t ldo = ld_out < 0 ? ld : ld_out;
+#define C_(n) return run_scale<n>(c, x, D, Du, ld, count, out, flags, s, min_per_warp, ldo)
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }

@@ -25,6 +25,7 @@
 #include <cmath>
 
 #include "rns_common.cuh"
+#include "rns_convert.cuh"
 
 namespace grns {
 
@@ -1077,6 +1078,66 @@ GRNS_HD void scale_fast(const Consts<N> &C, uint32_t *res, const uint32_t *x, un
     }
 #pragma unroll
     for (int i = 0; i < N; i++) res[i] = cur[i];
+}
+
+/* ---------------- power-of-two scaling in one pass ----------------
+ *
+ * floor(X / 2^D) = (X - (X mod 2^D)) 2^-D mod M (M odd).  With the exact rank
+ * k, X = sum_i s_i M_i - k M (s_i = x_i w_i mod m_i), so the low D bits of X
+ * are the low 26-bit chunks of that sum (the CRT weights M_i and M in 26-bit
+ * chunks, the binary conversion's tables), carried chunk by chunk; each chunk
+ * r_c of X mod 2^D enters every residue as r_c (2^(26 c) mod m_i).  Work
+ * grows with D / 26 (two n-term sums per chunk) instead of one rank and two
+ * passes over the residues per 52-bit step. */
+
+/* exact rank of X (the fixed-point estimate, decided by mixed radix when
+ * the fraction lies within E of an integer) */
+template <int N, class GetS, class GetX>
+GRNS_HD uint32_t scale_bin_rank(const Consts<N> &C, GetS gs, GetX gx) {
+    const u128 t = fx96_s<N>(C, gs);
+    const uint32_t kk = (uint32_t)(t >> 96);
+    if ((t & kMask96) >= (u128)C.E) return kk;
+    uint32_t a[N];
+    mrc_hd<N>(C, gx, a);
+    return a[N - 1] == 0 ? kk : kk - 1;
+}
+
+/* (x_i - r_i) 2^-D mod m_i from r_i = (X mod 2^D) mod m_i */
+template <int N>
+GRNS_HD uint32_t scale_bin_finish(const Consts<N> &C, int i, uint32_t x, uint32_t r, unsigned D) {
+    const uint32_t m = C.m[i];
+    const uint2 lo = ldg_u2(C.p2nlo + (int64_t)i * 64 + (D & 63u));
+    const uint2 hi = ldg_u2(C.p2nhi + (int64_t)i * C.p2rows + (D >> 6));
+    return mulmod_shoup(mulmod_shoup(submod(x, r, m), lo.x, lo.y, m), hi.x, hi.y, m);
+}
+
+template <int N>
+GRNS_HD void scale_bin(const Consts<N> &C, uint32_t *res, const uint32_t *x, unsigned D) {
+    if (D > (unsigned)C.log2M || D == 0) {  // X < M < 2^(log2M + 1): 0; D = 0: X
+        for (int i = 0; i < N; i++) res[i] = D ? 0u : x[i];
+        return;
+    }
+    uint32_t s[N];
+    uint64_t acc[N];
+    for (int i = 0; i < N; i++) {
+        s[i] = mulmod_shoup(x[i], C.w[i], C.w_sh[i], C.m[i]);
+        acc[i] = 0;
+    }
+    const uint32_t kk = scale_bin_rank<N>(C, [&](int i) { return s[i]; }, [&](int i) { return x[i]; });
+    const int chunks = (int)((D + kBinChunk - 1) / kBinChunk);
+    int64_t carry = 0;
+    for (int c = 0; c < chunks; c++) {
+        uint64_t a = 0;
+        const uint32_t *mi = C.bin_mi26 + (size_t)c * bin_ld(N);
+        for (int i = 0; i < N; i++) a += (uint64_t)s[i] * mi[i];
+        const int64_t v = (int64_t)a - (int64_t)kk * C.bin_m26[c] + carry;
+        carry = v >> kBinChunk;  // floor division (arithmetic shift)
+        uint32_t r = (uint32_t)v & kBinMask;
+        if (c == chunks - 1 && D % kBinChunk) r &= (1u << (D % kBinChunk)) - 1u;
+        const uint32_t *p = C.bin_p26 + (size_t)c * bin_ld(N);
+        for (int i = 0; i < N; i++) acc[i] += (uint64_t)r * p[i];
+    }
+    for (int i = 0; i < N; i++) res[i] = scale_bin_finish<N>(C, i, x[i], bin_mod64<N>(C, i, acc[i]), D);
 }
 
 }  // namespace grns

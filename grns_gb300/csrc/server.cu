@@ -17,7 +17,13 @@
  *     waited kPassCapUs: then nothing is admitted past it, so freed memory
  *     goes to it.  With several slots, requests arriving while launches are
  *     in flight are admitted and launched alongside them, so their work
- *     overlaps on the device;
+ *     overlaps on the device.  Requests of direct_min_count numbers or more
+ *     (eval, cmp, div, scale2pow, mp_int add/sub/mul) run in the same launch round
+ *     through the per-op kernels instead, after the packed kernel on the same
+ *     stream: the dedicated kernels (the division's prepared rows, the
+ *     one-pass scaling, the claimed evaluation) are faster than the packed
+ *     kernel's general forms once a request fills the GPU by itself, and
+ *     packing pays for the many small ones;
  *   - marks requests done from a host callback at the end of each launch and
  *     records submit-to-completion latency (p50/p99 in grns_server_stats).
  * Each array counts the unfinished requests that read it (counted at
@@ -48,6 +54,7 @@ using Clock = std::chrono::steady_clock;
 constexpr double kPassCapUs = 50e3;          // after this wait for memory, later requests stop passing one
 constexpr double kKeepFinishedUs = 60e6;     // finished requests stay readable this long
 constexpr size_t kKeepFinishedMax = 1 << 16; // and at most this many of them
+constexpr int32_t kDirectMinDefault = 1 << 18;  // default of grns_server_options.direct_min_count
 
 double now_us() {
     return std::chrono::duration<double, std::micro>(Clock::now().time_since_epoch()).count();
@@ -72,6 +79,7 @@ struct Req {
     uint64_t out0 = 0, out1 = 0;
     size_t footprint = 0;
     int64_t count = 0;
+    bool direct = false;  // runs through the per-op kernels (direct_min_count)
     double t_submit = 0, t_done = 0;
     uint64_t reads[4] = {0, 0, 0, 0};  // arrays whose reader count this request holds
 };
@@ -202,6 +210,51 @@ size_t footprint_of(const grns_server *sv, const Req &q) {
     }
 }
 
+/* whether a request runs through the per-op kernels: large enough, and
+ * shaped as they take it (one leading dimension for inputs and outputs) */
+bool direct_request(const grns_server *sv, const Req &q) {
+    const int32_t thr = sv->opt.direct_min_count == 0 ? kDirectMinDefault : sv->opt.direct_min_count;
+    if (thr < 0 || q.count < thr) return false;
+    switch (q.r.op) {
+        case GRNS_OP_EVAL:
+        case GRNS_OP_CMP:
+        case GRNS_OP_DIV:
+        case GRNS_OP_SCALE2POW:
+        case GRNS_OP_MPINT_ADD:
+        case GRNS_OP_MPINT_SUB:
+        case GRNS_OP_MPINT_MUL: return true;
+        default: return false;
+    }
+}
+
+/* device scratch of a request run through the per-op kernels */
+size_t direct_scratch(const grns_server *sv, const Req &q) {
+    const grns_ctx *c = sv->ctxs[q.r.ctx_index];
+    switch (q.r.op) {
+        case GRNS_OP_DIV: return grns::div_scratch_bytes(c, q.count);
+        case GRNS_OP_SCALE2POW: return q.r.b ? 4 * (size_t)q.count : 0;  // the longest-first order
+        default: return 256;                                                 // the evaluation's claim counter
+    }
+}
+
+/* one request through the per-op kernels on stream s (the plain calls'
+ * launches); SoA outputs are dense (leading dimension count) like the
+ * packed kernel's */
+grns_status run_direct(const grns_ctx *c, const grns_job &j, cudaStream_t s) {
+    const uint32_t *a = (const uint32_t *)j.a, *b = (const uint32_t *)j.b;
+    const bool soa = j.layout == GRNS_LAYOUT_SOA;
+    const int64_t ld = soa ? j.ld : 0, ldo = soa ? j.count : 0;
+    switch (j.op) {
+        case GRNS_OP_EVAL: return grns::launch_eval(c, a, ld, j.count, (interval_t *)j.out0, nullptr, s);
+        case GRNS_OP_CMP: return grns::launch_cmp(c, a, b, ld, j.count, (int32_t *)j.out0, nullptr, s);
+        case GRNS_OP_DIV:
+            return grns::launch_div(c, a, b, ld, j.count, (uint32_t *)j.out0, (uint32_t *)j.out1, nullptr, s, 0, ldo);
+        case GRNS_OP_SCALE2POW:
+            return grns::launch_scale2pow(c, a, b, j.D_uniform, ld, j.count, (uint32_t *)j.out0, nullptr, s, 0, ldo);
+        default: return grns::launch_mpint(c, j.op - GRNS_OP_MPINT_ADD, j.a, j.b, j.count, j.out0, nullptr, s);
+    }
+}
+
 /* scheduler: completions, admission, packing, launch (caller holds mu) */
 void schedule_locked(grns_server *sv) {
     for (Slot *sl : sv->slots) {
@@ -242,8 +295,9 @@ void schedule_locked(grns_server *sv) {
     for (Slot *sl : sv->slots) {
         if (sl->busy || sv->pending.empty()) continue;
         int ctx = -1;  // the moduli set of this launch: that of the oldest request admitted
-        std::vector<grns_job> jobs;
-        for (auto it = sv->pending.begin(); it != sv->pending.end() && (int)jobs.size() < sv->opt.max_jobs_per_launch;) {
+        std::vector<grns_job> jobs, direct;  // packed into the batched kernel / through the per-op kernels
+        for (auto it = sv->pending.begin();
+             it != sv->pending.end() && (int)(jobs.size() + direct.size()) < sv->opt.max_jobs_per_launch;) {
             const uint64_t id = *it;
             Req &q = sv->reqs.at(id);
             if (ctx >= 0 && q.r.ctx_index != ctx) {
@@ -341,11 +395,16 @@ void schedule_locked(grns_server *sv) {
             if (q.r.op == GRNS_OP_EVAL && q.count == A.count) sv->arrays[q.r.a].eval = q.out0;
             q.state = 1;
             sl->reqs.push_back(id);
-            jobs.push_back(j);
+            if (q.direct && !j.eval_a) direct.push_back(j);  // cached evaluations: the packed kernel reads them
+            else jobs.push_back(j);
         }
-        if (jobs.empty()) continue;
+        if (jobs.empty() && direct.empty()) continue;
         grns::NvtxRange range("grns_server launch");
-        grns_status st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
+        grns_status st = GRNS_OK;
+        if (!jobs.empty())
+            st = grns::batch_run_async(sv->ctxs[ctx], jobs.data(), (int)jobs.size(), sl->staging, sl->s);
+        for (const grns_job &j : direct)
+            if (st == GRNS_OK) st = run_direct(sv->ctxs[ctx], j, sl->s);
         if (st == GRNS_OK) st = grns::cuda_status(cudaLaunchHostFunc(sl->s, on_launch_done, sl));
         if (st != GRNS_OK) {
             for (uint64_t id : sl->reqs) finish(sv, id, sv->reqs.at(id), st, now_us());
@@ -354,7 +413,7 @@ void schedule_locked(grns_server *sv) {
         }
         sl->busy = true;
         sv->launches++;
-        sv->jobs_launched += jobs.size();
+        sv->jobs_launched += jobs.size() + direct.size();
     }
 }
 
@@ -570,6 +629,8 @@ grns_status grns_server_submit(grns_server *sv, const grns_request *r, uint64_t 
     q.r = *r;
     q.count = count;
     q.footprint = footprint_of(sv, q);
+    q.direct = direct_request(sv, q);
+    if (q.direct) q.footprint += direct_scratch(sv, q);
     q.t_submit = now_us();
     if (sv->t_first == 0) sv->t_first = q.t_submit;
     *request_id = id;

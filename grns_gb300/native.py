@@ -99,7 +99,7 @@ class Schedule(ctypes.Structure):
 class ServerOptions(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", c_size_t), ("launch_slots", ctypes.c_int32),
                 ("max_jobs_per_launch", ctypes.c_int32), ("admission_timeout_ms", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("alloc_cap_bytes", c_size_t)]
+                ("direct_min_count", ctypes.c_int32), ("alloc_cap_bytes", c_size_t)]
 
 
 class Request(ctypes.Structure):

@@ -12,9 +12,11 @@ OPS = {"eval": 0, "cmp": 1, "div": 2, "scale2pow": 3, "max": 4, "mpint_add": 5, 
 
 
 class Server:
-    def __init__(self, budget_bytes=0, slots=4, max_jobs=256, admission_timeout_ms=0, alloc_cap_bytes=0):
+    def __init__(self, budget_bytes=0, slots=4, max_jobs=256, admission_timeout_ms=0, alloc_cap_bytes=0,
+                 direct_min_count=0):
         self.L = native.lib()
-        opt = native.ServerOptions(budget_bytes, slots, max_jobs, admission_timeout_ms, 0, alloc_cap_bytes)
+        opt = native.ServerOptions(budget_bytes, slots, max_jobs, admission_timeout_ms, direct_min_count,
+                                   alloc_cap_bytes)
         h = ctypes.c_void_p()
         check(self.L.grns_server_create(ctypes.byref(opt), ctypes.byref(h)), "grns_server_create")
         self.h = h

@@ -374,7 +374,11 @@ typedef struct {
     int32_t max_jobs_per_launch; /* 0: 256 */
     int32_t admission_timeout_ms;/* a request not admitted within this time completes with
                                     GRNS_ERR_REJECTED (0: 10000) */
-    int32_t reserved;
+    int32_t direct_min_count;    /* requests of at least this many numbers run through the per-op
+                                    kernels (the plain calls' launches, on the launch's stream)
+                                    instead of inside the packed batched kernel: eval, cmp (unless
+                                    both evaluations are cached), div, scale2pow, mp_int
+                                    add/sub/mul.  0: 262144; negative: never */
     size_t alloc_cap_bytes;      /* hard cap on the device memory the server holds (0: none): a put
                                     beyond it returns, and an admitted request beyond it completes
                                     with, GRNS_ERR_OUT_OF_MEMORY; the server goes on */

@@ -76,6 +76,14 @@ int fc_scale(void *p, const uint32_t *x, const uint32_t *D, long cnt, uint32_t *
     return 0;
 }
 
+int fc_scale_bin(void *p, const uint32_t *x, const uint32_t *D, long cnt, uint32_t *out) {
+    Box *b = (Box *)p;
+#define C_(N) for (long k = 0; k < cnt; k++) scale_bin<N>(K<N>(b), out + k * N, x + k * N, D[k])
+    DISPATCH(b->n, C_)
+#undef C_
+    return 0;
+}
+
 /* fixed-point sums for direct checks: frac64 = fx64, and the 128-bit fx96 total */
 int fc_fx(void *p, const uint32_t *x, long cnt, uint64_t *f64, uint64_t *f96lo, uint64_t *f96hi) {
     Box *b = (Box *)p;

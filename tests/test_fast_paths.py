@@ -79,6 +79,10 @@ class FC:
         s = np.asarray(S, np.uint32)
         out = np.zeros_like(x)
         self.L.fc_scale(self.h, self.P(x), self.P(s), ctypes.c_long(len(X)), self.P(out))
+        # the one-pass form (the low D bits of X from the CRT sum in 26-bit chunks) agrees
+        out2 = np.zeros_like(x)
+        self.L.fc_scale_bin(self.h, self.P(x), self.P(s), ctypes.c_long(len(X)), self.P(out2))
+        assert np.array_equal(out, out2)
         return self.ints(out)
 
     def from_binary(self, vals, limbs):
@@ -210,6 +214,25 @@ def test_division_remainder_evaluation_wraps(fc, tag):
     assert q == [a // b for a, b in zip(X, Dv)]
     assert r == [a % b for a, b in zip(X, Dv)]
     assert not fl.any()
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_scaling_every_shift(fc, tag):
+    """floor(X / 2^D) for every D from 0 to log2M + 2 (the one-pass form's
+    last chunk is partial unless 26 divides D) on values at the edges: M - 1,
+    powers of two and their neighbours, values with long runs of ones"""
+    f = FC(fc, moduli_for(tag))
+    M = f.M
+    L = M.bit_length() - 1
+    rng = random.Random(31)
+    base = [M - 1, M - 2, (1 << L) - 1, 1 << L, (M - 1) // 2, 1, 3, rng.randrange(M), rng.randrange(M)]
+    base += [(1 << b) - 1 for b in range(26, L, 26)] + [1 << b for b in range(25, L, 26)]
+    X, S = [], []
+    for d in range(0, L + 3):
+        for v in base[:5] + [base[(d * 7) % len(base)]]:
+            X.append(v % M)
+            S.append(d)
+    assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
 
 
 @pytest.mark.parametrize("tag", ["ref8", "g8", "g32", "g64", "p16", "p32", "p64"])

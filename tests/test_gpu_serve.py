@@ -112,10 +112,14 @@ def server_bytes(srv, rid, op, n):
     return out
 
 
-def test_results_alone_and_in_the_mix(env):
+@pytest.mark.parametrize("direct", [-1, 5000])
+def test_results_alone_and_in_the_mix(env, direct):
+    """direct = -1: every request inside the packed kernel; 5000: requests of
+    5000 numbers or more (whole arrays for div and scale2pow) through the
+    per-op kernels in the same launch rounds"""
     G, native, ctxs = env
     from grns_gb300.serve import Server
-    srv = Server(slots=4, max_jobs=64)
+    srv = Server(slots=4, max_jobs=64, direct_min_count=direct)
     try:
         arrays = {}
         for n, ctx in ctxs.items():
@@ -143,7 +147,8 @@ def test_results_alone_and_in_the_mix(env):
             n = rng.choice([32, 64])
             A = arrays[n]
             op = rng.choice(["eval", "cmp", "div", "scale2pow", "max", "mpint_mul"])
-            count = rng.choice([1, 7, 100, 1000, 10000, A["cnt"]]) if op not in ("div",) else rng.choice([1, 50, 2000])
+            count = rng.choice([1, 7, 100, 1000, 10000, A["cnt"]]) if op not in ("div",) else \
+                rng.choice([1, 50, 2000, A["cnt"]])
             a = A["hma"] if op == "mpint_mul" else A["hx"]
             b = {"cmp": A["hy"], "div": A["hd"], "scale2pow": A["hD"], "mpint_mul": A["hmc"]}.get(op, 0)
             reqs.append((n, op, count, a, b))
