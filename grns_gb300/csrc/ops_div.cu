@@ -245,7 +245,7 @@ size_t scale_bin_smem(const Consts<N> &C) {
 }
 
 template <int N>
-__global__ void __launch_bounds__(kScaleBinBlock) k_scale_bin(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_constant__ Consts<N> C, Operand<N> x,
                                                               const uint32_t *__restrict__ Darr, uint32_t D_uniform,
                                                               int32_t *__restrict__ order, int64_t count,
                                                               int64_t per_warp, Output<N> out,
