@@ -432,8 +432,10 @@ bool wait_done(grns_server *sv, std::unique_lock<std::mutex> &lk, uint64_t id, i
     const int64_t cap = (int64_t)600 * 1000 * 1000;  // 10 minutes
     auto until = Clock::now() + std::chrono::microseconds(timeout_us < 0 || timeout_us > cap ? cap : timeout_us);
     while (!req_finished(sv, id)) {
-        if (Clock::now() >= until) return false;
-        sv->cv.wait_for(lk, std::chrono::milliseconds(1));
+        const auto now = Clock::now();
+        if (now >= until) return false;
+        /* wake at least every millisecond (completions notify without the lock), never past the deadline */
+        sv->cv.wait_until(lk, std::min(until, now + std::chrono::milliseconds(1)));
     }
     return true;
 }
