@@ -112,24 +112,8 @@ def find_lib(name):
 BLOCK_TAGS = ["g32", "g64", "p32", "p64"]
 
 
-def block_headers():
-    """oracle/_ref/block_src: the reference's src/ headers for the block
-    build, with `static __shared__` written `__shared__` (the shim defines
-    __shared__ as `static` there; CUDA's __shared__ locals are block-wide
-    statics already).  Generated from the checkout, never committed."""
-    src, dst = os.path.join(REF, "src"), os.path.join(OUT, "block_src")
-    os.makedirs(dst, exist_ok=True)
-    for f in os.listdir(src):
-        if f.endswith((".cuh", ".h")):
-            with open(os.path.join(src, f)) as fh:
-                text = fh.read()
-            with open(os.path.join(dst, f), "w") as fh:
-                fh.write(text.replace("static __shared__", "__shared__"))
-    return dst
-
-
 def build_one(tag, gmp, mpfr, block=False):
-    src = block_headers() if block else os.path.join(REF, "src")
+    src = os.path.join(REF, "src")
     out = os.path.join(OUT, f"libgrnsref_block_{tag}.so" if block else f"libgrnsref_{tag}.so")
     drv = os.path.join(HERE, "ref_block.cpp" if block else "ref_driver.cpp")
     cmd = ["g++", "-std=c++14", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-frounding-math",
@@ -139,6 +123,14 @@ def build_one(tag, gmp, mpfr, block=False):
         # private to each set's library (as GNU-unique symbols the loader
         # would merge the n = 32 and n = 64 sets' arrays across libraries)
         cmd += ["-DORACLE_BLOCK_EMULATION", "-pthread", "-fno-gnu-unique"]
+        # the translation unit comes on standard input: pairwise.cuh with its
+        # `static __shared__` written `__shared__` (the driver makes __shared__
+        # a static; a doubled `static` does not compile), then the driver,
+        # whose includes of the other headers read them from the checkout
+        with open(os.path.join(src, "pairwise.cuh")) as f:
+            pairwise = f.read().replace("static __shared__", "__shared__")
+        stdin_unit = ("#undef __shared__\n#define __shared__ static\n" + pairwise +
+                      "\n#undef __shared__\n#define __shared__\n#include \"" + drv + "\"\n")
     if isinstance(SETS[tag], str):
         cmd += ["-include", os.path.join(REF, SETS[tag])]
     elif SETS[tag] is not None:
@@ -146,12 +138,13 @@ def build_one(tag, gmp, mpfr, block=False):
         with open(hdr, "w") as f:
             f.write(params_header(SETS[tag]))
         cmd += ["-include", hdr]
-    cmd += ["-I", os.path.join(HERE, "shim"), "-I", src, drv, "-o", out, mpfr, gmp]
+    cmd += ["-I", os.path.join(HERE, "shim"), "-I", src]
+    cmd += (["-x", "c++", "-", "-x", "none"] if block else [drv]) + ["-o", out, mpfr, gmp]
     newest_input = max(os.path.getmtime(p) for p in [drv, os.path.abspath(__file__)] +
                        [os.path.join(HERE, "shim", f) for f in os.listdir(os.path.join(HERE, "shim"))])
     if os.path.exists(out) and os.path.getmtime(out) >= newest_input:
         return out
-    subprocess.run(cmd, check=True)
+    subprocess.run(cmd, check=True, input=stdin_unit if block else None, text=True)
     return out
 
 

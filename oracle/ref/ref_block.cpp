@@ -19,11 +19,20 @@
 #include <thread>
 #include <vector>
 
+/* CUDA gives a __shared__ local one instance per block: here a static.  The
+ * one header that writes `static __shared__` (pairwise.cuh) reaches this unit
+ * through the recipe's standard input with those two words as `__shared__`
+ * (oracle/ref/build_ref.py), ahead of this file; the rest are read as they
+ * lie in the reference checkout */
+#undef __shared__
+#define __shared__ static
 #include "rnseval.cuh"
 #include "rnscmp.cuh"
 #include "rnsdiv.cuh"
 #include "rnsscal.cuh"
 #include "mpint.cuh"
+#undef __shared__
+#define __shared__
 
 #define N_ RNS_MODULI_SIZE
 static_assert(N_ % 32 == 0, "block emulation needs whole warps");
@@ -99,6 +108,13 @@ extern "C" {
 
 int ref_block_n() { return N_; }
 
+}  // extern "C"
+
+/* the block's copies of the current number(s), block-wide like __shared__ */
+static int g_x[N_], g_y[N_], g_q[N_], g_r[N_];
+
+extern "C" {
+
 void ref_block_init() {
     rns_const_init();
     mpint_const_init();
@@ -106,7 +122,7 @@ void ref_block_init() {
 
 /* x: count numbers, AoS; every number evaluated by one block run */
 void ref_block_eval(const int *x, long count, interval_t *out) {
-    static int xs[N_];
+    int *xs = g_x;
     run_block([&](int t) {
         for (long k = 0; k < count; k++) {
             xs[t] = x[k * N_ + t];
@@ -118,7 +134,7 @@ void ref_block_eval(const int *x, long count, interval_t *out) {
 }
 
 void ref_block_cmp(const int *x, const int *y, long count, int *out) {
-    static int xs[N_], ys[N_];
+    int *xs = g_x, *ys = g_y;
     run_block([&](int t) {
         for (long k = 0; k < count; k++) {
             xs[t] = x[k * N_ + t];
@@ -133,7 +149,7 @@ void ref_block_cmp(const int *x, const int *y, long count, int *out) {
 
 /* fast = 0: rns_div_parallel, 1: rns_div_parallel_fast */
 void ref_block_div(const int *x, const int *d, long count, int *q, int *r, int fast) {
-    static int xs[N_], ds[N_], qs[N_], rs[N_];
+    int *xs = g_x, *ds = g_y, *qs = g_q, *rs = g_r;
     run_block([&](int t) {
         for (long k = 0; k < count; k++) {
             xs[t] = x[k * N_ + t];
@@ -150,7 +166,7 @@ void ref_block_div(const int *x, const int *d, long count, int *q, int *r, int f
 }
 
 void ref_block_mrc(const int *x, long count, int *mr) {
-    static int xs[N_], ms[N_];
+    int *xs = g_x, *ms = g_q;
     run_block([&](int t) {
         for (long k = 0; k < count; k++) {
             xs[t] = x[k * N_ + t];

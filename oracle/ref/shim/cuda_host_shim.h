@@ -19,10 +19,9 @@
  *    the serial checker never calls those variants.  With
  *    ORACLE_BLOCK_EMULATION defined (oracle/ref/ref_block.cpp) they run for
  *    real: one host thread per CUDA thread of a block, threadIdx per thread,
- *    __syncthreads a barrier of the block, __shfl_down_sync an exchange among
- *    the 32 lanes of a warp, and __shared__ locals block-wide statics (the
- *    CUDA meaning; the recipe drops the reference's redundant `static`
- *    before `__shared__` in its build copy of the headers).
+ *    __syncthreads a barrier of the block and __shfl_down_sync an exchange
+ *    among the 32 lanes of a warp (the driver makes __shared__ locals
+ *    block-wide statics around its include of the reference headers).
  */
 #ifndef ORACLE_CUDA_HOST_SHIM_H
 #define ORACLE_CUDA_HOST_SHIM_H
@@ -38,11 +37,7 @@
 #define __host__
 #define __global__
 #define __constant__
-#ifdef ORACLE_BLOCK_EMULATION
-#define __shared__ static
-#else
 #define __shared__
-#endif
 #define __forceinline__ inline
 
 typedef int cudaError_t;
