@@ -114,17 +114,23 @@ constexpr int kDivUnroll = 4;
 /* c = floor(R / D) when the fixed-point comparison was too close to call:
  * R = j D exactly (dv_final_tie, from the residues in the shared-memory
  * columns), else the exact comparisons */
-template <int N>
-__device__ __forceinline__ int div_final_tie(const DivK *K, const Consts<N> &C, const uint32_t *Rc, const uint32_t *Dc,
-                                             int stride, u128 UD) {
-    const int j = dv_final_tie<N>(C, UD, [&](int i) { return Rc[i * stride]; }, [&](int i) { return Dc[i * stride]; });
+/* the same with R and D read through accessors */
+template <int N, class GR, class GD>
+__device__ __forceinline__ int div_final_tie_g(const Consts<N> &C, GR gr, GD gd, u128 UD) {
+    const int j = dv_final_tie<N>(C, UD, gr, gd);
     if (j) return j;
     uint32_t a[N], b[N];
     for (int i = 0; i < N; i++) {
-        a[i] = Rc[i * stride];
-        b[i] = Dc[i * stride];
+        a[i] = gr(i);
+        b[i] = gd(i);
     }
     return dv_final_exact<N>(C, a, b);
+}
+
+template <int N>
+__device__ __forceinline__ int div_final_tie(const DivK *K, const Consts<N> &C, const uint32_t *Rc, const uint32_t *Dc,
+                                             int stride, u128 UD) {
+    return div_final_tie_g<N>(C, [&](int i) { return Rc[i * stride]; }, [&](int i) { return Dc[i * stride]; }, UD);
 }
 
 /* pass A over the numbers claim() hands out below end: rec[k] = record of
@@ -516,7 +522,9 @@ __device__ __forceinline__ int div_row_build(const DivK *K, const Consts<N> &C, 
 
 /* pass B over positions [0, end) of `order` (numbers with digit steps,
  * longest first) claimed with claim(); rows: kRowWords(N) words per number.
- * Column rows: R in [0, N), D in [N, 2N), Q in [2N, 3N). */
+ * Column rows: R in [0, N), Q in [N, 2N); D stays in the row (16-byte loads
+ * through the read-only path each step), which keeps the block's shared
+ * memory at 2n words a thread. */
 template <int N, class Claim>
 __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, uint32_t *rows,
                                              const int32_t *order, uint8_t *flags, int64_t end, Claim claim,
@@ -528,15 +536,14 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
     const unsigned lt = (1u << lane) - 1u;
     enum { Idle, Iter, Final, Dead };
     uint32_t *__restrict__ Rc = col;
-    uint32_t *__restrict__ Dc = col + N * stride;
-    uint32_t *__restrict__ Qc = col + 2 * N * stride;
+    uint32_t *__restrict__ Qc = col + N * stride;
     DivSt st;
     st.f = 0;
     st.left = 0;
     st.b = kDivB;
     u128 U = 0;
     int s = 0, ph = Idle;
-    uint32_t *row = rows;
+    uint32_t *row = rows;  // this lane's row: D stays there (read through the read-only path) until q replaces it
     int64_t idx = 0;
     for (;;) {
         const unsigned lv = __ballot_sync(FULL, ph == Iter);
@@ -544,10 +551,14 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
         if (lv == 0 || __popc(wt) >= kDivRefill) {
             if (ph == Final) {  // q = Q + c, r = (R - c D) 2^-s, into the row
                 int c = dv_final_fx(st, U, C.E);
-                if (c < 0) c = div_final_tie<N>(K, C, Rc, Dc, stride, st.UD);
+                if (c < 0)
+                    c = div_final_tie_g<N>(C, [&](int i) { return Rc[i * stride]; }, [&](int i) { return row[i]; },
+                                           st.UD);
 #pragma unroll 1
                 for (int i0 = 0; i0 < P; i0 += 4) {
                     uint32_t qv[4], rv[4];
+                    const uint4 d4 = *reinterpret_cast<const uint4 *>(row + i0);  // before q overwrites it
+                    const uint32_t dw[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
                     for (int j = 0; j < 4; j++) {
                         const int i = i0 + j;
@@ -555,7 +566,7 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
                         if (N % 4 == 0 || i < N) {
                             const DivK k = K[i];
                             const uint32_t m = k.a.x, cm = (uint32_t)c % m;
-                            const uint32_t v = submod(Rc[i * stride], kmulmod(cm, Dc[i * stride], k), m);
+                            const uint32_t v = submod(Rc[i * stride], kmulmod(cm, dw[j], k), m);
                             qv[j] = addmod(Qc[i * stride], cm, m);
                             rv[j] = mul_pow2neg<N>(C, i, v, s);
                         }
@@ -585,14 +596,12 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
                     div_hdr_get(h, st, U, s);
 #pragma unroll 2
                     for (int i0 = 0; i0 < P; i0 += 4) {
-                        const uint4 dv = *reinterpret_cast<const uint4 *>(row + i0);
                         const uint4 rv = *reinterpret_cast<const uint4 *>(row + P + i0);
-                        const uint32_t d4[4] = {dv.x, dv.y, dv.z, dv.w}, r4[4] = {rv.x, rv.y, rv.z, rv.w};
+                        const uint32_t r4[4] = {rv.x, rv.y, rv.z, rv.w};
 #pragma unroll
                         for (int j = 0; j < 4; j++) {
                             const int i = i0 + j;
                             if (N % 4 == 0 || i < N) {
-                                Dc[i * stride] = d4[j];
                                 Rc[i * stride] = r4[j];
                                 Qc[i * stride] = 0u;
                             }
@@ -613,12 +622,13 @@ __device__ __forceinline__ void divrow_range(const DivK *K, const Consts<N> &C, 
         Fx96 fx;
 #pragma unroll 1
         for (int i0 = 0; i0 < N; i0 += 4) {  // groups of 4: loads, arithmetic, stores
-            uint32_t rv[4], dv[4], qv[4];
+            uint32_t rv[4], qv[4];
+            const uint4 d4 = __ldg(reinterpret_cast<const uint4 *>(row + i0));  // D (zeros past N)
+            const uint32_t dv[4] = {d4.x, d4.y, d4.z, d4.w};
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int i = i0 + j < N ? i0 + j : N - 1;  // N not a multiple of 4: the last residue again
                 rv[j] = Rc[i * stride];
-                dv[j] = Dc[i * stride];
                 qv[j] = Qc[i * stride];
             }
 #pragma unroll
@@ -654,10 +664,11 @@ template <int N>
 constexpr size_t divprep_smem_bytes(int threads) {
     return sizeof(DivK) * N + (size_t)2 * N * 4 * threads;
 }
-/* shared memory of pass B with rows: the DivK table, then the columns */
+/* shared memory of pass B with rows: the DivK table, then the R and Q
+ * columns (D is read from the row) */
 template <int N>
 constexpr size_t divrow_smem_bytes(int threads) {
-    return sizeof(DivK) * N + (size_t)3 * N * 4 * threads;
+    return sizeof(DivK) * N + (size_t)2 * N * 4 * threads;
 }
 
 /* digit steps of a division from its record (0: no step loop) */

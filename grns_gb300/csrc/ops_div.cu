@@ -54,7 +54,7 @@ constexpr int kDivBlock = 128;
 /* resident 128-thread blocks per SM the register budget must allow: shared
  * memory (3N words per thread) allows 4 at n <= 32 and 2 at n = 64 */
 #ifndef GRNS_DIV_MIN_BLOCKS
-#define GRNS_DIV_MIN_BLOCKS 4
+#define GRNS_DIV_MIN_BLOCKS 5
 #endif
 template <int N>
 constexpr int div_min_blocks() {
