@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 N32 = 32
 PAIRS = 1 << 18
-DIV_TRAFFIC_BYTES = 446.3e6  # DRAM bytes of one 2^18-pair division call (ncu, five launches, each cold)
+DIV_TRAFFIC_BYTES = 447.1e6  # DRAM bytes of one 2^18-pair division call (ncu, five launches, each cold)
 CONV_COUNT = 1 << 22  # numbers per binary <-> RNS conversion call
 CMP_PAIRS = 1 << 20
 EVAL_COUNT = 1 << 22
