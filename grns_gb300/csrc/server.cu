@@ -17,13 +17,11 @@
  *     waited kPassCapUs: then nothing is admitted past it, so freed memory
  *     goes to it.  With several slots, requests arriving while launches are
  *     in flight are admitted and launched alongside them, so their work
- *     overlaps on the device.  Requests of direct_min_count numbers or more
- *     (eval, cmp, div, scale2pow, mp_int add/sub/mul) run in the same launch round
- *     through the per-op kernels instead, after the packed kernel on the same
- *     stream: the dedicated kernels (the division's prepared rows, the
- *     one-pass scaling, the claimed evaluation) are faster than the packed
- *     kernel's general forms once a request fills the GPU by itself, and
- *     packing pays for the many small ones;
+ *     overlaps on the device.  With direct_min_count set (off by default),
+ *     requests of that many numbers or more (eval, cmp, div, scale2pow,
+ *     mp_int add/sub/mul) run in the same launch round through the per-op
+ *     kernels instead, after the packed kernel on the same stream: lower
+ *     latency for the small requests under load, less throughput;
  *   - marks requests done from a host callback at the end of each launch and
  *     records submit-to-completion latency (p50/p99 in grns_server_stats).
  * Each array counts the unfinished requests that read it (counted at
@@ -54,7 +52,12 @@ using Clock = std::chrono::steady_clock;
 constexpr double kPassCapUs = 50e3;          // after this wait for memory, later requests stop passing one
 constexpr double kKeepFinishedUs = 60e6;     // finished requests stay readable this long
 constexpr size_t kKeepFinishedMax = 1 << 16; // and at most this many of them
-constexpr int32_t kDirectMinDefault = 1 << 18;  // default of grns_server_options.direct_min_count
+/* default of grns_server_options.direct_min_count: off.  On the served stream
+ * of the benchmark (64 requests of 10^3..10^7 numbers) packing everything ran
+ * 1.41-1.43 G numbers/s and 2^18 as the threshold 1.11-1.20 (lower p50 under
+ * Poisson load, higher p99): one persistent launch balances the large
+ * requests across the SMs better than their own kernels queued per slot */
+constexpr int32_t kDirectMinDefault = -1;
 
 double now_us() {
     return std::chrono::duration<double, std::micro>(Clock::now().time_since_epoch()).count();

@@ -378,7 +378,8 @@ typedef struct {
                                     kernels (the plain calls' launches, on the launch's stream)
                                     instead of inside the packed batched kernel: eval, cmp (unless
                                     both evaluations are cached), div, scale2pow, mp_int
-                                    add/sub/mul.  0: 262144; negative: never */
+                                    add/sub/mul.  0 or negative: never (the default: one packed
+                                    launch balanced the benchmark's served stream best) */
     size_t alloc_cap_bytes;      /* hard cap on the device memory the server holds (0: none): a put
                                     beyond it returns, and an admitted request beyond it completes
                                     with, GRNS_ERR_OUT_OF_MEMORY; the server goes on */
