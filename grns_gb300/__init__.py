@@ -36,7 +36,7 @@ from .native import GrnsError, check
 ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
 IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
 LAYOUTS = {"soa": 0, "aos": 1}
-SUPPORTED_N = (4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 32, 64)
+SUPPORTED_N = (4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 32, 64, 128, 256)
 
 FLAG_INVALID_INPUT = 1
 FLAG_DIV_BY_ZERO = 2

@@ -67,7 +67,8 @@ struct Part {  // max: best of one chunk
  * one: [DivK table][ScK table][warps' counters][columns of 3n words] */
 template <int N>
 struct BatchCfg {
-    static constexpr int kBlock = N > 32 ? 128 : 256;
+    /* one warp a block above 64 moduli: the division columns take 3n words a thread */
+    static constexpr int kBlock = N > 64 ? 32 : N > 32 ? 128 : 256;
     static constexpr int kMinBlocks = 2;
     static constexpr size_t kTables = (sizeof(DivK) + sizeof(ScK)) * N;
     static constexpr size_t kHeavySmem = kTables + (size_t)(kBlock / 32) * kDivBins * 4 + (size_t)3 * N * 4 * kBlock;
@@ -119,7 +120,7 @@ __device__ __forceinline__ uint64_t fx64_coop(const Consts<N> &C, const Operand<
     uint64_t a = 0;
     uint32_t b = 0;
     if (active) {
-#pragma unroll
+GRNS_UNROLL_TO(N / G)
         for (int r = 0; r < N / G; r++) {
             const int i = gl + r * G;
             const uint32_t v = x.load_cs(k, i);
@@ -143,7 +144,7 @@ template <int N>
 __device__ __forceinline__ void load_aos4(const uint32_t *base, int64_t k, uint32_t *v) {
     if constexpr (N % 4 == 0) {
         const uint4 *p = reinterpret_cast<const uint4 *>(base + k * N);
-#pragma unroll
+GRNS_UNROLL_TO(N / 4)
         for (int q = 0; q < N / 4; q++) {
             const uint4 w = __ldcs(p + q);
             v[4 * q] = w.x;
@@ -158,7 +159,7 @@ __device__ __forceinline__ void load_aos4(const uint32_t *base, int64_t k, uint3
 template <int N>
 __device__ __forceinline__ uint64_t fx64_arr(const Consts<N> &C, const uint32_t *v, uint32_t &bad) {
     uint64_t a = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         bad |= (uint32_t)(v[i] >= C.m[i]);
         a += (uint64_t)v[i] * C.c64l[i];
@@ -230,7 +231,7 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
                         load_aos4<N>(J.b, k, v);
                         b = fx64_arr<N>(C, v, bad);
                     } else {
-#pragma unroll
+GRNS_UNROLL_N
                         for (int i = 0; i < N; i++) {
                             const uint32_t xi = x.load_cs(k, i), yi = y.load_cs(k, i);
                             bad |= (uint32_t)(xi >= C.m[i]) | (uint32_t)(yi >= C.m[i]);
@@ -354,10 +355,11 @@ __device__ __forceinline__ void run_chunk(const Consts<N> &C, const JobDev &J, i
 }
 
 template <int N>
-__global__ void __launch_bounds__(BatchCfg<N>::kBlock, BatchCfg<N>::kMinBlocks) k_batch(const __grid_constant__ Consts<N> C,
+__global__ void __launch_bounds__(BatchCfg<N>::kBlock, BatchCfg<N>::kMinBlocks) k_batch(const __grid_constant__ CArg<N> CA,
                                                           const JobDev *__restrict__ jobs, int njobs,
                                                           int64_t total_chunks, unsigned long long *counter,
                                                           unsigned *done, Part *partials, int has_div) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 batch_smem4[];
     uint32_t *batch_smem = reinterpret_cast<uint32_t *>(batch_smem4);
     if (has_div) {  // division and scaling constants for every block

@@ -19,24 +19,36 @@ namespace grns {
 
 constexpr int kConvBlock = 128;
 
+/* the chunk tables are staged in shared memory up to 64 moduli (at most
+ * 316 x 64 words); above, a block holds only its rows */
+template <int N>
+constexpr bool conv_tables_shared() {
+    return N <= 64;
+}
+
 __host__ __device__ constexpr int odd_at_least(int v) { return v | 1; }
 
 /* ---------------- binary -> RNS ---------------- */
 
 /* out[k * ks + i * is] = (integer k) mod m_i; nonzero[k] (optional) = integer k != 0 */
 template <int N>
-__global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constant__ Consts<N> C,
+__global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constant__ CArg<N> CA,
                                                             const uint32_t *__restrict__ words, int nlimbs,
                                                             int64_t count, uint32_t *__restrict__ out, int64_t ks,
                                                             int64_t is, uint8_t *__restrict__ nonzero) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 conv_smem[];
     const int chunks = (32 * nlimbs + kBinChunk - 1) / kBinChunk;
     const int rs = odd_at_least(nlimbs + 1);  // row stride: limbs, one zero word, odd
     constexpr int L4 = bin_ld(N) / 4;         // 16-byte words per table row
-    uint4 *T4 = conv_smem;                    // [chunks][L4]
-    uint32_t *rows = reinterpret_cast<uint32_t *>(T4 + chunks * L4);
-    for (int w = threadIdx.x; w < chunks * L4; w += blockDim.x)
-        T4[w] = reinterpret_cast<const uint4 *>(C.bin_p26)[w];
+    constexpr bool kShared = conv_tables_shared<N>();
+    /* [chunks][L4]: staged in shared memory up to 64 moduli, else read through L1 / L2 */
+    const uint4 *T4 = kShared ? conv_smem : reinterpret_cast<const uint4 *>(C.bin_p26);
+    uint32_t *rows = reinterpret_cast<uint32_t *>(conv_smem + (kShared ? chunks * L4 : 0));
+    if (kShared)
+        for (int w = threadIdx.x; w < chunks * L4; w += blockDim.x)
+            conv_smem[w] = reinterpret_cast<const uint4 *>(C.bin_p26)[w];
+    const bool fold = chunks > kBinSumMax;
     uint32_t *row = rows + threadIdx.x * rs;
     for (int j = nlimbs; j < rs; j++) row[j] = 0;
     constexpr int G = (N % 8 == 0) ? 8 : 4;
@@ -72,6 +84,11 @@ __global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constan
                     acc[u + 2] += (uint64_t)ch * v.z;
                     acc[u + 3] += (uint64_t)ch * v.w;
                 }
+                if (fold && c % kBinFold == kBinFold - 1) {
+#pragma unroll
+                    for (int u = 0; u < G; u++)
+                        if (N % G == 0 || g + u < N) acc[u] = bin_mod64<N>(C, g + u, acc[u]);
+                }
             }
 #pragma unroll
             for (int u = 0; u < G; u++)
@@ -82,7 +99,7 @@ __global__ void __launch_bounds__(kConvBlock) k_from_binary(const __grid_constan
 
 template <int N>
 constexpr size_t from_binary_smem(int nlimbs) {
-    return (size_t)((32 * nlimbs + kBinChunk - 1) / kBinChunk) * bin_ld(N) * 4 +
+    return (conv_tables_shared<N>() ? (size_t)((32 * nlimbs + kBinChunk - 1) / kBinChunk) * bin_ld(N) * 4 : 0) +
            (size_t)kConvBlock * odd_at_least(nlimbs + 1) * 4;
 }
 
@@ -93,23 +110,30 @@ constexpr size_t from_binary_smem(int nlimbs) {
  * and sign_out: sign_out[k] = sign_in == 1 and X_k != 0 (mpint_get_mpz's
  * sign).  An invalid residue flags the number and gives zero. */
 template <int N>
-__global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant__ Consts<N> C,
+__global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant__ CArg<N> CA,
                                                           const uint32_t *__restrict__ x, int64_t ks, int64_t is,
                                                           int64_t count, uint32_t *__restrict__ words, int nout,
                                                           const int32_t *__restrict__ sign_in, int64_t ss,
                                                           int32_t *__restrict__ sign_out,
                                                           uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 conv_smem[];
     const int chunks = C.bin_chunks;
     const int m4 = (chunks + 3) / 4;
     const int rs = odd_at_least(chunks);
     constexpr int L = bin_ld(N);            // table row: N words and zeros up to a multiple of 4
-    uint4 *Mi4 = conv_smem;                 // [chunks][L / 4]
-    uint32_t *M26 = reinterpret_cast<uint32_t *>(Mi4 + chunks * (L / 4));  // [m4 * 4]
-    uint32_t *rows = M26 + m4 * 4;
-    for (int w = threadIdx.x; w < chunks * (L / 4); w += blockDim.x)
-        Mi4[w] = reinterpret_cast<const uint4 *>(C.bin_mi26)[w];
-    for (int w = threadIdx.x; w < m4 * 4; w += blockDim.x) M26[w] = C.bin_m26[w];
+    constexpr bool kShared = conv_tables_shared<N>();
+    /* [chunks][L / 4] and [m4 * 4]: staged in shared memory up to 64 moduli, else read through L1 / L2 */
+    uint4 *Mi4s = conv_smem;
+    uint32_t *M26s = reinterpret_cast<uint32_t *>(Mi4s + chunks * (L / 4));
+    const uint4 *Mi4 = kShared ? Mi4s : reinterpret_cast<const uint4 *>(C.bin_mi26);
+    const uint32_t *M26 = kShared ? M26s : C.bin_m26;
+    uint32_t *rows = kShared ? M26s + m4 * 4 : reinterpret_cast<uint32_t *>(conv_smem);
+    if (kShared) {
+        for (int w = threadIdx.x; w < chunks * (L / 4); w += blockDim.x)
+            Mi4s[w] = reinterpret_cast<const uint4 *>(C.bin_mi26)[w];
+        for (int w = threadIdx.x; w < m4 * 4; w += blockDim.x) M26s[w] = C.bin_m26[w];
+    }
     uint32_t *row = rows + threadIdx.x * rs;
     for (int64_t k0 = (int64_t)blockIdx.x * kConvBlock; k0 < count; k0 += (int64_t)gridDim.x * kConvBlock) {
         const int tile = count - k0 < kConvBlock ? (int)(count - k0) : kConvBlock;
@@ -118,9 +142,9 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
             const int64_t k = k0 + threadIdx.x;
             uint32_t s[L];
             uint32_t bad = 0, any = 0;
-#pragma unroll
+GRNS_UNROLL_TO(L)
             for (int i = N; i < L; i++) s[i] = 0;
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) {
                 const uint32_t v = __ldg(x + k * ks + (int64_t)i * is);
                 bad |= (uint32_t)(v >= C.m[i]);
@@ -134,8 +158,8 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
                 int64_t carry = 0;
                 for (int c = 0; c < chunks; c++) {
                     const uint4 *t = Mi4 + c * (L / 4);
-                    uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
+                    BinAcc<N> a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+GRNS_UNROLL_TO(L)
                     for (int i = 0; i < L; i += 4) {
                         const uint4 v = t[i / 4];
                         a0 += (uint64_t)s[i] * v.x;
@@ -143,8 +167,8 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
                         a2 += (uint64_t)s[i + 2] * v.z;
                         a3 += (uint64_t)s[i + 3] * v.w;
                     }
-                    const int64_t v = (int64_t)((a0 + a1) + (a2 + a3)) - (int64_t)kk * M26[c] + carry;
-                    carry = v >> kBinChunk;
+                    const BinSAcc<N> v = (BinSAcc<N>)((a0 + a1) + (a2 + a3)) - (BinSAcc<N>)kk * M26[c] + carry;
+                    carry = (int64_t)(v >> kBinChunk);
                     row[c] = (uint32_t)v & kBinMask;
                 }
                 if (carry < 0) {
@@ -171,7 +195,8 @@ __global__ void __launch_bounds__(kConvBlock) k_to_binary(const __grid_constant_
 
 template <int N>
 size_t to_binary_smem(const Consts<N> &C) {
-    return (size_t)C.bin_chunks * bin_ld(N) * 4 + (size_t)((C.bin_chunks + 3) / 4) * 16 +
+    return (conv_tables_shared<N>() ? (size_t)C.bin_chunks * bin_ld(N) * 4 + (size_t)((C.bin_chunks + 3) / 4) * 16
+                                    : 0) +
            (size_t)kConvBlock * odd_at_least(C.bin_chunks) * 4;
 }
 
@@ -180,10 +205,11 @@ size_t to_binary_smem(const Consts<N> &C) {
 /* mpint_set_mpz's record: digits from residue-major columns (ld = count), the
  * sign of a nonzero integer, the evaluation of the digits */
 template <int N>
-__global__ void __launch_bounds__(128) k_mpint_pack(const __grid_constant__ Consts<N> C,
+__global__ void __launch_bounds__(128) k_mpint_pack(const __grid_constant__ CArg<N> CA,
                                                     const uint32_t *__restrict__ res, const int32_t *__restrict__ signs,
                                                     const uint8_t *__restrict__ nonzero, int64_t count,
                                                     MpInt<N> *__restrict__ out) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         MpInt<N> r;
         uint32_t f = 0;

@@ -30,6 +30,19 @@ int64_t gcd64(int64_t a, int64_t b) {
     return a;
 }
 
+/* the constant block on the host, and on the device where kernels take it by address */
+template <int N>
+grns_status finish_consts(grns_ctx *c, const uint32_t *d_tables) {
+    grns::Consts<N> &C = *reinterpret_cast<grns::Consts<N> *>(c->consts);
+    grns::fill_consts<N>(C, c->T, d_tables);
+    C.self = nullptr;
+    if (!grns::consts_by_address<N>()) return GRNS_OK;
+    cudaError_t e = cudaMalloc(&c->d_consts, sizeof(C));
+    if (e != cudaSuccess) return grns::cuda_status(e);
+    C.self = c->d_consts;
+    return grns::cuda_status(cudaMemcpy(c->d_consts, &C, sizeof(C), cudaMemcpyHostToDevice));
+}
+
 grns_status build(grns_ctx *c, const uint32_t *moduli) {
     grns::build_tables(c->T, moduli, c->n);
     c->log2M = c->T.log2M;
@@ -39,9 +52,7 @@ grns_status build(grns_ctx *c, const uint32_t *moduli) {
     e = cudaMemcpy(c->d_tables, blob.data(), blob.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return grns::cuda_status(e);
     const uint32_t *d = (const uint32_t *)c->d_tables;
-#define C_(n)                                                                        \
-    grns::fill_consts<n>(*reinterpret_cast<grns::Consts<n> *>(c->consts), c->T, d); \
-    return GRNS_OK
+#define C_(n) return finish_consts<n>(c, d)
     GRNS_DISPATCH_N(c->n, C_)
 #undef C_
 }
@@ -235,6 +246,7 @@ grns_status grns_ctx_destroy(grns_ctx *c) {
         cudaEventDestroy(p.done);
     }
     if (c->d_tables) cudaFree(c->d_tables);
+    if (c->d_consts) cudaFree(c->d_consts);
     if (c->pool) cudaMemPoolDestroy(c->pool);  // released once outstanding scratch is freed
     delete c;
     return GRNS_OK;

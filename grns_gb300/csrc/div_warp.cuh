@@ -679,12 +679,13 @@ __device__ __forceinline__ int dv_rec_steps(const uint2 &r) {
     return a + 1 - (e < 0 ? 0 : (e - t) / kDivB + 1);
 }
 
-constexpr int kDivBins = 64;  // > log2(M) / 48 + 1 for every supported moduli set
+constexpr int kDivBins = 64;  // step-count bins of a warp's ordering (> log2(M) / 48 + 1 up to 64 moduli)
 
 /* order[begin + p] (p = 0..) = offsets of the range's numbers by decreasing
- * step count steps_of(k) in [0, kDivBins) (a counting sort; hist: this warp's
- * kDivBins shared counters), so a warp's last numbers are its cheapest and
- * the drain at the end of the range is short */
+ * step count steps_of(k) (a counting sort over kDivBins bins, counts of 63 or
+ * more sharing the last -- 128 and 256 moduli reach ~170 steps; hist: this
+ * warp's kDivBins shared counters), so a warp's last numbers are its
+ * cheapest and the drain at the end of the range is short */
 template <class StepsOf>
 __device__ __forceinline__ void lpt_order(StepsOf steps_of, int32_t *order, int64_t begin, int64_t end,
                                           uint32_t *hist) {
@@ -693,7 +694,8 @@ __device__ __forceinline__ void lpt_order(StepsOf steps_of, int32_t *order, int6
     hist[lane] = 0;
     hist[lane + 32] = 0;
     __syncwarp();
-    for (int64_t e = begin + lane; e < end; e += 32) atomicAdd(&hist[steps_of(e)], 1u);
+    auto bin = [&](int64_t e) { return min(kDivBins - 1, (int)steps_of(e)); };
+    for (int64_t e = begin + lane; e < end; e += 32) atomicAdd(&hist[bin(e)], 1u);
     __syncwarp();
     /* exclusive prefix over bins in decreasing order: lane l holds bins 63 - l and 31 - l */
     const uint32_t h0 = hist[63 - lane], h1 = hist[31 - lane];
@@ -712,7 +714,7 @@ __device__ __forceinline__ void lpt_order(StepsOf steps_of, int32_t *order, int6
     hist[31 - lane] = s1 - h1;
     __syncwarp();
     for (int64_t e = begin + lane; e < end; e += 32) {
-        const uint32_t p = atomicAdd(&hist[steps_of(e)], 1u);
+        const uint32_t p = atomicAdd(&hist[bin(e)], 1u);
         order[begin + p] = (int32_t)(e - begin);
     }
     __syncwarp();  // the order written by one lane is read by another

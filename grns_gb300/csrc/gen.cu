@@ -24,9 +24,10 @@ __device__ __forceinline__ uint64_t draw(uint64_t key, uint64_t ctr) { return sp
 inline uint64_t stream_key(uint64_t seed, uint32_t stream) { return splitmix64(seed ^ ((uint64_t)stream << 32)); }
 
 template <int N>
-__global__ void k_gen_uniform(const __grid_constant__ Consts<N> C, uint64_t key, int64_t count, Output<N> out) {
+__global__ void k_gen_uniform(const __grid_constant__ CArg<N> CA, uint64_t key, int64_t count, Output<N> out) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             const uint32_t m = C.m[i];
             const uint64_t thr = (0ull - (uint64_t)m) % m;
@@ -42,8 +43,9 @@ __global__ void k_gen_uniform(const __grid_constant__ Consts<N> C, uint64_t key,
 }
 
 template <int N>
-__global__ void k_gen_divisors(const __grid_constant__ Consts<N> C, uint64_t key_len, uint64_t key_limb, int log2M,
+__global__ void k_gen_divisors(const __grid_constant__ CArg<N> CA, uint64_t key_len, uint64_t key_limb, int log2M,
                                int64_t count, Output<N> out) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         const int L = (int)__umul64hi(draw(key_len, (uint64_t)k), (uint64_t)log2M) + 1;
         const int nl = (L + 31) / 32;
@@ -72,8 +74,9 @@ __global__ void k_gen_divisors(const __grid_constant__ Consts<N> C, uint64_t key
  * digits by the device evaluation (the reference's mpint_set_mpz,
  * src/mpint.cuh:74, evaluates on the host) */
 template <int N>
-__global__ void k_gen_mpint(const __grid_constant__ Consts<N> C, uint64_t key_mag, uint64_t key_sign, int bits,
+__global__ void k_gen_mpint(const __grid_constant__ CArg<N> CA, uint64_t key_mag, uint64_t key_sign, int bits,
                             int64_t count, MpInt<N> *out) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         const int nl = (bits + 31) / 32;
         MpInt<N> v;

@@ -34,6 +34,7 @@ struct grns_ctx {
     int eval_fp64_eighths = 4;
     grns::HostTables T;  // host copies of all tables
     void *d_tables = nullptr;  // one device allocation holding the table blob
+    void *d_consts = nullptr;  // device copy of the constant block, where kernels take it by address
     /* stream-ordered pool for per-call scratch (division records, scaling and
      * batch orders, max partials); keeps up to kPoolKeepBytes across
      * synchronisations so repeated calls do not map fresh memory */
@@ -147,10 +148,11 @@ grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *
  * GRNS_PART_N lists; unit 0 (GRNS_PART_MAIN) also holds the file's other
  * code, whose dispatch sees the templates through extern declarations.
  * Without GRNS_PART one unit holds everything.  The groups balance compile
- * time (n = 32 and n = 64 cost about as much as n = 4..16 together). */
+ * time (n = 32 and n = 64 cost about as much as n = 4..16 together; 128 and
+ * 256, whose loops over the moduli stay rolled, little). */
 #define GRNS_N_PARTS 4
 #define GRNS_N_PART0_(X) X(4) X(5) X(6) X(7) X(8) X(9) X(10)
-#define GRNS_N_PART1_(X) X(11) X(12) X(13) X(14) X(15) X(16)
+#define GRNS_N_PART1_(X) X(11) X(12) X(13) X(14) X(15) X(16) X(128) X(256)
 #define GRNS_N_PART2_(X) X(32)
 #define GRNS_N_PART3_(X) X(64)
 #if !defined(GRNS_PART)

@@ -22,25 +22,26 @@
 namespace grns {
 
 template <int N, bool FAST>
-__global__ void __launch_bounds__(128) k_div(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d,
+__global__ void __launch_bounds__(128) k_div(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> d,
                                              int64_t count, Output<N> q, Output<N> r, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t xa[N], da[N], qa[N], ra[N], f = 0;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             xa[i] = x.load(k, i);
             da[i] = d.load(k, i);
             f |= (xa[i] >= C.m[i] || da[i] >= C.m[i]) ? kFlagInvalidInput : 0u;
         }
         if (f) {
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) { qa[i] = 0; ra[i] = 0; }
         } else if (FAST) {
             div_fast<N>(C, qa, ra, xa, da, f);
         } else {
             div_ref<N>(C, qa, ra, xa, da, f);
         }
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             q.store(k, i, qa[i]);
             r.store(k, i, ra[i]);
@@ -76,8 +77,9 @@ struct DivRowsG {
  * 8-byte record (div_warp.cuh, divnorm_range) */
 template <int N>
 __global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
-    k_div_a(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
+    k_div_a(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> d, uint2 *__restrict__ rec,
             DivRowsG *__restrict__ G, int64_t count) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 div_smem[];
     DivK *K = reinterpret_cast<DivK *>(div_smem);
     uint32_t *cols = reinterpret_cast<uint32_t *>(K + N);  // layout of divprep_smem_bytes
@@ -94,10 +96,11 @@ __global__ void __launch_bounds__(kDivBlock, N > 32 ? 3 : 6)
  * lane busy); per number its row, its step count and (no digit step) its
  * flags; the step-count histogram */
 template <int N>
-__global__ void __launch_bounds__(256) k_div_rows(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> d,
+__global__ void __launch_bounds__(256) k_div_rows(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> d,
                                                   const uint2 *__restrict__ rec, uint32_t *__restrict__ rows,
                                                   uint8_t *__restrict__ steps, uint8_t *__restrict__ flags,
                                                   DivRowsG *__restrict__ G, int64_t count) {
+    const Consts<N> &C = CA.get();
     __shared__ DivK K[N];
     __shared__ uint32_t hist[kDivRowBins];
     divk_fill<N>(C, K);
@@ -151,8 +154,9 @@ static __global__ void __launch_bounds__(256) k_div_place(const uint8_t *__restr
  * done already */
 template <int N>
 __global__ void __launch_bounds__(kDivBlock, div_min_blocks<N>())
-    k_div_b(const __grid_constant__ Consts<N> C, uint32_t *__restrict__ rows, const int32_t *__restrict__ order,
+    k_div_b(const __grid_constant__ CArg<N> CA, uint32_t *__restrict__ rows, const int32_t *__restrict__ order,
             uint8_t *__restrict__ flags, DivRowsG *__restrict__ G, int64_t count) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 div_smem[];
     DivK *K = reinterpret_cast<DivK *>(div_smem);
     uint32_t *cols = reinterpret_cast<uint32_t *>(K + N);  // layout of divrow_smem_bytes
@@ -207,9 +211,10 @@ __global__ void __launch_bounds__(256) k_div_out(const uint32_t *__restrict__ ro
 
 template <int N>
 __global__ void __launch_bounds__(kDivBlock, N > 32 ? 4 : 6)
-    k_scale_warp(const __grid_constant__ Consts<N> C, Operand<N> x, const uint32_t *__restrict__ D,
+    k_scale_warp(const __grid_constant__ CArg<N> CA, Operand<N> x, const uint32_t *__restrict__ D,
                  uint32_t D_uniform, int32_t *__restrict__ order, int64_t count, int64_t per_warp, Output<N> out,
                  uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 scale_smem[];
     ScK *K = reinterpret_cast<ScK *>(scale_smem);
     uint32_t *hist = reinterpret_cast<uint32_t *>(K + N);
@@ -245,11 +250,12 @@ size_t scale_bin_smem(const Consts<N> &C) {
 }
 
 template <int N>
-__global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                               const uint32_t *__restrict__ Darr, uint32_t D_uniform,
                                                               int32_t *__restrict__ order, int64_t count,
                                                               int64_t per_warp, Output<N> out,
                                                               uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 sb_smem[];
     constexpr int L4 = bin_ld(N) / 4;
     const int chunks = C.bin_chunks, m4 = (chunks + 3) / 4;
@@ -276,13 +282,13 @@ __global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_co
         const int64_t idx = Darr ? b + order[p] : p;
         const unsigned D = Darr ? __ldg(Darr + idx) : D_uniform;
         uint32_t s[4 * L4], bad = 0;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             const uint32_t v = x.load(idx, i);
             bad |= (uint32_t)(v >= C.m[i]);
             s[i] = mulmod_shoup(v, C.w[i], C.w_sh[i], C.m[i]);
         }
-#pragma unroll
+GRNS_UNROLL_TO(4 * L4)
         for (int i = N; i < 4 * L4; i++) s[i] = 0;
         if (flags) flags[idx] = bad ? (uint8_t)kFlagInvalidInput : (uint8_t)0;
         if (bad || D > (unsigned)C.log2M || D == 0) {  // invalid or 2^D > X: 0; D = 0: X
@@ -294,14 +300,14 @@ __global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_co
         const int nch = (int)((D + kBinChunk - 1) / kBinChunk);
         const uint32_t top = D % kBinChunk ? (1u << (D % kBinChunk)) - 1u : kBinMask;
         uint64_t acc[4 * L4];
-#pragma unroll
+GRNS_UNROLL_TO(4 * L4)
         for (int i = 0; i < 4 * L4; i++) acc[i] = 0;
         int64_t carry = 0;
 #pragma unroll 1
         for (int c = 0; c < nch; c++) {
             const uint4 *t = MI4 + c * L4;
             uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
+GRNS_UNROLL_TO(L4)
             for (int q = 0; q < L4; q++) {
                 const uint4 v = t[q];
                 a0 += (uint64_t)s[4 * q] * v.x;
@@ -313,7 +319,7 @@ __global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_co
             carry = v >> kBinChunk;  // floor division (arithmetic shift)
             const uint32_t r = (uint32_t)v & (c == nch - 1 ? top : kBinMask);
             const uint4 *pp = P4 + c * L4;
-#pragma unroll
+GRNS_UNROLL_TO(L4)
             for (int q = 0; q < L4; q++) {
                 const uint4 w = pp[q];
                 acc[4 * q] += (uint64_t)r * w.x;
@@ -322,33 +328,34 @@ __global__ void __launch_bounds__(kScaleBinBlock, 3) k_scale_bin(const __grid_co
                 acc[4 * q + 3] += (uint64_t)r * w.w;
             }
         }
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++)
             out.store(idx, i, scale_bin_finish<N>(C, i, x.load(idx, i), bin_mod64<N>(C, i, acc[i]), D));
     }
 }
 
 template <int N, bool FAST>
-__global__ void __launch_bounds__(128) k_scale(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(128) k_scale(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                const uint32_t *__restrict__ D, uint32_t D_uniform, int64_t count,
                                                Output<N> out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t xa[N], ya[N], f = 0;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             xa[i] = x.load(k, i);
             f |= xa[i] >= C.m[i] ? kFlagInvalidInput : 0u;
         }
         unsigned dk = D ? __ldg(D + k) : D_uniform;
         if (f) {
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) ya[i] = 0;
         } else if (FAST) {
             scale_fast<N>(C, ya, xa, dk);
         } else {
             scale2pow_ref<N>(C, ya, xa, dk);
         }
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) out.store(k, i, ya[i]);
         if (flags) flags[k] = (uint8_t)f;
     }
@@ -363,6 +370,14 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
                                                                count, Output<N>{q, ldo}, Output<N>{r, ldo}, flags);
         return cuda_status(cudaGetLastError());
     }
+    if constexpr (N > 64) {
+        /* the digit recurrence one number per thread (its row in local memory):
+         * the warp passes' shared-memory columns (2n words a thread) do not fit */
+        k_div<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
+                                                              count, Output<N>{q, ldo}, Output<N>{r, ldo}, flags);
+        (void)min_per_warp;
+        return cuda_status(cudaGetLastError());
+    } else {
     /* fast path (div_warp.cuh): pass A writing records, the rows, the longest-first order
      * over the whole call, pass B over the rows, the rows to the caller's
      * layout -- in chunks whose scratch stays below kDivScratchBytes */
@@ -431,6 +446,7 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
     }
     scratch_free(scratch, s);
     return cuda_status(e);
+    }
 }
 
 template <int N>
@@ -468,8 +484,12 @@ grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, u
         e = cudaGetLastError();
         if (order) scratch_free(order, s);
         return cuda_status(e);
-    } else {
+    } else if constexpr (N <= 64) {
         return run_scale_steps<N>(c, x, D, Du, ld, count, out, flags, s, min_per_warp, ldo);
+    } else {  // exact 52-bit steps one number per thread (no per-n shared memory)
+        k_scale<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
+                                                                Output<N>{out, ldo}, flags);
+        return cuda_status(cudaGetLastError());
     }
 }
 

@@ -41,8 +41,9 @@ __device__ __forceinline__ void eval_split(const Consts<N> &C, bool fp, Get get,
 }
 
 template <int N, bool FAST = false>
-__global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+__global__ void __launch_bounds__(256) k_eval(const __grid_constant__ CArg<N> CA, Operand<N> x, int64_t count,
                                               Er *__restrict__ out, uint8_t *__restrict__ flags, int fp_eighths) {
+    const Consts<N> &C = CA.get();
     const bool fp = warp_on_fp64(fp_eighths);
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = 0;
@@ -59,22 +60,23 @@ __global__ void __launch_bounds__(256) k_eval(const __grid_constant__ Consts<N> 
  * current one is evaluated (the common path is latency-bound on its loads
  * otherwise); the rare branch re-reads its residues from memory */
 template <int N, bool FAST = false>
-__global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                       int64_t count, Er *__restrict__ out,
                                                       uint8_t *__restrict__ flags, int fp_eighths) {
+    const Consts<N> &C = CA.get();
     const bool fp = warp_on_fp64(fp_eighths);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t cur[N];
     if (k < count) {
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) cur[i] = x.load(k, i);
     }
     for (; k < count; k += stride) {
         uint32_t nxt[N];
         const int64_t kn = k + stride;
         if (kn < count) {
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) nxt[i] = x.load(kn, i);
         }
         uint32_t f = 0;
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Co
         out[2 * k] = lo;
         out[2 * k + 1] = up;
         if (flags) flags[k] = (uint8_t)f;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) cur[i] = nxt[i];
     }
 }
@@ -99,10 +101,11 @@ __global__ void __launch_bounds__(256, 2) k_eval_pipe(const __grid_constant__ Co
 constexpr int kEvalClaim = 8;  // numbers per lane per claim
 
 template <int N, bool FAST = false>
-__global__ void __launch_bounds__(256, 2) k_eval_claim(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(256, 2) k_eval_claim(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                        int64_t count, Er *__restrict__ out,
                                                        uint8_t *__restrict__ flags, int fp_eighths,
                                                        unsigned long long *__restrict__ ctr) {
+    const Consts<N> &C = CA.get();
     const bool fp = warp_on_fp64(fp_eighths);
     const int lane = threadIdx.x & 31;
     auto claim = [&]() -> int64_t {
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(256, 2) k_eval_claim(const __grid_constant__ C
     int64_t k = base + lane;
     uint32_t cur[N];
     if (k < count) {
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) cur[i] = x.load(k, i);
     }
     while (base < count) {  // warp-uniform
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(256, 2) k_eval_claim(const __grid_constant__ C
         const int64_t kn = nbase + 32 * nj + lane;
         uint32_t nxt[N];
         if (kn < count) {
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) nxt[i] = x.load(kn, i);
         }
         if (k < count) {
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(256, 2) k_eval_claim(const __grid_constant__ C
             out[2 * k + 1] = up;
             if (flags) flags[k] = (uint8_t)f;
         }
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) cur[i] = nxt[i];
         base = nbase;
         j = nj;
@@ -159,8 +162,9 @@ __device__ __noinline__ void eval_tight_fallback(const Consts<N> &C, const Opera
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_eval_tight(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+__global__ void __launch_bounds__(256) k_eval_tight(const __grid_constant__ CArg<N> CA, Operand<N> x, int64_t count,
                                                     Er *__restrict__ out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = 0, bad = 0;
         Er lo, up;
@@ -181,15 +185,16 @@ __global__ void __launch_bounds__(256) k_eval_tight(const __grid_constant__ Cons
 /* four consecutive numbers per thread with 16-byte loads of each modulus
  * slice (SoA, leading dimension a multiple of 4, 16-byte aligned base) */
 template <int N>
-__global__ void __launch_bounds__(256, 2) k_eval_tight_soa4(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(256, 2) k_eval_tight_soa4(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                             int64_t count, Er *__restrict__ out,
                                                             uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     const int64_t quads = count / 4;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < quads; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t k = 4 * t;
         Fx128 f[4];
         uint32_t bad = 0;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(x.base + (int64_t)i * x.ld + k));
             const uint32_t m = C.m[i], c0 = C.c128w_0[i], c1 = C.c128w_1[i], c2 = C.c128w_2[i], c3 = C.c128w_3[i];
@@ -223,8 +228,9 @@ __global__ void __launch_bounds__(256, 2) k_eval_tight_soa4(const __grid_constan
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_cmp(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> y,
+__global__ void __launch_bounds__(256) k_cmp(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> y,
                                              int64_t count, int32_t *__restrict__ out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = 0;
         Er xl, xu, yl, yu;
@@ -263,15 +269,16 @@ __device__ __forceinline__ void cmp_finish(const Consts<N> &C, const Operand<N> 
 }
 
 template <int N>
-__global__ void __launch_bounds__(256, 3) k_cmp_fast_soa4(const __grid_constant__ Consts<N> C, Operand<N> x,
+__global__ void __launch_bounds__(256, 3) k_cmp_fast_soa4(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                           Operand<N> y, int64_t count, int32_t *__restrict__ out,
                                                           uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     const int64_t quads = count / 4;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < quads; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t k = 4 * t;
         uint64_t a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0};
         uint32_t bad = 0;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             const uint4 xv = __ldcs(reinterpret_cast<const uint4 *>(x.base + (int64_t)i * x.ld + k));
             const uint4 yv = __ldcs(reinterpret_cast<const uint4 *>(y.base + (int64_t)i * y.ld + k));
@@ -310,16 +317,17 @@ __global__ void __launch_bounds__(256, 3) k_cmp_fast_soa4(const __grid_constant_
 }
 
 template <int N>
-__global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ Consts<N> C, Operand<N> x, Operand<N> y,
+__global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> y,
                                                      int64_t count, int32_t *__restrict__ out,
                                                      uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint64_t a = 0, b = 0;
         uint32_t bad = 0;
         if (x.ld == 0 && (N % 4) == 0) {  /* AoS: the number's residues are contiguous */
             const uint4 *px = reinterpret_cast<const uint4 *>(x.base + k * N);
             const uint4 *py = reinterpret_cast<const uint4 *>(y.base + k * N);
-#pragma unroll
+GRNS_UNROLL_TO(N / 4)
             for (int q = 0; q < N / 4; q++) {
                 const uint4 xv = __ldcs(px + q), yv = __ldcs(py + q);
                 const uint32_t xs[4] = {xv.x, xv.y, xv.z, xv.w}, ys[4] = {yv.x, yv.y, yv.z, yv.w};
@@ -332,7 +340,7 @@ __global__ void __launch_bounds__(256, 3) k_cmp_fast(const __grid_constant__ Con
                 }
             }
         } else {
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) {
                 const uint32_t xi = x.load_cs(k, i), yi = y.load_cs(k, i);
                 bad |= (uint32_t)(xi >= C.m[i]) | (uint32_t)(yi >= C.m[i]);

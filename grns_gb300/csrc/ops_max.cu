@@ -70,9 +70,10 @@ __device__ __forceinline__ Cand block_reduce(const Consts<N> &C, const Operand<N
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) k_max(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+__global__ void __launch_bounds__(256) k_max(const __grid_constant__ CArg<N> CA, Operand<N> x, int64_t count,
                                              uint32_t *__restrict__ out_value, int64_t *__restrict__ out_index,
                                              unsigned *__restrict__ ticket, Cand *__restrict__ partial) {
+    const Consts<N> &C = CA.get();
     __shared__ Cand sm[32];
     __shared__ bool last;
     Cand best{{0.0, 0}, {0.0, 0}, -1};
@@ -156,9 +157,10 @@ __device__ __forceinline__ FCand fblock_reduce(const Consts<N> &C, const Operand
 }
 
 template <int N>
-__global__ void __launch_bounds__(256, 3) k_max_fast(const __grid_constant__ Consts<N> C, Operand<N> x, int64_t count,
+__global__ void __launch_bounds__(256, 3) k_max_fast(const __grid_constant__ CArg<N> CA, Operand<N> x, int64_t count,
                                                   uint32_t *__restrict__ out_value, int64_t *__restrict__ out_index,
                                                   unsigned *__restrict__ ticket, FCand *__restrict__ partial) {
+    const Consts<N> &C = CA.get();
     __shared__ FCand sm[32];
     __shared__ bool last;
     FCand best{0, -1};
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(256, 3) k_max_fast(const __grid_constant__ Con
              t += (int64_t)gridDim.x * blockDim.x) {
             const int64_t k = 4 * t;
             uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i++) {
                 const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(x.base + (int64_t)i * x.ld + k));
                 const uint32_t cl = C.c64l[i], ch = C.c64h[i];

@@ -17,9 +17,10 @@
 namespace grns {
 
 template <int N>
-__global__ void __launch_bounds__(256) k_mpint(const __grid_constant__ Consts<N> C, int op,
+__global__ void __launch_bounds__(256) k_mpint(const __grid_constant__ CArg<N> CA, int op,
                                                const MpInt<N> *__restrict__ x, const MpInt<N> *__restrict__ y,
                                                int64_t count, MpInt<N> *__restrict__ out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         MpInt<N> a = x[k], b = y[k], r;
         clear_pad(r);
@@ -155,10 +156,11 @@ __device__ __forceinline__ void mp_chunk(const Consts<N> &C, const uint4 *K, int
  * while the warp computes chunk i in place and bulk-stores it.  A stage is
  * reloaded only after the store that read it has finished reading. */
 template <int N>
-__global__ void __launch_bounds__(256) k_mpint_bulk(const __grid_constant__ Consts<N> C, int op,
+__global__ void __launch_bounds__(256) k_mpint_bulk(const __grid_constant__ CArg<N> CA, int op,
                                                     const MpInt<N> *__restrict__ x, const MpInt<N> *__restrict__ y,
                                                     int64_t count, MpInt<N> *__restrict__ out,
                                                     uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     extern __shared__ uint4 mp_smem[];
     __shared__ uint4 K[N];  // per modulus: m, mu, b (the lanes of a warp read different moduli at once)
     constexpr int RB = (int)sizeof(MpInt<N>);
@@ -258,12 +260,13 @@ __global__ void __launch_bounds__(256) k_mpint_gather(const MpInt<N> *__restrict
  * quotient and remainder columns; flags holds the division's flags on entry.
  * A zero divisor or an invalid digit gives the zero record. */
 template <int N>
-__global__ void __launch_bounds__(128) k_mpint_div_finish(const __grid_constant__ Consts<N> C,
+__global__ void __launch_bounds__(128) k_mpint_div_finish(const __grid_constant__ CArg<N> CA,
                                                           const MpInt<N> *__restrict__ x,
                                                           const MpInt<N> *__restrict__ y,
                                                           const uint32_t *__restrict__ q,
                                                           const uint32_t *__restrict__ r, int64_t count,
                                                           MpInt<N> *__restrict__ out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t f = flags[k];
         MpInt<N> res;
@@ -301,15 +304,18 @@ template <int N>
 static grns_status run_mpint(const grns_ctx *c, int op, const void *x, const void *y, int64_t count, void *out,
                              uint8_t *flags, cudaStream_t s) {
     const int B = 256;
-    if ((((uintptr_t)x | (uintptr_t)y | (uintptr_t)out) & 15) == 0) {  // chunks start 16-byte aligned
-        /* 8 warps: 2 mbarriers each, then 2 stages of x and y chunks each */
-        constexpr size_t smem = 16 * 8 + (size_t)(B / 32) * 4 * kMpRecs * sizeof(MpInt<N>);
-        static std::atomic<int> occ[kOccDevices];  // resident blocks per SM, per device
-        const int per_sm = resident_blocks(occ, c, k_mpint_bulk<N>, B, smem);
-        const int64_t chunks = (count + kMpRecs - 1) / kMpRecs;
-        k_mpint_bulk<N><<<grid_for(c, chunks * 32, B, per_sm), B, smem, s>>>(
-            consts_of<N>(c), op, (const MpInt<N> *)x, (const MpInt<N> *)y, count, (MpInt<N> *)out, flags);
-        return cuda_status(cudaGetLastError());
+    /* staged chunks up to 64 moduli (above, 4 kMpRecs records a warp exceed shared memory) */
+    if constexpr (N <= 64) {
+        if ((((uintptr_t)x | (uintptr_t)y | (uintptr_t)out) & 15) == 0) {  // chunks start 16-byte aligned
+            /* 8 warps: 2 mbarriers each, then 2 stages of x and y chunks each */
+            constexpr size_t smem = 16 * 8 + (size_t)(B / 32) * 4 * kMpRecs * sizeof(MpInt<N>);
+            static std::atomic<int> occ[kOccDevices];  // resident blocks per SM, per device
+            const int per_sm = resident_blocks(occ, c, k_mpint_bulk<N>, B, smem);
+            const int64_t chunks = (count + kMpRecs - 1) / kMpRecs;
+            k_mpint_bulk<N><<<grid_for(c, chunks * 32, B, per_sm), B, smem, s>>>(
+                consts_of<N>(c), op, (const MpInt<N> *)x, (const MpInt<N> *)y, count, (MpInt<N> *)out, flags);
+            return cuda_status(cudaGetLastError());
+        }
     }
     k_mpint<N><<<grid_for(c, count, B), B, 0, s>>>(consts_of<N>(c), op, (const MpInt<N> *)x, (const MpInt<N> *)y,
                                                   count, (MpInt<N> *)out, flags);

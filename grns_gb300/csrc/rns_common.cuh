@@ -3,7 +3,9 @@
  *
  *   * per-moduli-set constant block passed to every kernel by value (so the
  *     per-modulus constants sit in the kernel-parameter constant bank and are
- *     read with compile-time offsets from fully unrolled loops);
+ *     read with compile-time offsets from fully unrolled loops); the
+ *     256-moduli block exceeds the parameter space and is passed by the
+ *     address of its device copy (CArg);
  *   * modular arithmetic on the integer pipe: Shoup multiplication by a
  *     constant, Barrett multiplication of two residues, branch-free add/sub;
  *   * extended-range float (er_float_t) helpers with the reference's exact
@@ -14,13 +16,23 @@
  */
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
+#include <type_traits>
 
 #ifdef __CUDACC__
 #define GRNS_HD __host__ __device__ __forceinline__
 #else
 #define GRNS_HD inline
 #endif
+
+/* Loops over the moduli are unrolled fully up to 64 moduli.  For 128 and 256
+ * they stay rolled: their per-number arrays live in local memory either way,
+ * and full unrolling there costs minutes of compile time per kernel.
+ * GRNS_UNROLL_TO(B) is for a loop of at most B trips in a template on N. */
+#define GRNS_PRAGMA_(x) _Pragma(#x)
+#define GRNS_UNROLL_TO(B) GRNS_PRAGMA_(unroll((N) > 64 ? 1 : (B)))
+#define GRNS_UNROLL_N GRNS_UNROLL_TO(N)
 
 #ifndef __CUDACC__
 struct uint4 { uint32_t x, y, z, w; };
@@ -29,7 +41,7 @@ struct uint2 { uint32_t x, y; };
 
 namespace grns {
 
-constexpr int kMaxModuli = 64;
+constexpr int kMaxModuli = 256;
 constexpr int kScaleStep = 30;  // RNS_P2_SCALING_THRESHOLD (reference src/params.h:22)
 constexpr int kDivB = 48;       // quotient bits per step of the integer division
 constexpr int kScaleB = 52;     // bits per step of the integer power-of-two scaling
@@ -38,10 +50,12 @@ constexpr int kPow2NegRows = 64;  // rows j = 0..63 of the 2^-j mod m_i table
 constexpr int pow2_hi_rows(int log2M) { return (log2M + 64) / 64 + 1; }
 /* binary <-> RNS conversion: integers as 32-bit little-endian limbs, worked
  * on in 26-bit chunks (26 + 30.42 bits per product: up to 158 products, or
- * 64 moduli, sum below 2^64) */
+ * 64 moduli, sum below 2^64; longer sums fold every kBinFold products or, for
+ * more than 64 moduli, add in 128 bits) */
 constexpr int kBinChunk = 26;
-constexpr int kBinMaxLimbs = 128;                                   // 4096-bit inputs
-constexpr int kBinMaxChunks = (32 * kBinMaxLimbs + kBinChunk - 1) / kBinChunk;  // 158
+constexpr int kBinMaxLimbs = 256;                                   // 8192-bit inputs
+constexpr int kBinMaxChunks = (32 * kBinMaxLimbs + kBinChunk - 1) / kBinChunk;  // 316
+constexpr int kBinFold = 128;
 
 /* levels of the pairwise summation tree over n leaves */
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c((n + 1) / 2); }
@@ -52,11 +66,13 @@ struct Er {  // er_float_t
 };
 
 /* Constant block of one moduli set, specialised on the moduli count N. */
-/* the moduli counts kernels are built for: every n from 4 to 16 (the
- * reference's params catalogue up to 16 moduli), 32 and 64 */
+/* the moduli counts kernels are built for: every n from 4 to 16, 32, 64, 128
+ * and 256 (the sizes of the reference's params catalogue) */
 #define GRNS_FOR_EACH_N(X) \
-    X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(32) X(64)
-GRNS_HD constexpr bool supported_n(int n) { return (n >= 4 && n <= 16) || n == 32 || n == 64; }
+    X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(32) X(64) X(128) X(256)
+GRNS_HD constexpr bool supported_n(int n) {
+    return (n >= 4 && n <= 16) || n == 32 || n == 64 || n == 128 || n == 256;
+}
 
 /* words per row of the binary conversion tables: n rounded up to a multiple of 4 */
 GRNS_HD constexpr int bin_ld(int n) { return (n + 3) / 4 * 4; }
@@ -115,7 +131,24 @@ struct Consts {
     const uint32_t *bin_m26;    // [bin_chunks]         26-bit chunk c of M
     int bin_chunks;             // ceil(bits(M) / 26)
     int bin_limbs;              // ceil(bits(M) / 32): 32-bit limbs of an integer below M
+    const void *self;           // device copy of this block (set where kernels take it by address)
+    GRNS_HD const Consts &get() const { return *this; }
 };
+
+/* A kernel's constant-block parameter: the block itself while it fits the
+ * 32 KB kernel parameter space (with room for the other arguments), else the
+ * address of its device copy.  In the kernel: const Consts<N> &C = CA.get(). */
+constexpr size_t kParamConstsMax = 30 * 1024;
+template <int N>
+struct ConstsRef {
+    const Consts<N> *p;
+    GRNS_HD ConstsRef(const Consts<N> &c) : p(static_cast<const Consts<N> *>(c.self)) {}
+    GRNS_HD const Consts<N> &get() const { return *p; }
+};
+template <int N>
+using CArg = typename std::conditional<(sizeof(Consts<N>) > kParamConstsMax), ConstsRef<N>, Consts<N>>::type;
+template <int N>
+constexpr bool consts_by_address() { return sizeof(Consts<N>) > kParamConstsMax; }
 
 /* ---------------- modular arithmetic ---------------- */
 

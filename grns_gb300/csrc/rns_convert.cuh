@@ -2,7 +2,9 @@
  * grns_gb300 -- binary <-> RNS conversion, host+device arithmetic.
  *
  * Integers travel as little-endian 32-bit limbs.  Both directions work on
- * 26-bit chunks so that every sum of products fits one 64-bit word:
+ * 26-bit chunks so that every sum of products fits one 64-bit word (up to
+ * 64 moduli and kBinSumMax chunks; longer chunk sums are reduced every
+ * kBinFold products, and more than 64 moduli sum in 128 bits):
  *
  *   from binary (rns_from_binary, reference src/rnsbase.cuh:253, which takes
  *   mpz_mod_ui per modulus): x_i = sum_c chunk_c * (2^(26 c) mod m_i) mod m_i,
@@ -24,6 +26,14 @@
 namespace grns {
 
 constexpr uint32_t kBinMask = (1u << kBinChunk) - 1u;
+/* products of a 26-bit chunk and a residue below 2^30.42 whose sum stays below 2^64 */
+constexpr int kBinSumMax = 158;
+
+/* the CRT chunk sums: 64-bit up to 64 moduli, 128-bit above (n products of 56.42 bits) */
+template <int N>
+using BinAcc = typename std::conditional<(N > 64), unsigned __int128, uint64_t>::type;
+template <int N>
+using BinSAcc = typename std::conditional<(N > 64), __int128, int64_t>::type;
 
 /* chunk c (bits [26 c, 26 c + 26)) of the little-endian limbs row[0..nlimbs) */
 GRNS_HD uint32_t bin_chunk(const uint32_t *row, int nlimbs, int c) {
@@ -49,7 +59,10 @@ GRNS_HD void from_binary(const Consts<N> &C, const uint32_t *row, int nlimbs, ui
     const int chunks = (32 * nlimbs + kBinChunk - 1) / kBinChunk;
     for (int i = 0; i < N; i++) {
         uint64_t acc = 0;
-        for (int c = 0; c < chunks; c++) acc += (uint64_t)bin_chunk(row, nlimbs, c) * C.bin_p26[c * bin_ld(N) + i];
+        for (int c = 0; c < chunks; c++) {
+            acc += (uint64_t)bin_chunk(row, nlimbs, c) * C.bin_p26[c * bin_ld(N) + i];
+            if (chunks > kBinSumMax && c % kBinFold == kBinFold - 1) acc = bin_mod64<N>(C, i, acc);
+        }
         res[i] = bin_mod64<N>(C, i, acc);
     }
 }
@@ -58,7 +71,7 @@ GRNS_HD void from_binary(const Consts<N> &C, const uint32_t *row, int nlimbs, ui
 template <int N>
 GRNS_HD uint32_t bin_rank(const Consts<N> &C, const uint32_t *s) {
     uint64_t S0 = 0, S1 = 0, S2 = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint64_t p0 = (uint64_t)s[i] * C.c96_0[i];
         const uint64_t p1 = (uint64_t)s[i] * C.c96_1[i];
@@ -74,11 +87,11 @@ GRNS_HD uint32_t bin_rank(const Consts<N> &C, const uint32_t *s) {
 /* one chunk of sum_i s_i M_i - kk M plus the signed carry */
 template <int N>
 GRNS_HD uint32_t bin_crt_chunk(const Consts<N> &C, const uint32_t *s, uint32_t kk, int c, int64_t &carry) {
-    uint64_t acc = 0;
+    BinAcc<N> acc = 0;
     const uint32_t *row = C.bin_mi26 + (size_t)c * bin_ld(N);
-    for (int i = 0; i < N; i++) acc += (uint64_t)s[i] * row[i];
-    const int64_t v = (int64_t)acc - (int64_t)kk * C.bin_m26[c] + carry;
-    carry = v >> kBinChunk;  // floor division (arithmetic shift)
+    for (int i = 0; i < N; i++) acc += (BinAcc<N>)s[i] * row[i];
+    const BinSAcc<N> v = (BinSAcc<N>)acc - (BinSAcc<N>)kk * C.bin_m26[c] + carry;
+    carry = (int64_t)(v >> kBinChunk);  // floor division (arithmetic shift)
     return (uint32_t)v & kBinMask;
 }
 
@@ -111,7 +124,7 @@ template <int N, class Get>
 GRNS_HD bool to_binary(const Consts<N> &C, Get x, uint32_t *d, int stride) {
     uint32_t s[N];
     bool bad = false;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t v = x(i);
         bad |= v >= C.m[i];

@@ -51,7 +51,7 @@ struct Operand {
 #pragma unroll 4
             for (int i = 0; i < N; i++) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (int64_t)i * ld + k));
         } else {
-#pragma unroll
+GRNS_UNROLL_N
             for (int i = 0; i < N; i += 32) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + k * N + i));
         }
     }
@@ -122,7 +122,7 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
     uint32_t s[N];
     PTree<N, false> tl;
     PTree<N, true> tu;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         s[i] = mulmod_shoup(get(i), C.w[i], C.w_sh[i], C.m[i]);
         double d = u32_to_double(s[i]);
@@ -162,7 +162,7 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
         if (k < 0 || k > C.log2M) { flags |= kFlagIterCap; break; }
         const uint32_t *p2 = C.pow2 + (int64_t)k * N;
         PTree<N, true> t2;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) {
             s[i] = mulmod_barrett(s[i], __ldg(p2 + i), C.m[i], C.mu[i], C.b[i]);
             t2.push(i, __dmul_ru(u32_to_double(s[i]), C.rru[i]));
@@ -172,7 +172,7 @@ __device__ __noinline__ void eval_full(const Consts<N> &C, Get get, Er &low, Er 
         K += k;
     }
     PTree<N, false> t3;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) t3.push(i, __dmul_rd(u32_to_double(s[i]), C.rrd[i]));
     suml = t3.total();
     suml = __dsub_rd(suml, u32_to_double(__double2uint_rz(suml)));
@@ -193,7 +193,7 @@ template <int N, class Get, bool FAST = false>
 __device__ __forceinline__ int eval_fp64(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
     PTree<N, false> tl;
     PTree<N, true> tu;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t xi = get(i);
         bad |= (uint32_t)(xi >= C.m[i]);
@@ -324,7 +324,7 @@ template <int N>
 __device__ __forceinline__ uint32_t rank_ref(const Consts<N> &C, const uint32_t *x, const uint32_t *c, bool checked) {
     PTree<N, true> tu;
     PTree<N, false> tl;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         double dd = u32_to_double(c[i]);
         tu.push(i, __dmul_ru(dd, C.rru[i]));
@@ -347,12 +347,12 @@ __device__ __forceinline__ void scaling_step(const Consts<N> &C, uint32_t *y, ui
     const uint32_t mask = (j >= 32) ? 0xffffffffu : ((1u << j) - 1u);
     const uint32_t *hrow = C.mi_pow2 + (int64_t)(j - 1) * N;
     uint64_t acc = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) acc += (uint64_t)((__ldg(hrow + i) * c[i]) & mask);
     uint32_t res = (uint32_t)((acc - (uint64_t)k * __ldg(C.m_pow2 + j - 1)) & mask);
     const uint32_t *inv = C.pow2_inv + (int64_t)(j - 1) * N;
     const uint32_t *inv_sh = C.pow2_inv_sh + (int64_t)(j - 1) * N;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         uint32_t m = C.m[i];
         uint32_t rm = res % m;
@@ -366,13 +366,13 @@ __device__ __forceinline__ void scaling_step(const Consts<N> &C, uint32_t *y, ui
 template <int N>
 __device__ __noinline__ void scale2pow_ref(const Consts<N> &C, uint32_t *res, const uint32_t *x, unsigned D) {
     uint32_t c[N], cur[N];
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) cur[i] = x[i];
     unsigned t = D / kScaleStep;
     bool first = true;
 #pragma unroll 1
     while (t > 0) {
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) c[i] = mulmod_shoup(cur[i], C.w[i], C.w_sh[i], C.m[i]);
         uint32_t k = rank_ref<N>(C, cur, c, first);
         scaling_step<N>(C, cur, k, kScaleStep, cur, c);
@@ -381,12 +381,12 @@ __device__ __noinline__ void scale2pow_ref(const Consts<N> &C, uint32_t *res, co
     }
     unsigned dr = D % kScaleStep;
     if (dr > 0) {
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) c[i] = mulmod_shoup(cur[i], C.w[i], C.w_sh[i], C.m[i]);
         uint32_t k = rank_ref<N>(C, cur, c, first);
         scaling_step<N>(C, cur, k, dr, cur, c);
     }
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) res[i] = cur[i];
 }
 

@@ -105,7 +105,7 @@ GRNS_HD uint32_t reduce64(const Consts<N> &C, int i, uint64_t v) {
 template <int N, class Get>
 GRNS_HD uint64_t fx64(const Consts<N> &C, Get get) {
     uint64_t a = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t x = get(i);
         a += (uint64_t)x * C.c64l[i];
@@ -119,7 +119,7 @@ GRNS_HD uint64_t fx64(const Consts<N> &C, Get get) {
 template <int N, class GetS>
 GRNS_HD u128 fx96_s(const Consts<N> &C, GetS gets) {
     uint64_t S0 = 0, S1 = 0, S2 = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         uint32_t s = gets(i);
         uint64_t p0 = (uint64_t)s * C.c96_0[i];
@@ -138,7 +138,7 @@ GRNS_HD u128 fx96_k(const Consts<N> &C, Get get, int k) {
     const uint4 *row = C.c96k + (int64_t)k * N;
     uint64_t S0 = 0, S1 = 0;
     uint32_t S2 = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t x = get(i);
 #ifdef __CUDA_ARCH__
@@ -161,7 +161,7 @@ template <int N, class Get>
 GRNS_HD u128 fx96w(const Consts<N> &C, Get get) {
     uint64_t S0 = 0, S1 = 0;
     uint32_t S2 = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t x = get(i);
         const uint64_t p0 = (uint64_t)x * C.c96w_0[i];
@@ -183,8 +183,8 @@ GRNS_HD u128 fx96(const Consts<N> &C, Get get) {
  * The common path of rns_eval_compute (src/rnseval.cuh:182-215) multiplies
  * s_i = x_i w_i mod m_i by RNS_MODULI_RECIP_RD / _RU with rounding down / up
  * and adds the products pairwise with rounding down / up.  Every value on it
- * is 0 or a double in [2^-31, 64) with 53 significant bits, i.e. an integer
- * multiple of 2^17 at scale 2^100 below 2^106.  So each operation is computed
+ * is 0 or a double in [2^-31, n) with 53 significant bits, i.e. an integer
+ * multiple of 2^17 at scale 2^100 below 2^108 (n <= 256).  So each operation is computed
  * exactly as a 128-bit integer and rounded to 53 significant bits by masking
  * (a nonzero value is >= 2^69 at this scale, so its bit length is 64 +
  * bitlen(hi) and the rounding position 11 + bitlen(hi) lies in the low word):
@@ -276,7 +276,7 @@ template <int N, class Get, bool FAST = false>
 GRNS_HD int eval_int(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
     Fx100Tree<N, false> tl;
     Fx100Tree<N, true> tu;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t xi = get(i);
         bad |= (uint32_t)(xi >= C.m[i]);
@@ -429,7 +429,7 @@ GRNS_HD bool eval_tight_finish(u128 T, uint64_t E, Er &low, Er &upp) {
 template <int N, class Get>
 GRNS_HD bool eval_tight(const Consts<N> &C, Get get, Er &low, Er &upp, uint32_t &bad) {
     Fx128 f;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t x = get(i);
         bad |= (uint32_t)(x >= C.m[i]);
@@ -599,6 +599,8 @@ GRNS_HD_RARE int dv_cmp_vec(const Consts<N> &C, const uint32_t *a, const uint32_
 }
 
 enum : int { kNormMore = 0, kNormOk = 1, kNormNear = 2, kNormCap = 3 };
+/* normalisation steps of 48 bits a nonzero value can need (M below 2^(32 kMaxModuli)) */
+constexpr int kNormMaxSteps = 32 * kMaxModuli / kDivB + 2;
 
 /* One normalisation step of a nonzero Z: U = fx96w(Z 2^k).  U >= 2^43 fixes
  * the magnitude: Z 2^k / M in [U - E, U] / 2^96, U >= 2^43.  Below that Z 2^k
@@ -614,7 +616,7 @@ GRNS_HD int dn_step(const Consts<N> &C, u128 U, int &k, int &guard) {
         return kNormOk;
     }
     k += kDivB;
-    if (++guard > 64 || k > C.log2M) return kNormCap;
+    if (++guard > kNormMaxSteps || k > C.log2M) return kNormCap;
     return kNormMore;
 }
 
@@ -1040,11 +1042,11 @@ template <int N>
 GRNS_HD void scaling_step_big(const Consts<N> &C, uint32_t *y, uint32_t k, int j, const uint32_t *x,
                               const uint32_t *c) {
     uint64_t acc = 0;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) acc += (uint64_t)c[i] * C.mi64[i];
     const uint64_t res = (acc - (uint64_t)k * C.m64) & ((((uint64_t)1) << j) - 1);
     const uint32_t *inv = C.pow2neg + (int64_t)j * N, *inv_sh = C.pow2neg_sh + (int64_t)j * N;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t m = C.m[i];
         y[i] = mulmod_shoup(submod(x[i], reduce53<N>(C, i, res), m), ldg_u32(inv + i), ldg_u32(inv_sh + i), m);
@@ -1057,26 +1059,26 @@ GRNS_HD void scaling_step_big(const Consts<N> &C, uint32_t *y, uint32_t k, int j
 template <int N>
 GRNS_HD void scale_fast(const Consts<N> &C, uint32_t *res, const uint32_t *x, unsigned D) {
     uint32_t cur[N], c[N];
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) cur[i] = x[i];
     bool small = false;
     if (D > (unsigned)C.log2M) D = 0, small = true;  // X < M < 2^(log2M + 1): the result is 0
     if (small) {
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) res[i] = 0;
         return;
     }
 #pragma unroll 1
     for (unsigned left = D; left > 0;) {
         const int j = left < (unsigned)kScaleB ? (int)left : kScaleB;
-#pragma unroll
+GRNS_UNROLL_N
         for (int i = 0; i < N; i++) c[i] = mulmod_shoup(cur[i], C.w[i], C.w_sh[i], C.m[i]);
         const uint32_t k = rank_fast<N>(C, cur, c, small);
         scaling_step_big<N>(C, cur, k, j, cur, c);
         left -= (unsigned)j;
         small = true;
     }
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) res[i] = cur[i];
 }
 

@@ -152,7 +152,7 @@ __device__ __forceinline__ void mpint_addsub(const Consts<N> &C, MpInt<N> &res, 
     Er lo, up;
     const bool minus = mpint_addsub_eval(head_of(x), head_of(y), sub, lo, up);
     const int sx = x.sign, sy = sub ? (y.sign ^ 1) : y.sign;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) res.digits[i] = mpint_addsub_digit(x.digits[i], y.digits[i], C.m[i], sx, sy, minus, flags);
     res.sign = minus;
     res.eval[0] = lo;
@@ -166,7 +166,7 @@ __device__ __forceinline__ void mpint_mul(const Consts<N> &C, MpInt<N> &res, con
     res.eval[0] = er_md_i<false>(x.eval[0], y.eval[0], C.unit_upp, C.unit_rcp_upp);
     res.eval[1] = er_md_i<true>(x.eval[1], y.eval[1], C.unit_low, C.unit_rcp_low);
     bool zero = true;
-#pragma unroll
+GRNS_UNROLL_N
     for (int i = 0; i < N; i++) {
         const uint32_t m = C.m[i], a = x.digits[i], b = y.digits[i];
         flags |= (a >= m || b >= m) ? kFlagInvalidInput : 0u;

@@ -66,8 +66,14 @@
 #define ON 64
 #include "grns_oracle_n.h"
 #undef ON
+#define ON 128
+#include "grns_oracle_n.h"
+#undef ON
+#define ON 256
+#include "grns_oracle_n.h"
+#undef ON
 
-#define OR_SUPPORTED(n) (((n) >= 4 && (n) <= 16) || (n) == 32 || (n) == 64)
+#define OR_SUPPORTED(n) (((n) >= 4 && (n) <= 16) || (n) == 32 || (n) == 64 || (n) == 128 || (n) == 256)
 
 /* mod_inverse semantics (src/rnsbase.cuh:121/:156): the inverse in [0, m). */
 static long or_inverse(long x, long m) {
@@ -236,6 +242,8 @@ int oracle_max_threads(void) {
         case 16: CALL(16); break;        \
         case 32: CALL(32); break;        \
         case 64: CALL(64); break;        \
+        case 128: CALL(128); break;      \
+        case 256: CALL(256); break;      \
         default: break;                      \
     }
 

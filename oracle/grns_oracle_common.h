@@ -21,7 +21,7 @@
 #include <stdint.h>
 #include <string.h>
 
-#define OR_MAXN 64
+#define OR_MAXN 256
 #define OR_T 30 /* RNS_P2_SCALING_THRESHOLD, reference src/params.h:22 */
 
 typedef struct { double frac; long exp; } or_er;          /* er_float_t, src/types.cuh:13 */

@@ -21,7 +21,7 @@ ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
 IV_DTYPE = np.dtype([("low", ER_DTYPE), ("upp", ER_DTYPE)])
 
 PATH_HOST, PATH_DEVICE, PATH_HOST_FAST, PATH_DEVICE_PARALLEL, PATH_DEVICE_FAST = 0, 1, 2, 3, 4
-SUPPORTED_N = (4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 32, 64)
+SUPPORTED_N = (4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 32, 64, 128, 256)
 
 _lib = None
 

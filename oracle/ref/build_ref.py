@@ -60,14 +60,14 @@ BASE = {
     "p64": "src/params/moduli-100-6400-bit/params.64m.1600b.h",  # 26-bit moduli
 }
 
-# the rest of the catalogue up to 64 moduli: catNN_nK = params.Km.*.h of the
+# the rest of the catalogue: catNN_nK = params.Km.*.h of the
 # family moduli-*-NN-bit (p16 / p32 / p64 above are cat69_n16 / cat4096_n32 /
 # cat6400_n64)
 _FAMILIES = {
     "69": ("moduli-10-69-bit", {4: 10, 5: 13, 6: 17, 7: 22, 8: 26, 9: 31, 10: 36, 11: 41, 12: 47, 13: 52, 14: 58,
                                 15: 63}),
-    "4096": ("moduli-64-4096-bit", {4: 64, 8: 128, 16: 256, 64: 1024}),
-    "6400": ("moduli-100-6400-bit", {4: 100, 8: 200, 16: 400, 32: 800}),
+    "4096": ("moduli-64-4096-bit", {4: 64, 8: 128, 16: 256, 64: 1024, 128: 2048, 256: 4096}),
+    "6400": ("moduli-100-6400-bit", {4: 100, 8: 200, 16: 400, 32: 800, 128: 3200, 256: 6400}),
 }
 CATALOGUE = {f"cat{fam}_n{n}": f"src/params/{d}/params.{n}m.{b}b.h"
              for fam, (d, sizes) in _FAMILIES.items() for n, b in sizes.items()}

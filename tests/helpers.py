@@ -8,11 +8,13 @@ from oracle.oracle import REFERENCE_DEFAULT_MODULI, greedy_moduli
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # moduli sets: the reference's shipped default (ref8), greedy 30-bit sets (gN),
 # three sets of the reference's params catalogue (pN: moduli 3..59, 17-bit,
-# 26-bit) and the catalogue's other files up to 64 moduli (catFAMILY_nK =
-# src/params/moduli-*-FAMILY-bit/params.Km.*.h)
+# 26-bit) and the catalogue's other files (catFAMILY_nK =
+# src/params/moduli-*-FAMILY-bit/params.Km.*.h; BIG_TAGS: 128 and 256 moduli)
 BASE_TAGS = ["ref8", "g8", "g12", "g32", "g64", "p16", "p32", "p64"]
 CATALOGUE_TAGS = ["cat69_n%d" % n for n in range(4, 16)] + ["cat4096_n%d" % n for n in (4, 8, 16, 64)] + \
     ["cat6400_n%d" % n for n in (4, 8, 16, 32)]
+BIG_TAGS = ["cat4096_n128", "cat6400_n128", "cat4096_n256", "cat6400_n256"]
+CATALOGUE_TAGS += BIG_TAGS
 TAGS = BASE_TAGS + CATALOGUE_TAGS
 
 ER_DTYPE = np.dtype([("frac", "<f8"), ("exp", "<i8")])
@@ -29,6 +31,26 @@ def moduli_for(tag):
 
 def golden(tag):
     return dict(np.load(os.path.join(GOLDEN, f"golden_{tag}.npz")))
+
+
+def thin_golden(g, n, keep=12):
+    """For 128 and 256 moduli, every k-th entry of each per-number array (the
+    rows stay aligned: arrays of one length are thinned alike; byte arrays of
+    intervals and mp_int records by record), so that the CPU suite stays
+    short: the reference's one-bit division runs ~log2 M steps per pair.
+    Smaller sets are returned whole."""
+    if n < 128:
+        return g
+    out = {}
+    for k, v in g.items():
+        rec = None
+        if v.dtype == np.uint8 and v.ndim == 1:
+            rec = 32 if k.startswith("eval") else mpint_dtype(n).itemsize
+            v = v.reshape(-1, rec)
+        if k not in ("moduli", "mpint_kat") and v.ndim and len(v) > keep:
+            v = v[::-(-len(v) // keep)]
+        out[k] = v.reshape(-1) if rec else v
+    return out
 
 
 def mpint_dtype(n):

@@ -15,7 +15,7 @@ struct Box {
     int n;
     HostTables T;
     std::vector<uint32_t> blob;
-    alignas(16) unsigned char consts[sizeof(Consts<64>)];
+    alignas(16) unsigned char consts[sizeof(Consts<kMaxModuli>)];
 };
 
 template <int N>
