@@ -67,9 +67,11 @@ const char *grns_version(void);
  * Replaces rns_const_init() (reference src/rnsbase.cuh:324) and
  * mpint_const_init() (src/mpint.cuh:20), which fill process-global tables;
  * here every moduli set is its own context, so several (e.g. n = 32 and
- * n = 64) can be resident together.  Supported n: every n from 4 to 16, 32
- * and 64 (the reference's params catalogue up to 64 moduli);
- * moduli odd, pairwise coprime, 3 <= m_i <= 1431655765. */
+ * n = 64) can be resident together.  Supported n: every n from 4 to 16, 32,
+ * 64, 128 and 256 (the sizes of the reference's params catalogue);
+ * moduli odd, pairwise coprime, 3 <= m_i <= 1431655765.  Above 64 moduli the
+ * division and scaling run one number per thread and the kernels' loops over
+ * the moduli stay rolled (correct results, not tuned throughput). */
 grns_status grns_ctx_create(const int32_t *moduli, int n, grns_ctx **out);
 grns_status grns_ctx_destroy(grns_ctx *ctx);
 
@@ -215,7 +217,7 @@ grns_status grns_mrc(grns_ctx *ctx, const int32_t *x, int64_t count, int layout,
 /* ---- binary <-> RNS conversion ----
  * Binary integers are number-major rows of `limbs` little-endian 32-bit
  * words (word l of number k at words[k * limbs + l]; GMP's
- * mpz_export(w, NULL, -1, 4, 0, 0, z) writes this form), limbs <= 128.
+ * mpz_export(w, NULL, -1, 4, 0, 0, z) writes this form), limbs <= 256.
  *   grns_from_binary      : out = residues of each nonnegative integer, as
  *                           rns_from_binary (reference src/rnsbase.cuh:253);
  *                           integers of M or more give their residues mod M.

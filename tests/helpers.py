@@ -53,6 +53,13 @@ def thin_golden(g, n, keep=12):
     return out
 
 
+def sized(n, small, large):
+    """random-input counts of a test: `small` up to 16 moduli, `large` up to
+    64, a quarter of `large` (at least 8) for 128 and 256 moduli, whose
+    oracle checks on the CPU cost ~log2 M steps per number"""
+    return small if n <= 16 else large if n <= 64 else max(8, large // 4)
+
+
 def mpint_dtype(n):
     off = ((4 * n + 4 + 7) // 8) * 8
     return np.dtype({"names": ["digits", "sign", "eval"], "formats": [("<i4", (n,)), "<i4", (ER_DTYPE, (2,))],

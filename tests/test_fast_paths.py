@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from grns_gb300 import workload as W
-from tests.helpers import IV_DTYPE as IV, TAGS, moduli_for
+from tests.helpers import IV_DTYPE as IV, TAGS, moduli_for, sized
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SMALL_SETS = [[3, 5, 7, 11], [3, 5, 7, 11, 13, 17, 19, 23], [3, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43]]
@@ -152,7 +152,7 @@ def test_random_and_special(fc, tag):
     M = f.M
     L = M.bit_length() - 1
     rng = random.Random(17)
-    N = 400 if f.n <= 16 else 120
+    N = sized(f.n, 400, 120)
     X = [rng.randrange(M) for _ in range(N)]
     Y = [rng.randrange(M) for _ in range(N)]
     # ties, neighbours, tiny and near-M values, powers of two
@@ -182,7 +182,7 @@ def test_division_quotient_boundaries(fc, tag):
     L = M.bit_length() - 1
     rng = random.Random(99)
     X, Dv = [], []
-    for _ in range(150 if f.n <= 16 else 60):
+    for _ in range(sized(f.n, 150, 60)):
         b = rng.randrange(1, L + 1)
         d = rng.randrange(1 << (b - 1), 1 << b)
         qmax = (M - 1) // d
@@ -250,7 +250,7 @@ def test_division_short_and_extreme_dividends(fc, tag):
     L = M.bit_length() - 1
     rng = random.Random(5)
     X, Dv = [], []
-    for _ in range(200 if f.n <= 16 else 80):
+    for _ in range(sized(f.n, 200, 80)):
         bx, bd = rng.randrange(1, L + 1), rng.randrange(1, L + 1)
         X.append(rng.randrange(1 << (bx - 1), 1 << bx))
         Dv.append(rng.randrange(1 << (bd - 1), 1 << bd))
@@ -375,11 +375,11 @@ def test_binary_conversion_exhaustive_small(fc, moduli):
     assert np.array_equal(f.from_binary(vals, limbs), x)
 
 
-@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("tag", TAGS + ["g128", "g256"])
 def test_binary_conversion(fc, tag):
     """rns_from_binary / rns_to_binary arithmetic against exact integers: uniform
     values, values of every bit length, near 0 and M (the rank estimate is one
-    too high there), inputs of M and more, up to 128 limbs"""
+    too high there), inputs of M and more, up to 256 limbs (past 158 chunks the sums fold)"""
     f = FC(fc, moduli_for(tag))
     rng = random.Random(11)
     vals = [rng.randrange(f.M) for _ in range(400)]
@@ -387,7 +387,7 @@ def test_binary_conversion(fc, tag):
     vals += list(range(0, 40)) + [f.M - k for k in range(1, 40)] + [f.M // 2 + d for d in (-1, 0, 1)]
     back, ok = f.to_binary(f.res(vals))
     assert back == vals and ok.all()
-    for limbs in (1, 3, (f.M.bit_length() + 31) // 32, 128):
+    for limbs in (1, 3, (f.M.bit_length() + 31) // 32, 128, 256):
         wide = [rng.randrange(1 << (32 * limbs)) for _ in range(60)] + [(1 << (32 * limbs)) - 1]
         assert np.array_equal(f.from_binary(wide, limbs), f.res([v % f.M for v in wide]))
     # a residue >= its modulus is refused

@@ -9,7 +9,7 @@ import pytest
 
 import grns_gb300 as G
 from oracle import oracle as O
-from tests.helpers import TAGS, golden, moduli_for, mpint_dtype
+from tests.helpers import TAGS, golden, moduli_for, mpint_dtype, sized
 
 pytestmark = pytest.mark.gpu
 
@@ -69,7 +69,7 @@ def test_to_binary(case, layout):
     assert LM == (orc.M.bit_length() + 31) // 32
     got = ctx.rns_to_binary(to_dev(g["x"], layout), layout=layout).cpu().numpy()
     assert got.view(np.uint32).tobytes() == g["tobin_words"].tobytes()
-    vals = edge_values(orc, random.Random(5), 3000 if orc.n <= 16 else 1000)
+    vals = edge_values(orc, random.Random(5), sized(orc.n, 3000, 1000))
     x = orc.exact.to_rns(vals)
     flags = torch.zeros(len(vals), dtype=torch.uint8, device="cuda")
     wide = ctx.rns_to_binary(to_dev(x, layout), layout=layout, limbs=LM + 3, flags=flags).cpu().numpy()
@@ -84,7 +84,7 @@ def test_from_binary(case, layout):
                    layout)
     assert np.array_equal(got, g["frombin_rns"])
     rng = random.Random(6)
-    for limbs in (1, 2, ctx.binary_limbs, 128):
+    for limbs in (1, 2, ctx.binary_limbs, 128, 256):
         vals = [rng.randrange(1 << (32 * limbs)) for _ in range(700)] + [0, (1 << (32 * limbs)) - 1]
         got = from_dev(ctx.rns_from_binary(limbs_dev(vals, limbs), layout=layout), layout)
         assert np.array_equal(got, orc.exact.to_rns([v % orc.M for v in vals])), limbs
@@ -98,6 +98,26 @@ def test_round_trip_and_partial_tiles(case):
         vals = [rng.randrange(orc.M) for _ in range(count)]
         x = ctx.rns_from_binary(limbs_dev(vals, ctx.binary_limbs))
         assert G.limbs_to_ints(ctx.rns_to_binary(x).cpu().numpy()) == vals
+
+
+@pytest.mark.parametrize("n", [128, 256])
+def test_round_trip_large_moduli(dev, n):
+    """n greedy 30-bit moduli: each CRT chunk sums n products of up to 56.4
+    bits, past 2^64 for n = 256 (the 128-bit sums); values of every size up
+    to M - 1, and 256-limb inputs reduced mod M"""
+    from oracle.oracle import greedy_moduli
+    mods = greedy_moduli(n)
+    ctx = G.RNSContext(mods)
+    M = 1
+    for m in mods:
+        M *= m
+    rng = random.Random(n)
+    vals = [rng.randrange(M) for _ in range(300)] + [M - 1, M - 2, 0, 1] + [rng.randrange(1 << b) for b in (1, 64, 3000)]
+    x = ctx.rns_from_binary(limbs_dev(vals, ctx.binary_limbs))
+    assert G.limbs_to_ints(ctx.rns_to_binary(x).cpu().numpy()) == vals
+    wide = [rng.randrange(1 << (32 * 256)) for _ in range(200)] + [(1 << (32 * 256)) - 1]
+    y = ctx.rns_from_binary(limbs_dev(wide, 256))
+    assert G.limbs_to_ints(ctx.rns_to_binary(y).cpu().numpy()) == [v % M for v in wide]
 
 
 def test_invalid_residue_flagged(case):
@@ -123,7 +143,7 @@ def test_mpint_binary(case):
     assert words.cpu().numpy().view(np.uint32).tobytes() == g["mpint_tobin_words"].tobytes()
     assert np.array_equal(signs.cpu().numpy(), g["mpint_tobin_signs"])
     rng = random.Random(8)
-    vals = [rng.choice((-1, 1)) * v for v in edge_values(orc, rng, 800 if orc.n <= 16 else 300)]
+    vals = [rng.choice((-1, 1)) * v for v in edge_values(orc, rng, sized(orc.n, 800, 300))]
     mags = [abs(v) for v in vals]
     sg = torch.tensor([1 if v < 0 else 0 for v in vals], dtype=torch.int32, device="cuda")
     rec = ctx.mpint_set_binary(limbs_dev(mags, ctx.binary_limbs), sg).cpu().numpy().view(dt)

@@ -9,7 +9,7 @@ import pytest
 
 from grns_gb300 import workload as W
 from oracle import oracle as O
-from tests.helpers import IV_DTYPE, TAGS, golden, moduli_for, mpint_dtype, product_safe_bits
+from tests.helpers import IV_DTYPE, TAGS, golden, moduli_for, mpint_dtype, product_safe_bits, sized
 
 pytestmark = pytest.mark.gpu
 
@@ -136,7 +136,7 @@ def test_eval_fast(case, layout):
     if len(xs) == 0 or np.array_equal(ctx.device_ceil_log2(xs), np.ceil(np.log2(xs)).astype(np.int32)):
         assert got.tobytes() == g["eval_fast_dev"].tobytes()
     rng = random.Random(9)
-    vals = [rng.randrange(orc.M // 2) for _ in range(3000 if orc.n <= 16 else 1000)]
+    vals = [rng.randrange(orc.M // 2) for _ in range(sized(orc.n, 3000, 1000))]
     vals += [rng.randrange(1, 1 << rng.randrange(1, orc.log2M)) for _ in range(300)]
     x = orc.exact.to_rns(vals)
     flags = flags_buf(len(x))
@@ -151,7 +151,7 @@ def test_eval_fast(case, layout):
 @pytest.mark.parametrize("layout", ["soa", "aos"])
 def test_eval_random_bit_exact_and_enclosing(case, layout):
     tag, ctx, orc, g = case
-    N = 6000 if orc.n <= 16 else 2000
+    N = sized(orc.n, 6000, 2000)
     x = W.uniform_residues(orc.moduli, N, seed=101, stream=W.S_X, layout="aos")
     # sprinkle small values (refinement loop) and values near M (ambiguity branch)
     rng = random.Random(5)
@@ -173,7 +173,7 @@ def test_cmp(case, layout, path):
     tag, ctx, orc, g = case
     got = ctx.rns_cmp(to_dev(g["x"], layout), to_dev(g["y"], layout), layout=layout).cpu().numpy()
     assert np.array_equal(got, g["cmp_dev"])
-    N = 8000 if orc.n <= 16 else 2000
+    N = sized(orc.n, 8000, 2000)
     x = W.uniform_residues(orc.moduli, N, seed=7, stream=W.S_X, layout="aos")
     y = W.uniform_residues(orc.moduli, N, seed=7, stream=W.S_Y, layout="aos")
     y[::7] = x[::7]                      # equal pairs
@@ -188,10 +188,12 @@ def test_cmp(case, layout, path):
 @pytest.mark.parametrize("layout", ["soa", "aos"])
 def test_div(case, layout, path):
     tag, ctx, orc, g = case
+    if orc.n >= 128 and path == "reference" and layout == "aos":
+        pytest.skip("the reference's one-bit division at 2048 to 6400 bits: checked in the SoA layout")
     q, r = ctx.rns_div(to_dev(g["xd"], layout), to_dev(g["d"], layout), layout=layout)
     assert np.array_equal(from_dev(q, layout), g["div_q_dev"])
     assert np.array_equal(from_dev(r, layout), g["div_r_dev"])
-    N = (400 if orc.n <= 16 else 120) if path == "fast" else (100 if orc.n <= 16 else 24)
+    N = sized(orc.n, 400, 120) if path == "fast" else sized(orc.n, 100, 24)
     x = W.uniform_residues(orc.moduli, N, seed=3, stream=W.S_X, layout="aos")
     d, dv = W.divisors(orc.moduli, orc.log2M, N, seed=3, layout="aos")
     flags = flags_buf(N)
@@ -253,7 +255,7 @@ def test_scale2pow(case, layout, path):
     same = (out == ref_dev).all(axis=1)
     wrong_ref = [orc.exact.from_rns(ref_dev[i:i + 1])[0] != X[i] >> int(g["shift"][i]) for i in range(len(X))]
     assert all(s or w for s, w in zip(same, wrong_ref))
-    N = 1500 if orc.n <= 16 else 400
+    N = sized(orc.n, 1500, 400)
     x = W.uniform_residues(orc.moduli, N, seed=9, stream=W.S_X, layout="aos")
     Dh = W.shifts(N, min(900, orc.log2M + 40), seed=9)
     out = from_dev(ctx.rns_scale2pow(to_dev(x, layout), torch.from_numpy(Dh.astype(np.int32)).cuda(), layout=layout),
@@ -340,10 +342,12 @@ def test_mpint_div(case, path):
     xs = orc.log2_inputs(got["digits"])
     if len(xs) == 0 or np.array_equal(ctx.device_ceil_log2(xs), np.ceil(np.log2(xs)).astype(np.int32)):
         assert got.tobytes() == want.tobytes()
+    if orc.n >= 128 and path == "reference":
+        return  # the reference's one-bit division at 2048 to 6400 bits: the golden pairs only
     # fresh operands: signed dividends over the whole range, nonzero divisors of
     # random bit lengths, quotients from 0 to M - 1
     rng = random.Random(31)
-    N = 1500 if orc.n <= 16 else 400
+    N = sized(orc.n, 1500, 400)
     va = [rng.choice((-1, 1)) * rng.randrange(orc.M) for _ in range(N)]
     vb = []
     for _ in range(N):
@@ -377,7 +381,7 @@ def test_mrc(case, layout):
     tag, ctx, orc, g = case
     got = from_dev(ctx.mrc(to_dev(g["x"], layout), layout=layout), layout)
     assert np.array_equal(got, g["mrc_dev"])
-    N = 5000 if orc.n <= 16 else 1500
+    N = sized(orc.n, 5000, 1500)
     x = W.uniform_residues(orc.moduli, N, seed=41, stream=W.S_X, layout="aos")
     x[:3] = orc.exact.to_rns([0, 1, orc.M - 1])
     x[3, 1] = orc.moduli[1]  # invalid residue
@@ -412,7 +416,7 @@ def test_mpint_overflow_flag(case):
 @pytest.mark.parametrize("layout", ["soa", "aos"])
 def test_max(case, layout, path):
     tag, ctx, orc, g = case
-    N = 20000 if orc.n <= 16 else 5000
+    N = sized(orc.n, 20000, 5000)
     x = W.uniform_residues(orc.moduli, N, seed=21, stream=W.S_MAX, layout="aos")
     X = orc.exact.from_rns(x)
     top = max(X)
