@@ -273,8 +273,8 @@ def run_only(args):
     from grns_gb300 import native
     from grns_gb300.workload import S_X, S_Y
     L = native.lib(build_if_missing=True)
-    n = {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32, "mpint64": 64,
-         "mpdiv32": 32, "tobin32": 32, "frombin32": 32, "tobin64": 64, "mrc32": 32}[args.only]
+    n = args.n or {"div": 32, "scale": 32, "cmp32": 32, "cmp8": 8, "max64": 64, "eval32": 32, "evtight32": 32,
+                   "mpint64": 64, "mpdiv32": 32, "tobin32": 32, "frombin32": 32, "tobin64": 64, "mrc32": 32}[args.only]
     ctx = G.RNSContext(greedy(n))
     if args.eval_split is not None:
         native.check(L.grns_ctx_set_eval_split(ctx.handle, args.eval_split))
@@ -348,7 +348,8 @@ def run_only(args):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     ms = statistics.median(times) if times else 0.0
-    print(json.dumps({"only": args.only, "count": cnt, "flush": bool(args.flush), "calls": args.warmup + args.steps,
+    print(json.dumps({"only": args.only, "n": n, "count": cnt, "flush": bool(args.flush),
+                      "calls": args.warmup + args.steps,
                       "eval_split": L.grns_ctx_get_eval_split(ctx.handle),
                       "ms_median": ms,
                       "Mnum_s": cnt / (ms * 1e-3) / 1e6 if ms else None}))
@@ -771,6 +772,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline workload only")
     ap.add_argument("--pairs", type=int, default=PAIRS, help="numbers per op (profiling cases use fewer)")
     ap.add_argument("--flush", action="store_true", help="profiling mode: flush L2 (256 MiB write) before each call")
+    ap.add_argument("--n", type=int, default=None,
+                    help="profiling: moduli count of the --only case (greedy 30-bit moduli), e.g. 128 or 256")
     ap.add_argument("--mp-op", default="mul", choices=["add", "sub", "mul"], help="profiling: the mpint64 operation")
     ap.add_argument("--eval-split", type=int, default=None,
                     help="profiling: eighths of the evaluation's warps on the FP64 pipe (grns_ctx_set_eval_split)")
