@@ -18,6 +18,7 @@
 #include "internal.h"
 #include "rns_device.cuh"
 #include "rns_fast.cuh"
+#include "div_coop.cuh"
 
 namespace grns {
 
@@ -51,6 +52,48 @@ GRNS_UNROLL_N
 }
 
 constexpr int kDivBlock = 128;
+
+/* one division per warp (div_coop.cuh), for the 128- and 256-moduli sets:
+ * lane l holds residues l + 32 j; scratch for the rare exact comparisons */
+constexpr int kDivCoopBlock = 128;
+template <int N>
+__global__ void __launch_bounds__(kDivCoopBlock)
+    k_div_coop(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> d, int64_t count, Output<N> q,
+               Output<N> r, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
+    constexpr int J = N / 32;
+    __shared__ DivK K[N];
+    __shared__ uint32_t scratch[kDivCoopBlock / 32][2 * N];
+    divk_fill<N>(C, K);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    uint32_t *sc = scratch[threadIdx.x >> 5];
+    const int64_t warps = ((int64_t)gridDim.x * kDivCoopBlock) >> 5;
+    for (int64_t k = ((int64_t)blockIdx.x * kDivCoopBlock + threadIdx.x) >> 5; k < count; k += warps) {
+        uint32_t xa[J], da[J], qa[J], ra[J];
+        bool bad = false;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int i = lane + 32 * j;
+            xa[j] = x.load(k, i);
+            da[j] = d.load(k, i);
+            bad |= xa[j] >= C.m[i] || da[j] >= C.m[i];
+        }
+        uint32_t f = __any_sync(kWarpFull, bad) ? kFlagInvalidInput : 0u;
+        if (f) {
+#pragma unroll
+            for (int j = 0; j < J; j++) qa[j] = ra[j] = 0;
+        } else {
+            div_warp_coop<N>(K, C, qa, ra, xa, da, f, lane, sc);
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            q.store(k, lane + 32 * j, qa[j]);
+            r.store(k, lane + 32 * j, ra[j]);
+        }
+        if (flags && lane == 0) flags[k] = (uint8_t)f;
+    }
+}
 
 /* resident 128-thread blocks per SM the register budget must allow: shared
  * memory (3N words per thread) allows 4 at n <= 32 and 2 at n = 64 */
@@ -371,10 +414,11 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
         return cuda_status(cudaGetLastError());
     }
     if constexpr (N > 64) {
-        /* the digit recurrence one number per thread (its row in local memory):
-         * the warp passes' shared-memory columns (2n words a thread) do not fit */
-        k_div<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
-                                                              count, Output<N>{q, ldo}, Output<N>{r, ldo}, flags);
+        /* one division per warp: the warp passes' shared-memory columns (2n
+         * words a thread) do not fit, and one number per thread keeps its
+         * residue arrays in local memory */
+        k_div_coop<N><<<grid_for(c, count * 32, kDivCoopBlock, 16), kDivCoopBlock, 0, s>>>(
+            consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld}, count, Output<N>{q, ldo}, Output<N>{r, ldo}, flags);
         (void)min_per_warp;
         return cuda_status(cudaGetLastError());
     } else {

@@ -3,9 +3,8 @@
  *
  *   * per-moduli-set constant block passed to every kernel by value (so the
  *     per-modulus constants sit in the kernel-parameter constant bank and are
- *     read with compile-time offsets from fully unrolled loops); the
- *     256-moduli block exceeds the parameter space and is passed by the
- *     address of its device copy (CArg);
+ *     read with compile-time offsets from fully unrolled loops); above 64
+ *     moduli the block is passed by the address of its device copy (CArg);
  *   * modular arithmetic on the integer pipe: Shoup multiplication by a
  *     constant, Barrett multiplication of two residues, branch-free add/sub;
  *   * extended-range float (er_float_t) helpers with the reference's exact
@@ -135,10 +134,12 @@ struct Consts {
     GRNS_HD const Consts &get() const { return *this; }
 };
 
-/* A kernel's constant-block parameter: the block itself while it fits the
- * 32 KB kernel parameter space (with room for the other arguments), else the
- * address of its device copy.  In the kernel: const Consts<N> &C = CA.get(). */
-constexpr size_t kParamConstsMax = 30 * 1024;
+/* A kernel's constant-block parameter: the block itself up to 64 moduli, else
+ * the address of its device copy -- the 256-moduli block (about 37 KB)
+ * exceeds the 32 KB kernel parameter space, and kernels that spread a
+ * number's residues over a warp's lanes read 32 different entries at once,
+ * which the constant bank serves one address at a time and L1 in one
+ * request.  In the kernel: const Consts<N> &C = CA.get(). */
 template <int N>
 struct ConstsRef {
     const Consts<N> *p;
@@ -146,9 +147,9 @@ struct ConstsRef {
     GRNS_HD const Consts<N> &get() const { return *p; }
 };
 template <int N>
-using CArg = typename std::conditional<(sizeof(Consts<N>) > kParamConstsMax), ConstsRef<N>, Consts<N>>::type;
+using CArg = typename std::conditional<(N > 64), ConstsRef<N>, Consts<N>>::type;
 template <int N>
-constexpr bool consts_by_address() { return sizeof(Consts<N>) > kParamConstsMax; }
+constexpr bool consts_by_address() { return N > 64; }
 
 /* ---------------- modular arithmetic ---------------- */
 
