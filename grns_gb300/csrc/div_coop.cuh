@@ -1,5 +1,6 @@
 /*
- * grns_gb300 -- one division per warp, for the 128- and 256-moduli sets.
+ * grns_gb300 -- one division (and one power-of-two scaling) per warp, for the
+ * 128- and 256-moduli sets.
  *
  * The n-threaded schedule of the reference's division (src/rnsdiv.cuh:244
  * and :301 run one number per block of n threads): here a warp holds one
@@ -18,6 +19,10 @@
  * residues of each array in registers, and the per-modulus constants come
  * from the block's DivK table in shared memory (a lane reads the same n / 32
  * records for every number).
+ *
+ * The scaling (scale_warp_coop) runs scale_fast's 52-bit steps the same way:
+ * per step the rank's fixed-point sum (exact in 128 bits) and the low bits
+ * of X (a sum mod 2^64) are warp sums, the rest is per residue.
  */
 #pragma once
 
@@ -38,6 +43,13 @@ __device__ __forceinline__ u128 warp_sum_u128(u128 v) {
         lo = s;
     }
     return ((u128)hi << 64) | lo;
+}
+
+/* the sum over the warp of v mod 2^64, in every lane */
+__device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kWarpFull, v, o);
+    return v;
 }
 
 /* fx96w over a number spread over the warp (v[j]: residue lane + 32 j) */
@@ -224,6 +236,89 @@ __device__ __forceinline__ void div_warp_coop(const DivK *K, const Consts<N> &C,
         r[j] = submod(x[j], kmulmod(q[j], d[j], k), m);
     }
     flags |= st.f;
+}
+
+/* the top mixed-radix digit of the number in v[0, N) (the rank's tie-break) */
+template <int N>
+__device__ __noinline__ uint32_t mrc_top_digit(const Consts<N> &C, const uint32_t *v) {
+    uint32_t a[N];
+    mrc_hd<N>(C, [&](int i) { return v[i]; }, a);
+    return a[N - 1];
+}
+
+/* rank_fast for a number spread over the warp (c[j] = x w mod m of residue
+ * lane + 32 j); scratch: N words of shared memory for this warp */
+template <int N>
+__device__ __forceinline__ uint32_t rank_warp(const Consts<N> &C, const uint32_t (&x)[N / 32],
+                                              const uint32_t (&c)[N / 32], bool small, int lane, uint32_t *scratch) {
+    uint64_t S0 = 0, S1 = 0, S2 = 0;
+#pragma unroll
+    for (int j = 0; j < N / 32; j++) {
+        const int i = lane + 32 * j;
+        const uint32_t sv = c[j];
+        const uint64_t p0 = (uint64_t)sv * C.c96_0[i];
+        const uint64_t p1 = (uint64_t)sv * C.c96_1[i];
+        const uint64_t p2 = (uint64_t)sv * C.c96_2[i];
+        S0 += (uint32_t)p0;
+        S1 += (p0 >> 32) + (uint32_t)p1;
+        S2 += (p1 >> 32) + p2;
+    }
+    const u128 t = warp_sum_u128((u128)S0 + ((u128)S1 << 32) + ((u128)S2 << 64));
+    const uint32_t kk = (uint32_t)(t >> 96);
+    if ((t & kMask96) >= (u128)C.E || small) return kk;
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < N / 32; j++) scratch[lane + 32 * j] = x[j];
+    __syncwarp();
+    uint32_t top = 0;
+    if (lane == 0) top = mrc_top_digit<N>(C, scratch);
+    top = __shfl_sync(kWarpFull, top, 0);
+    return top == 0 ? kk : kk - 1;
+}
+
+/* scale_fast for a number spread over the warp (x canonical; res this lane's
+ * residues of floor(X / 2^D)); scratch: N words of shared memory for this warp */
+template <int N>
+__device__ __forceinline__ void scale_warp_coop(const Consts<N> &C, uint32_t (&res)[N / 32],
+                                                const uint32_t (&x)[N / 32], unsigned D, int lane,
+                                                uint32_t *scratch) {
+    constexpr int J = N / 32;
+    uint32_t cur[J], c[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) cur[j] = x[j];
+    if (D > (unsigned)C.log2M) {  // X < M < 2^(log2M + 1): the result is 0
+#pragma unroll
+        for (int j = 0; j < J; j++) res[j] = 0;
+        return;
+    }
+    bool small = false;
+#pragma unroll 1
+    for (unsigned left = D; left > 0;) {
+        const int step = left < (unsigned)kScaleB ? (int)left : kScaleB;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int i = lane + 32 * j;
+            c[j] = mulmod_shoup(cur[j], C.w[i], C.w_sh[i], C.m[i]);
+        }
+        const uint32_t k = rank_warp<N>(C, cur, c, small, lane, scratch);
+        /* scaling_step_big: X mod 2^step from the CRT sum in 64-bit wrap-around arithmetic */
+        uint64_t acc = 0;
+#pragma unroll
+        for (int j = 0; j < J; j++) acc += (uint64_t)c[j] * C.mi64[lane + 32 * j];
+        acc = warp_sum_u64(acc);
+        const uint64_t low = (acc - (uint64_t)k * C.m64) & ((((uint64_t)1) << step) - 1);
+        const uint32_t *inv = C.pow2neg + (int64_t)step * N, *inv_sh = C.pow2neg_sh + (int64_t)step * N;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            const int i = lane + 32 * j;
+            const uint32_t m = C.m[i];
+            cur[j] = mulmod_shoup(submod(cur[j], reduce53<N>(C, i, low), m), ldg_u32(inv + i), ldg_u32(inv_sh + i), m);
+        }
+        left -= (unsigned)step;
+        small = true;
+    }
+#pragma unroll
+    for (int j = 0; j < J; j++) res[j] = cur[j];
 }
 
 }  // namespace grns

@@ -377,6 +377,40 @@ GRNS_UNROLL_N
     }
 }
 
+/* one power-of-two scaling per warp (div_coop.cuh), for the 128- and
+ * 256-moduli sets */
+template <int N>
+__global__ void __launch_bounds__(kDivCoopBlock)
+    k_scale_coop(const __grid_constant__ CArg<N> CA, Operand<N> x, const uint32_t *__restrict__ D,
+                 uint32_t D_uniform, int64_t count, Output<N> out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
+    constexpr int J = N / 32;
+    __shared__ uint32_t scratch[kDivCoopBlock / 32][N];
+    const int lane = threadIdx.x & 31;
+    uint32_t *sc = scratch[threadIdx.x >> 5];
+    const int64_t warps = ((int64_t)gridDim.x * kDivCoopBlock) >> 5;
+    for (int64_t k = ((int64_t)blockIdx.x * kDivCoopBlock + threadIdx.x) >> 5; k < count; k += warps) {
+        uint32_t xa[J], ya[J];
+        bool bad = false;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+            xa[j] = x.load(k, lane + 32 * j);
+            bad |= xa[j] >= C.m[lane + 32 * j];
+        }
+        const uint32_t f = __any_sync(kWarpFull, bad) ? kFlagInvalidInput : 0u;
+        const unsigned dk = D ? __ldg(D + k) : D_uniform;
+        if (f) {
+#pragma unroll
+            for (int j = 0; j < J; j++) ya[j] = 0;
+        } else {
+            scale_warp_coop<N>(C, ya, xa, dk, lane, sc);
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) out.store(k, lane + 32 * j, ya[j]);
+        if (flags && lane == 0) flags[k] = (uint8_t)f;
+    }
+}
+
 template <int N, bool FAST>
 __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                const uint32_t *__restrict__ D, uint32_t D_uniform, int64_t count,
@@ -530,9 +564,9 @@ grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, u
         return cuda_status(e);
     } else if constexpr (N <= 64) {
         return run_scale_steps<N>(c, x, D, Du, ld, count, out, flags, s, min_per_warp, ldo);
-    } else {  // exact 52-bit steps one number per thread (no per-n shared memory)
-        k_scale<N, true><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
-                                                                Output<N>{out, ldo}, flags);
+    } else {  // exact 52-bit steps, one number per warp
+        k_scale_coop<N><<<grid_for(c, count * 32, kDivCoopBlock, 16), kDivCoopBlock, 0, s>>>(
+            consts_of<N>(c), Operand<N>{x, ld}, D, Du, count, Output<N>{out, ldo}, flags);
         return cuda_status(cudaGetLastError());
     }
 }
