@@ -61,9 +61,88 @@ __global__ void __launch_bounds__(kMrcBlock) k_mrc(const __grid_constant__ CArg<
     }
 }
 
+/* the 128- and 256-moduli sets, P = 512 / n numbers per warp (lane l holds
+ * residues l + 32 j of each): column by column, digit j (residue j once
+ * every earlier digit is applied) is broadcast from its lane and every later
+ * residue i becomes (x_i - a_j) m_j^-1 mod m_i -- per residue the same
+ * operations in the same order as k_mrc, so the same digits.  Each inverse
+ * read from the n^2 table (512 KB at n = 256, through L2) serves the P
+ * numbers. */
+template <int N>
+constexpr int mrc_warp_numbers() {
+    return 512 / N;
+}
+template <int N>
+__global__ void __launch_bounds__(kMrcBlock) k_mrc_warp(const __grid_constant__ CArg<N> CA, Operand<N> x,
+                                                        int64_t count, Output<N> out, uint8_t *__restrict__ flags) {
+    const Consts<N> &C = CA.get();
+    constexpr int J = N / 32, P = mrc_warp_numbers<N>();
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint32_t m[J], b[J], mu[J];
+#pragma unroll
+    for (int j = 0; j < J; j++) {
+        m[j] = C.m[lane + 32 * j];
+        b[j] = C.b[lane + 32 * j];
+        mu[j] = C.mu[lane + 32 * j];
+    }
+    const int64_t warps = ((int64_t)gridDim.x * kMrcBlock) >> 5;
+    for (int64_t k0 = (((int64_t)blockIdx.x * kMrcBlock + threadIdx.x) >> 5) * P; k0 < count; k0 += warps * P) {
+        uint32_t y[P][J];
+        bool bad[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+            bool bp = false;
+#pragma unroll
+            for (int j = 0; j < J; j++) {
+                y[p][j] = k0 + p < count ? x.load(k0 + p, lane + 32 * j) : 0u;
+                bp |= y[p][j] >= m[j];
+            }
+            bad[p] = __any_sync(FULL, bp);
+        }
+#pragma unroll
+        for (int jj = 0; jj < J; jj++) {
+#pragma unroll 1
+            for (int l = 0; l < 32; l++) {
+                const int j = 32 * jj + l;
+                uint32_t a[P];
+#pragma unroll
+                for (int p = 0; p < P; p++) a[p] = __shfl_sync(FULL, y[p][jj], l);  // digit j of each number
+                const uint32_t mj = C.m[j];
+#pragma unroll
+                for (int j2 = jj; j2 < J; j2++) {
+                    const int i = lane + 32 * j2;
+                    if (j2 > jj || lane > l) {
+                        const uint32_t c = __ldg(C.mrc_inv + j * N + i), cs = __ldg(C.mrc_inv_sh + j * N + i);
+#pragma unroll
+                        for (int p = 0; p < P; p++) {
+                            uint32_t t = a[p];
+                            if (mj > m[j2]) t = b[j2] >= 16 ? mulmod_barrett(t, 1u, m[j2], mu[j2], b[j2]) : t % m[j2];
+                            y[p][j2] = mulmod_shoup(submod(y[p][j2], t, m[j2]), c, cs, m[j2]);
+                        }
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+            if (k0 + p >= count) break;
+#pragma unroll
+            for (int j = 0; j < J; j++) out.store(k0 + p, lane + 32 * j, bad[p] ? 0u : y[p][j]);
+            if (flags && lane == 0) flags[k0 + p] = bad[p] ? (uint8_t)kFlagInvalidInput : (uint8_t)0;
+        }
+    }
+}
+
 template <int N>
 static grns_status run_mrc(const grns_ctx *c, const uint32_t *x, int64_t ld, int64_t count, uint32_t *out,
                            uint8_t *flags, cudaStream_t s) {
+    if constexpr (N > 64) {
+        constexpr int P = mrc_warp_numbers<N>();
+        k_mrc_warp<N><<<grid_for(c, (count + P - 1) / P * 32, kMrcBlock, 16), kMrcBlock, 0, s>>>(
+            consts_of<N>(c), Operand<N>{x, ld}, count, Output<N>{out, ld}, flags);
+        return cuda_status(cudaGetLastError());
+    }
     const size_t smem = (mrc_inv_shared<N>() ? (size_t)N * N * sizeof(uint2) : 0) + (size_t)N * kMrcBlock * 4;
     static std::atomic<int> per_sm[kOccDevices];  // resident blocks per SM, per device
     const int occ = resident_blocks(per_sm, c, k_mrc<N>, kMrcBlock, smem);
