@@ -22,7 +22,8 @@
 
 namespace grns {
 
-template <int N, bool FAST>
+/* the reference's division (div_ref, one quotient bit a step), one number per thread */
+template <int N>
 __global__ void __launch_bounds__(128) k_div(const __grid_constant__ CArg<N> CA, Operand<N> x, Operand<N> d,
                                              int64_t count, Output<N> q, Output<N> r, uint8_t *__restrict__ flags) {
     const Consts<N> &C = CA.get();
@@ -37,8 +38,6 @@ GRNS_UNROLL_N
         if (f) {
 GRNS_UNROLL_N
             for (int i = 0; i < N; i++) { qa[i] = 0; ra[i] = 0; }
-        } else if (FAST) {
-            div_fast<N>(C, qa, ra, xa, da, f);
         } else {
             div_ref<N>(C, qa, ra, xa, da, f);
         }
@@ -411,7 +410,8 @@ __global__ void __launch_bounds__(kDivCoopBlock)
     }
 }
 
-template <int N, bool FAST>
+/* the reference's power-of-two scaling (scale2pow_ref), one number per thread */
+template <int N>
 __global__ void __launch_bounds__(128) k_scale(const __grid_constant__ CArg<N> CA, Operand<N> x,
                                                const uint32_t *__restrict__ D, uint32_t D_uniform, int64_t count,
                                                Output<N> out, uint8_t *__restrict__ flags) {
@@ -427,8 +427,6 @@ GRNS_UNROLL_N
         if (f) {
 GRNS_UNROLL_N
             for (int i = 0; i < N; i++) ya[i] = 0;
-        } else if (FAST) {
-            scale_fast<N>(C, ya, xa, dk);
         } else {
             scale2pow_ref<N>(C, ya, xa, dk);
         }
@@ -443,7 +441,7 @@ grns_status run_div(const grns_ctx *c, const uint32_t *x, const uint32_t *d, int
                     uint32_t *r, uint8_t *flags, cudaStream_t s, int min_per_warp, int64_t ldo) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
-        k_div<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
+        k_div<N><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, Operand<N>{d, ld},
                                                                count, Output<N>{q, ldo}, Output<N>{r, ldo}, flags);
         return cuda_status(cudaGetLastError());
     }
@@ -537,7 +535,7 @@ grns_status run_scale(const grns_ctx *c, const uint32_t *x, const uint32_t *D, u
                       uint32_t *out, uint8_t *flags, cudaStream_t s, int min_per_warp, int64_t ldo) {
     const int B = 128;
     if (c->path == GRNS_PATH_REFERENCE) {
-        k_scale<N, false><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
+        k_scale<N><<<grid_for(c, count, B, 16), B, 0, s>>>(consts_of<N>(c), Operand<N>{x, ld}, D, Du, count,
                                                                  Output<N>{out, ldo}, flags);
         return cuda_status(cudaGetLastError());
     }
