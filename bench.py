@@ -50,6 +50,7 @@ SERVE_LEN = (1e3, 1e7)      # log-uniform request lengths
 SERVE_POOL = 10 ** 7        # device-resident operand pools
 SERVE_BUDGET = 48 << 30     # server HBM budget for outputs
 SERVE_LOADS = (0.5, 0.9)    # offered load as a fraction of the all-at-once throughput
+SERVE_GATHER_US = 500       # gathering window of the second all-at-once run (the server's gather_us)
 DMAX = 900
 SEED = 20260101
 WARMUP_SECONDS = 0.25       # minimum warm-up time before the timed steps
@@ -711,6 +712,10 @@ def bench_served(ctx_for, L, dev, stream, sp, P, seed):
 
     run(0)  # warm-up
     wall_all, st_all = run(0)
+    # the same burst with a gathering window: free slots wait while requests keep arriving
+    sv.set_gather_us(SERVE_GATHER_US)
+    wall_g, st_g = run(0)
+    sv.set_gather_us(0)
     total = sum(lens)
     cap_rps = len(lens) / wall_all
     sweeps = []
@@ -752,6 +757,9 @@ def bench_served(ctx_for, L, dev, stream, sp, P, seed):
         "ops": "uniform over eval+cmp, div, scale2pow (n=32), mp_int mul, max (n=64)",
         "all_at_once": {"Mnum_s": total / wall_all / 1e6, "p50_ms": st_all["p50_us"] / 1e3,
                         "p99_ms": st_all["p99_us"] / 1e3, "mean_jobs_per_launch": st_all["mean_jobs_per_launch"]},
+        "all_at_once_gathered": {"gather_us": SERVE_GATHER_US, "Mnum_s": total / wall_g / 1e6,
+                                 "p50_ms": st_g["p50_us"] / 1e3, "p99_ms": st_g["p99_us"] / 1e3,
+                                 "mean_jobs_per_launch": st_g["mean_jobs_per_launch"]},
         "poisson": sweeps,
         "per_request_plain": {"Mnum_s": total / (t_plain * 1e-3) / 1e6,
                               "p50_ms": svc_sorted[len(svc) // 2],

@@ -131,6 +131,7 @@ struct grns_server {
     std::vector<double> lat;
     uint64_t completed = 0, rejected = 0, cancelled = 0, launches = 0, jobs_launched = 0;
     double numbers = 0, t_first = 0, t_last = 0;
+    double t_last_submit = 0;  // submission time of the newest request (the gathering window)
 };
 
 namespace {
@@ -294,6 +295,12 @@ void schedule_locked(grns_server *sv) {
         finish(sv, *it, q, GRNS_ERR_REJECTED, now);
         sv->rejected++;
         it = sv->pending.erase(it);
+    }
+    /* gathering: while requests keep arriving, free slots wait for more */
+    if (sv->opt.gather_us > 0 && !sv->pending.empty() &&
+        (int)sv->pending.size() < sv->opt.max_jobs_per_launch) {
+        const double oldest = sv->reqs.at(sv->pending.front()).t_submit;
+        if (now - sv->t_last_submit < sv->opt.gather_us && now - oldest < 4.0 * sv->opt.gather_us) return;
     }
     for (Slot *sl : sv->slots) {
         if (sl->busy || sv->pending.empty()) continue;
@@ -647,6 +654,7 @@ grns_status grns_server_submit(grns_server *sv, const grns_request *r, uint64_t 
         return GRNS_OK;
     }
     sv->pending.push_back(id);
+    sv->t_last_submit = q.t_submit;
     sv->cv.notify_all();
     return GRNS_OK;
 }
@@ -716,6 +724,14 @@ grns_status grns_server_stats_get(grns_server *sv, grns_server_stats *st) {
         st->mean_us = s / (double)v.size();
     }
     if (sv->t_last > sv->t_first) st->numbers_per_s = sv->numbers / ((sv->t_last - sv->t_first) * 1e-6);
+    return GRNS_OK;
+}
+
+grns_status grns_server_set_gather_us(grns_server *sv, int32_t gather_us) {
+    if (!sv) return GRNS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->opt.gather_us = gather_us;
+    sv->cv.notify_all();
     return GRNS_OK;
 }
 

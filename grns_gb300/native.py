@@ -77,6 +77,7 @@ SIGNATURES = {
     "grns_server_stats_get": (c_int, [c_void_p, c_void_p]),
     "grns_server_cancel": (c_int, [c_void_p, ctypes.c_uint64]),
     "grns_server_reset_stats": (c_int, [c_void_p]),
+    "grns_server_set_gather_us": (c_int, [c_void_p, ctypes.c_int32]),
     "grns_gen_uniform": (c_int, [c_void_p, ctypes.c_uint64, c_uint32, c_int64, c_int, c_void_p, c_void_p]),
     "grns_gen_divisors": (c_int, [c_void_p, ctypes.c_uint64, c_int64, c_int, c_void_p, c_void_p]),
     "grns_gen_shifts": (c_int, [ctypes.c_uint64, c_int64, c_uint32, c_void_p, c_void_p]),
@@ -99,7 +100,8 @@ class Schedule(ctypes.Structure):
 class ServerOptions(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", c_size_t), ("launch_slots", ctypes.c_int32),
                 ("max_jobs_per_launch", ctypes.c_int32), ("admission_timeout_ms", ctypes.c_int32),
-                ("direct_min_count", ctypes.c_int32), ("alloc_cap_bytes", c_size_t)]
+                ("direct_min_count", ctypes.c_int32), ("alloc_cap_bytes", c_size_t),
+                ("gather_us", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):

@@ -13,10 +13,10 @@ OPS = {"eval": 0, "cmp": 1, "div": 2, "scale2pow": 3, "max": 4, "mpint_add": 5, 
 
 class Server:
     def __init__(self, budget_bytes=0, slots=4, max_jobs=256, admission_timeout_ms=0, alloc_cap_bytes=0,
-                 direct_min_count=0):
+                 direct_min_count=0, gather_us=0):
         self.L = native.lib()
         opt = native.ServerOptions(budget_bytes, slots, max_jobs, admission_timeout_ms, direct_min_count,
-                                   alloc_cap_bytes)
+                                   alloc_cap_bytes, gather_us, 0)
         h = ctypes.c_void_p()
         check(self.L.grns_server_create(ctypes.byref(opt), ctypes.byref(h)), "grns_server_create")
         self.h = h
@@ -105,3 +105,7 @@ class Server:
 
     def reset_stats(self):
         check(self.L.grns_server_reset_stats(self.h), "grns_server_reset_stats")
+
+    def set_gather_us(self, us):
+        """the gathering window (grns_server_options.gather_us) on the live server"""
+        check(self.L.grns_server_set_gather_us(self.h, int(us)), "grns_server_set_gather_us")

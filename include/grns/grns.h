@@ -385,6 +385,12 @@ typedef struct {
     size_t alloc_cap_bytes;      /* hard cap on the device memory the server holds (0: none): a put
                                     beyond it returns, and an admitted request beyond it completes
                                     with, GRNS_ERR_OUT_OF_MEMORY; the server goes on */
+    int32_t gather_us;           /* gathering window (0 or negative: off): while the newest pending
+                                    request is younger than this, free launch slots wait for more
+                                    requests, until the oldest pending one has waited 4 windows or
+                                    the pending requests fill a launch.  More requests per launch
+                                    for bursts, up to 4 windows more latency */
+    int32_t reserved;            /* 0 */
 } grns_server_options;
 
 typedef struct {
@@ -431,6 +437,8 @@ grns_status grns_server_wait(grns_server *srv, uint64_t request_id, int64_t time
 grns_status grns_server_cancel(grns_server *srv, uint64_t request_id);
 grns_status grns_server_stats_get(grns_server *srv, grns_server_stats *stats);
 grns_status grns_server_reset_stats(grns_server *srv);
+/* the gathering window of grns_server_options.gather_us, changed on a live server */
+grns_status grns_server_set_gather_us(grns_server *srv, int32_t gather_us);
 
 /* ---- seeded synthetic inputs in device memory ----
  * No counterpart in the reference (its tests draw from GMP's Mersenne

@@ -173,6 +173,32 @@ def test_results_alone_and_in_the_mix(env, direct):
         srv.close()
 
 
+def test_gathering_window_packs_a_burst(env):
+    """with gather_us set, a burst submitted back to back shares few launches
+    (free slots wait while requests keep arriving) and every result is the
+    per-call API's"""
+    G, native, ctxs = env
+    from grns_gb300.serve import Server
+    ctx = ctxs[32]
+    srv = Server(slots=4, max_jobs=256, gather_us=2000)
+    try:
+        ci = srv.add_context(ctx)
+        cnt = 5000
+        x = gen(native, ctx, cnt, 1, 501)
+        y = gen(native, ctx, cnt, 2, 502)
+        torch.cuda.synchronize()
+        hx, hy = srv.put(ci, x), srv.put(ci, y)
+        counts = [1 + 97 * t for t in range(40)]
+        ids = [srv.submit("cmp", ci, hx, hy, c) for c in counts]
+        got = [server_bytes(srv, rid, "cmp", 32) for rid in ids]
+        st = srv.stats()
+        assert st["completed"] == len(ids) and st["mean_jobs_per_launch"] >= 8
+        for c, g in zip(counts, got):
+            assert as_bytes(per_call(native, ctx, "cmp", x, y, c)) == g, c
+    finally:
+        srv.close()
+
+
 def test_cached_evaluations_and_admission(env):
     G, native, ctxs = env
     from grns_gb300.serve import Server
