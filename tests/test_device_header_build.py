@@ -13,7 +13,7 @@ from tests.helpers import moduli_for
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g32"])
+@pytest.mark.parametrize("tag", ["ref8", "g32", "cat6400_n256"])
 def test_drop_in_compiles(tmp_path, tag):
     from grns_gb300.build import nvcc
     exe = nvcc()
