@@ -146,7 +146,7 @@ def test_fixed_point_enclosure(fc):
                 assert U - E <= Fraction(v, f.M) * 2 ** 96 <= U
 
 
-@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("tag", TAGS + ["g128", "g256"])
 def test_random_and_special(fc, tag):
     f = FC(fc, moduli_for(tag))
     M = f.M
@@ -172,7 +172,7 @@ def test_random_and_special(fc, tag):
     assert f.scale(X, S) == [a >> s for a, s in zip(X, S)]
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64", "p16", "p32", "p64"])
+@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64", "p16", "p32", "p64", "g256"])
 def test_division_quotient_boundaries(fc, tag):
     """dividends just below, at and above multiples of the divisor, divisors
     near M and near powers of two: the certified quotient estimate must never
@@ -216,7 +216,7 @@ def test_division_remainder_evaluation_wraps(fc, tag):
     assert not fl.any()
 
 
-@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("tag", TAGS + ["g256"])
 def test_scaling_every_shift(fc, tag):
     """floor(X / 2^D) for every D from 0 to log2M + 2 (the one-pass form's
     last chunk is partial unless 26 divides D) on values at the edges: M - 1,
@@ -346,7 +346,7 @@ def test_one_ulp_evaluation(fc, tag):
         assert up - lo <= rup - rlo
 
 
-@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64", "p16", "p32", "p64"])
+@pytest.mark.parametrize("tag", ["ref8", "g12", "g32", "g64", "p16", "p32", "p64", "g256"])
 def test_scaling_step_boundaries(fc, tag):
     """exponents at and around multiples of the 52-bit step, the full range,
     and dividends next to 0 and M (the first step's checked rank)"""
