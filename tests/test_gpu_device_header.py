@@ -22,7 +22,7 @@ torch = pytest.importorskip("torch")
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-@pytest.fixture(scope="module", params=["ref8", "g32", "g64"])
+@pytest.fixture(scope="module", params=["ref8", "g32", "g64", "cat6400_n256"])
 def user_lib(request, tmp_path_factory):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
