@@ -180,7 +180,7 @@ def test_gathering_window_packs_a_burst(env):
     G, native, ctxs = env
     from grns_gb300.serve import Server
     ctx = ctxs[32]
-    srv = Server(slots=4, max_jobs=256, gather_us=2000)
+    srv = Server(slots=4, max_jobs=256, gather_us=5000)  # a window well above the gaps between submissions
     try:
         ci = srv.add_context(ctx)
         cnt = 5000
