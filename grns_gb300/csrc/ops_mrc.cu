@@ -19,25 +19,14 @@ namespace grns {
 constexpr int kMrcBlock = 128;
 
 template <int N>
-constexpr bool mrc_inv_shared() {
-    return N <= 64;
-}
-
-template <int N>
 __global__ void __launch_bounds__(kMrcBlock) k_mrc(const __grid_constant__ CArg<N> CA, Operand<N> x, int64_t count,
                                                    Output<N> out, uint8_t *__restrict__ flags) {
     const Consts<N> &C = CA.get();
     extern __shared__ uint2 mrc_smem[];
-    /* [j * N + i] = (m_j^-1 mod m_i, Shoup companion), j < i: staged in shared
-     * memory up to 64 moduli, read through L1 / L2 above (n^2 8-byte entries,
-     * 512 KB at n = 256) */
-    constexpr bool kInvShared = mrc_inv_shared<N>();
-    uint2 *inv = mrc_smem;
-    uint32_t *col = reinterpret_cast<uint32_t *>(inv + (kInvShared ? N * N : 0)) + threadIdx.x;
-    if (kInvShared) {
-        for (int w = threadIdx.x; w < N * N; w += blockDim.x) inv[w] = make_uint2(C.mrc_inv[w], C.mrc_inv_sh[w]);
-        __syncthreads();
-    }
+    uint2 *inv = mrc_smem;  // [j * N + i] = (m_j^-1 mod m_i, Shoup companion), j < i
+    uint32_t *col = reinterpret_cast<uint32_t *>(inv + N * N) + threadIdx.x;
+    for (int w = threadIdx.x; w < N * N; w += blockDim.x) inv[w] = make_uint2(C.mrc_inv[w], C.mrc_inv_sh[w]);
+    __syncthreads();
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         uint32_t bad = 0;
 #pragma unroll 1
@@ -49,8 +38,7 @@ __global__ void __launch_bounds__(kMrcBlock) k_mrc(const __grid_constant__ CArg<
             for (int j = 0; j < i; j++) {
                 uint32_t t = col[j * kMrcBlock];
                 if (C.m[j] > m) t = b >= 16 ? mulmod_barrett(t, 1u, m, mu, b) : t % m;  // digit j below m_j
-                const uint2 c = kInvShared ? inv[j * N + i]
-                                           : make_uint2(__ldg(C.mrc_inv + j * N + i), __ldg(C.mrc_inv_sh + j * N + i));
+                const uint2 c = inv[j * N + i];
                 v = mulmod_shoup(submod(v, t, m), c.x, c.y, m);
             }
             col[i * kMrcBlock] = v;
@@ -142,13 +130,14 @@ static grns_status run_mrc(const grns_ctx *c, const uint32_t *x, int64_t ld, int
         k_mrc_warp<N><<<grid_for(c, (count + P - 1) / P * 32, kMrcBlock, 16), kMrcBlock, 0, s>>>(
             consts_of<N>(c), Operand<N>{x, ld}, count, Output<N>{out, ld}, flags);
         return cuda_status(cudaGetLastError());
+    } else {  // one number per thread, the inverses staged in shared memory (n^2 8-byte entries)
+        const size_t smem = (size_t)N * N * sizeof(uint2) + (size_t)N * kMrcBlock * 4;
+        static std::atomic<int> per_sm[kOccDevices];  // resident blocks per SM, per device
+        const int occ = resident_blocks(per_sm, c, k_mrc<N>, kMrcBlock, smem);
+        k_mrc<N><<<grid_for(c, count, kMrcBlock, occ), kMrcBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld},
+                                                                              count, Output<N>{out, ld}, flags);
+        return cuda_status(cudaGetLastError());
     }
-    const size_t smem = (mrc_inv_shared<N>() ? (size_t)N * N * sizeof(uint2) : 0) + (size_t)N * kMrcBlock * 4;
-    static std::atomic<int> per_sm[kOccDevices];  // resident blocks per SM, per device
-    const int occ = resident_blocks(per_sm, c, k_mrc<N>, kMrcBlock, smem);
-    k_mrc<N><<<grid_for(c, count, kMrcBlock, occ), kMrcBlock, smem, s>>>(consts_of<N>(c), Operand<N>{x, ld}, count,
-                                                                          Output<N>{out, ld}, flags);
-    return cuda_status(cudaGetLastError());
 }
 
 }  // namespace grns
