@@ -67,8 +67,7 @@ struct Part {  // max: best of one chunk
  * one: [DivK table][ScK table][warps' counters][columns of 3n words] */
 template <int N>
 struct BatchCfg {
-    /* one warp a block above 64 moduli: the division columns take 3n words a thread */
-    static constexpr int kBlock = N > 64 ? 32 : N > 32 ? 128 : 256;
+    static constexpr int kBlock = N > 32 ? 128 : 256;
     static constexpr int kMinBlocks = 2;
     static constexpr size_t kTables = (sizeof(DivK) + sizeof(ScK)) * N;
     static constexpr size_t kHeavySmem = kTables + (size_t)(kBlock / 32) * kDivBins * 4 + (size_t)3 * N * 4 * kBlock;
@@ -408,20 +407,35 @@ struct grns_batch {
 
 namespace grns {
 
+/* the kernel is built for up to kBatchMaxModuli moduli (batches of larger
+ * sets are refused at creation) */
 template <int N>
 grns_status launch_batch_kernel(grns_batch *b, cudaStream_t s) {
-    k_batch<N><<<b->grid, BatchCfg<N>::kBlock, b->smem, s>>>(consts_of<N>(b->ctx), b->d_jobs, b->njobs, b->total_chunks,
-                                              b->d_counter, b->d_done, b->d_parts, b->smem ? 1 : 0);
-    return cuda_status(cudaGetLastError());
+    if constexpr (N > kBatchMaxModuli) {
+        (void)b;
+        (void)s;
+        return GRNS_ERR_UNSUPPORTED;
+    } else {
+        k_batch<N><<<b->grid, BatchCfg<N>::kBlock, b->smem, s>>>(consts_of<N>(b->ctx), b->d_jobs, b->njobs,
+                                                                 b->total_chunks, b->d_counter, b->d_done, b->d_parts,
+                                                                 b->smem ? 1 : 0);
+        return cuda_status(cudaGetLastError());
+    }
 }
 
 template <int N>
 int occupancy_blocks(size_t smem) {
-    if (BatchCfg<N>::kHeavySmem > 48 * 1024)  // per device: set on every shape computation
-        cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BatchCfg<N>::kHeavySmem);
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, BatchCfg<N>::kBlock, smem);
-    return nb > 0 ? nb : 1;
+    if constexpr (N > kBatchMaxModuli) {
+        (void)smem;
+        return 1;
+    } else {
+        if (BatchCfg<N>::kHeavySmem > 48 * 1024)  // per device: set on every shape computation
+            cudaFuncSetAttribute(k_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)BatchCfg<N>::kHeavySmem);
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<N>, BatchCfg<N>::kBlock, smem);
+        return nb > 0 ? nb : 1;
+    }
 }
 
 /* the per-count entry points: extern here, instantiated for this unit's counts */
@@ -593,6 +607,7 @@ namespace grns {
 size_t batch_staging_bytes(int njobs) { return sizeof(JobDev) * (size_t)(njobs > 0 ? njobs : 1); }
 
 grns_status batch_run_async(grns_ctx *c, const grns_job *jobs, int njobs, void *staging, cudaStream_t s) {
+    if (c->n > kBatchMaxModuli) return GRNS_ERR_UNSUPPORTED;
     NvtxRange range("grns batch_run");
     grns_batch b;
     b.ctx = c;
@@ -655,6 +670,7 @@ grns_status grns_ctx_set_schedule(grns_ctx *c, int op, const grns_schedule *s) {
 grns_status grns_batch_create(grns_ctx *c, const grns_job *jobs, int njobs, int use_graph, grns_batch **out) {
     if (!c || !out || njobs < 0 || (njobs > 0 && !jobs)) return GRNS_ERR_INVALID_ARGUMENT;
     *out = nullptr;
+    if (c->n > grns::kBatchMaxModuli) return GRNS_ERR_UNSUPPORTED;
     for (int t = 0; t < njobs; t++)
         if (!job_ok(c, jobs[t])) return GRNS_ERR_INVALID_ARGUMENT;
     grns_batch *b = new (std::nothrow) grns_batch();

@@ -145,7 +145,7 @@ grns_status grns_gen_divisors(grns_ctx *c, uint64_t seed, int64_t count, int lay
 }
 
 grns_status grns_gen_mpint(grns_ctx *c, uint64_t seed, int64_t count, int bits, void *out, void *s) {
-    if (!c || !out || count < 0 || bits < 1 || bits > 32 * 64) return GRNS_ERR_INVALID_ARGUMENT;
+    if (!c || !out || count < 0 || bits < 1 || bits > 32 * grns::kMaxModuli) return GRNS_ERR_INVALID_ARGUMENT;
     if (count == 0) return GRNS_OK;
     const uint64_t km = stream_key(seed, S_MAG), ks = stream_key(seed, S_SIGN);
 #define C_(n)                                                                                                   \

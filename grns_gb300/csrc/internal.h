@@ -63,6 +63,10 @@ inline const Consts<N> &consts_of(const grns_ctx *c) {
 
 constexpr uint64_t kPoolKeepBytes = 256ull << 20;
 
+/* the batched kernel (and so the server and the autotuner) serves moduli sets
+ * of up to 64 moduli; the plain calls cover 128 and 256 */
+constexpr int kBatchMaxModuli = 64;
+
 /* an NVTX range over a host-side scope (batched launches, served launches,
  * host-buffer calls): visible in Nsight timelines, a no-op without a tool */
 struct NvtxRange {

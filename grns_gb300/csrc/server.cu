@@ -531,6 +531,7 @@ grns_status grns_server_destroy(grns_server *sv) {
 
 grns_status grns_server_add_context(grns_server *sv, grns_ctx *c, int *index) {
     if (!sv || !c || !index) return GRNS_ERR_INVALID_ARGUMENT;
+    if (c->n > grns::kBatchMaxModuli) return GRNS_ERR_UNSUPPORTED;  // requests run in the batched kernel
     std::lock_guard<std::mutex> g(sv->mu);
     sv->ctxs.push_back(c);
     *index = (int)sv->ctxs.size() - 1;

@@ -41,6 +41,7 @@ extern "C" {
 grns_status grns_autotune(grns_ctx *c, int op, int64_t count, const char *cache_path, grns_schedule *chosen,
                           double *best_ms) {
     if (!c || op < GRNS_OP_EVAL || op > GRNS_OP_MPINT_MUL || count <= 0) return GRNS_ERR_INVALID_ARGUMENT;
+    if (c->n > grns::kBatchMaxModuli) return GRNS_ERR_UNSUPPORTED;
     const int n = c->n;
     const bool mp = op >= GRNS_OP_MPINT_ADD;
     const size_t num_bytes = mp ? GRNS_MPINT_BYTES(n) : (size_t)n * 4;

@@ -316,6 +316,9 @@ typedef struct {
 } grns_job;
 
 typedef struct grns_batch grns_batch;
+/* contexts of up to 64 moduli (GRNS_ERR_UNSUPPORTED above; the plain calls
+ * cover 128 and 256); the same holds for grns_autotune and
+ * grns_server_add_context, whose requests run in this kernel */
 grns_status grns_batch_create(grns_ctx *ctx, const grns_job *jobs, int njobs, int use_graph, grns_batch **out);
 /* new pointers for the same job shapes (op, count, layout); keeps the graph.
  * The job table is copied synchronously from the host: call it once the
@@ -448,7 +451,8 @@ grns_status grns_server_set_gather_us(grns_server *srv, int32_t gather_us);
  *   grns_gen_divisors: divisors of bit length L, L uniform in [1, log2 M]
  *   grns_gen_shifts  : exponents uniform in [1, dmax]
  *   grns_gen_mpint   : mp_int_t records of signed integers, magnitude uniform in
- *                      [0, 2^bits), fair-coin sign, interval evaluation filled */
+ *                      [0, 2^bits) (1 <= bits <= 8192), fair-coin sign, interval
+ *                      evaluation filled */
 grns_status grns_gen_uniform(grns_ctx *ctx, uint64_t seed, uint32_t stream, int64_t count, int layout, int32_t *out,
                              void *cuda_stream);
 grns_status grns_gen_divisors(grns_ctx *ctx, uint64_t seed, int64_t count, int layout, int32_t *out, void *cuda_stream);
